@@ -1,0 +1,318 @@
+#!/usr/bin/env python
+"""Benchmark: explicit Cahn-Hilliard, [0,64]^3, 64^3 cells, FE_Q degree 2, periodic, FP64.
+
+One step = one increment of the application's solve loop: the c block (c from old c and
+grad old mu) then the mu block (mu from c and grad c), each an explicit solve
+u = invM (.) A_rhs followed by the constraints. Metric: DoF-updates/s = 2 N per step
+(N = 129^3 lattice DoFs per field, periodic images included as deal.II keeps them).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device time with the state resident in HBM (per-step CUDA events on the
+engine's stream, L2 flushed between steps). `e2e` is the same metric through the public C
+ABI with the step's inputs uploaded from pinned host memory and its result downloaded every
+step. `--impl reference` times the CPU restatement of the reference algorithm (the oracle;
+the reference itself needs deal.II/MPI/p4est, which neither machine has) on all host cores.
+Under torchrun each rank runs an independent replica (replicas only: an explicit step of
+one simulation is not sharded); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DoF-updates/s (explicit Cahn-Hilliard Q2 3-D step, FP64)"
+UNIT = "DoF-updates/s"
+WORKLOAD = dict(refine=6, degree=2, size=64.0, dt=1e-4)
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "cahn_hilliard_3d explicit, [0,64]^3, 64^3 cells, FE_Q(2) on GL points, periodic, "
+                       "dt=1e-4, M=1, kappa=1.5, f=c^2(1-c)^2, c0=0.5+0.05U(-1,1)",
+           "dofs_per_field": 129 ** 3, "fields_updated_per_step": 2, "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d.get("hbm_gbs") or d.get("hbm_GBs") or 6800.0), "of measured"
+        except Exception:
+            pass
+    return 6800.0, "of fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for r in csv.reader(f):
+                    if len(r) >= 9:
+                        rows.append([x.strip() for x in r])
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cell_flops_per_step(degree=2, dim=3):
+    """Algorithmic FP64 flops of one CH step per cell (sum factorisation + pointwise).
+
+    per block: gradient of one field (dim*nq*n FMA) + integration of the gradient term
+    (dim*nq*n FMA) + JxW scaling of value (nq) and gradient terms (dim*nq) + the callback
+    (c block: 4 flops/q; mu block: 8 flops/q). FMA counts 2.
+    """
+    n = degree + 1
+    nq = n ** dim
+    sf = 2 * (2 * dim * nq * n) + nq + dim * nq
+    return (sf + 4 * nq) + (sf + 8 * nq)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle
+    from phasefield_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    wl = W.cahn_hilliard_3d(**WORKLOAD)
+    o = pyoracle.Oracle(wl, threads=threads)
+    o.run(0)
+    inc = 1
+    for _ in range(args.warmup):
+        o.run(inc)
+        inc += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run(inc)
+        inc += 1
+    dt = time.perf_counter() - t0
+    N = 129 ** 3
+    value = 2 * N * args.steps / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": workload_config({"parallelism": "host threads (OpenMP)"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of the workload"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline_sample(budget_s=12.0):
+    from oracle import pyoracle
+    from phasefield_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    wl = W.cahn_hilliard_3d(**WORKLOAD)
+    o = pyoracle.Oracle(wl, threads=threads)
+    o.run(0)
+    o.run(1)  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.run(2 + steps)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= 200:
+            break
+    N = 129 ** 3
+    return {"value": 2 * N * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} full steps of the workload on {threads} threads ({el:.1f} s)"}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from phasefield_gb300 import build as pbuild
+    if rank == 0:
+        pbuild.build()
+    if ws > 1:
+        dist.barrier()
+    from phasefield_gb300 import capi
+    from phasefield_gb300 import workloads as W
+    lib = capi.load()
+
+    wl = W.cahn_hilliard_3d(**WORKLOAD)
+    p = wl.make_problem()
+    N = p.n_nodes
+    stream = torch.cuda.current_stream(dev)
+    lib.ppf_set_stream(p.h, C.c_void_p(stream.cuda_stream))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    p.solve(0)  # increment 0: initial condition + mu block
+    inc = 1
+    for _ in range(args.warmup):
+        p.solve(inc)
+        inc += 1
+    torch.cuda.synchronize()
+
+    # ---- device-timed steps ----
+    lib.ppf_kernel_stats_reset(p.h)
+    lib.ppf_kernel_timing(p.h, 1)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            p.solve(inc)
+            evs[k][1].record(stream)
+            inc += 1
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(step_ms))
+    cell_ms = C.c_double()
+    cell_n, all_n = C.c_longlong(), C.c_longlong()
+    lib.ppf_kernel_stats(p.h, C.byref(cell_ms), C.byref(cell_n), C.byref(all_n))
+    lib.ppf_kernel_timing(p.h, 0)
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    dof_updates = 2 * N * args.steps * ws
+    value = dof_updates / (max_ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers ----
+    pin = [torch.empty(N, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+    for f in (0, 1):
+        p.lib.ppf_download_state(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0)
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        for f in (0, 1):  # inputs of this step: old c and old mu
+            rc = lib.ppf_upload_state(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0)
+            assert rc == 0
+        p.solve(inc)
+        inc += 1
+        for f in (0, 1):  # results of this step
+            rc = lib.ppf_download_state(p.h, f, 1, C.cast(pin[2 + f].data_ptr(), C.POINTER(C.c_double)), 0)
+            assert rc == 0
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": 2 * N * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N,
+           "d2h_bytes_per_step": 2 * 8 * N}
+
+    if rank == 0:
+        peak, peak_src = measured_peaks()
+        avg_launch_s = cell_ms.value * 1e-3 / max(cell_n.value, 1)
+        bytes_per_launch = 20 * N  # c block 24N (read c_old, mu_old, write c), mu block 16N: mean 20N
+        achieved = bytes_per_launch / avg_launch_s / 1e9
+        fp64_peak = C.c_double()
+        lib.ppf_device_fp64_peak(C.byref(fp64_peak))
+        ncells = 64 ** 3
+        flops_per_launch = cell_flops_per_step() * ncells / 2
+        fp64_achieved = flops_per_launch / avg_launch_s / 1e12
+        cpu = cpu_baseline_sample()
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
+                "e2e": e2e, "gpu_launches": int(all_n.value), "clocks": clk.summary(),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                             "kernel": "cell_kernel<CahnHilliard<3,2>>", "bytes_per_launch": bytes_per_launch,
+                             "avg_launch_ms": avg_launch_s * 1e3},
+                "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
+                                  "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
+                                  "flops_per_launch": flops_per_launch, "peak_source": "measured in this run"},
+                "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    p.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,178 @@
+/*
+ * ppf_gb300.h — C ABI of the GB300 matrix-free operator-evaluation engine.
+ *
+ * Plain C: opaque handle, plain pointers and sizes, int status codes. No C++ or torch types
+ * cross this boundary. Every entry point names the PRISMS-PF interface it replaces (paths
+ * are inside prisms-center/phaseField).
+ *
+ * Vectors exchanged through this ABI are FP64. Their ordering is chosen per call:
+ *   PPF_ORDER_LATTICE  lattice order: node (I,J,K) of the (k*Cx+1)x(k*Cy+1)x(k*Cz+1) node
+ *                      lattice at index I + NX*(J + NY*K); vector fields component-major
+ *                      (component c occupies [c*N, (c+1)*N)). Periodic images are kept,
+ *                      as deal.II keeps periodic slave DoFs in the vector.
+ *   PPF_ORDER_DEALII   the DoF numbering deal.II's DoFHandler::distribute_dofs produces for
+ *                      the same mesh (cells in refinement order; per cell vertices, lines,
+ *                      quads, hex interior; FESystem components per object).
+ *
+ * Threading: a handle is not thread-safe; it owns one CUDA stream. Errors never throw:
+ * every call returns PPF_OK or a PPF_ERR_* code, and ppf_last_error() gives the message.
+ */
+#ifndef PPF_GB300_H
+#define PPF_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPF_MAX_FIELDS 8
+#define PPF_MAX_BLOCKS 8
+#define PPF_NAGE 6 /* dependency ages: current, old_1..old_4, src */
+
+enum ppf_status {
+  PPF_OK = 0,
+  PPF_ERR_ARG = 1,          /* invalid argument */
+  PPF_ERR_NAN = 2,          /* non-finite value after a solve (problem.cc:455-469 exit status 2) */
+  PPF_ERR_CUDA = 3,         /* CUDA runtime error */
+  PPF_ERR_NOCONV = 4,       /* linear solver did not converge (linear_solver.h:382-391) */
+  PPF_ERR_DEPENDENCY = 5,   /* callback read an undeclared dependency (field_container.h:603-632) */
+  PPF_ERR_UNSUPPORTED = 6,  /* configuration outside what this build implements */
+  PPF_ERR_TIMEOUT = 7       /* a bounded device-side wait gave up */
+};
+
+enum ppf_ordering { PPF_ORDER_LATTICE = 0, PPF_ORDER_DEALII = 1 };
+
+/* dependency flags (dependencies.h:134-213: values, grad(), hess()/lap()/hessdiag()) */
+enum ppf_dep_flag { PPF_DEP_VALUE = 1, PPF_DEP_GRADIENT = 2, PPF_DEP_HESSIAN = 4 };
+
+/* solve types / timings, same values as type_enums.h SolveType and solve_block.h SolveTiming */
+enum ppf_solve_type { PPF_CONSTANT = 0, PPF_EXPLICIT = 1, PPF_LINEAR = 2, PPF_NEWTON = 3 };
+enum ppf_solve_timing { PPF_PRIMARY = 0, PPF_SECONDARY = 1, PPF_POSTPROCESS = 2, PPF_NUCLEATION_RATE = 3 };
+
+typedef struct ppf_handle_s* ppf_handle;
+
+/* RectangularMesh + global refinement (spatial_discretization.cc:133-177,
+ * triangulation_manager.cc:107-118): subdivided hyper-rectangle refined `global_refinement`
+ * times; boundary ids x-=0, x+=1, y-=2, y+=3, z-=4, z+=5. */
+typedef struct {
+  int dim;                 /* 2 or 3 */
+  int degree;              /* FE_Q degree 1..4 on Gauss-Lobatto points (system_wide.h:40-61) */
+  int subdivisions[3];
+  double lower[3];
+  double size[3];
+  int global_refinement;
+  int periodic[3];         /* periodic directions (pairs 2d <-> 2d+1) */
+} ppf_mesh_desc;
+
+/* FieldAttributes + boundary conditions (field_attributes.h, constraint_parameters.cc:41-107).
+ * dirichlet[c][b] != 0 makes component c Dirichlet on boundary id b with value
+ * dirichlet_value[c][b] (the value set_dirichlet returns there; constant per face). */
+typedef struct {
+  int rank;                /* 0 scalar, 1 vector */
+  int dirichlet[3][6];
+  double dirichlet_value[3][6];
+} ppf_field_desc;
+
+/* SolveBlock (solve_block.h:56-127) with its dependency sets as flag tables:
+ * dep_rhs[f][age] / dep_lhs[f][age] = OR of ppf_dep_flag, ages in the order
+ * current, old_1, old_2, old_3, old_4, src (make_dependency_set result). */
+typedef struct {
+  int id;
+  int solve_type;
+  int solve_timing;
+  int n_fields;
+  int field_indices[PPF_MAX_FIELDS];
+  unsigned char dep_rhs[PPF_MAX_FIELDS][PPF_NAGE];
+  unsigned char dep_lhs[PPF_MAX_FIELDS][PPF_NAGE];
+} ppf_block_desc;
+
+/* Build the system once on the host and upload it: mesh, lattice/DoF maps, constraint maps,
+ * inverse lumped mass, per-block cell tables (replaces Problem::init_system,
+ * problem.cc:229-338). `model` names a compiled PDE operator set ("allen_cahn",
+ * "cahn_hilliard", "eshelby", "coupled_acch"); `constants` are its Model constants in the
+ * order that operator documents. */
+int ppf_create(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields,
+               const ppf_block_desc* blocks, int n_blocks, const char* model,
+               const double* constants, int n_constants, double dt, ppf_handle* out);
+void ppf_destroy(ppf_handle h);
+const char* ppf_last_error(ppf_handle h);
+
+/* sizes: lattice nodes per component, vector length of field f, cell count */
+long long ppf_n_nodes(ppf_handle h);
+long long ppf_field_length(ppf_handle h, int field);
+long long ppf_n_cells(ppf_handle h);
+
+/* deal.II DoF numbering of the scalar (rank 0) or vector (rank 1) handler as a map
+ * dealii_index -> lattice index (dof_manager.cc:12-26). `out` has field_length entries. */
+int ppf_dof_map(ppf_handle h, int rank, long long* out);
+
+/* Constraint map of field f in lattice order: master index (>=0, itself when unconstrained)
+ * or -1-j for the j-th Dirichlet row (constraint_manager.cc:258-304 after close()). */
+int ppf_constraint_map(ppf_handle h, int field, int* out);
+
+/* Inverse lumped mass of a scalar field in lattice order (invm_manager.h:121-239). */
+int ppf_invm(ppf_handle h, double* out);
+
+/* Field state I/O (GroupSolutionHandler current/old vectors). age 0 = current, 1..4 = old_k. */
+int ppf_upload_state(ppf_handle h, int field, int age, const double* host, int ordering);
+int ppf_download_state(ppf_handle h, int field, int age, double* host, int ordering);
+
+/* Apply the constraints of field f to its current vector (AffineConstraints::distribute,
+ * group_solution_handler.cc:339-353). */
+int ppf_apply_constraints(ppf_handle h, int field);
+
+/* Increment loop of Problem::solve (problem.cc:341-557): runs increments from the current
+ * one up to and including n_increments. Increment 0 applies the initial condition of
+ * Primary blocks (uploaded beforehand) and solves Secondary blocks; PostProcess blocks run
+ * on increments divisible by output_every (never when output_every <= 0). */
+int ppf_run(ppf_handle h, unsigned int n_increments, int output_every);
+
+/* One explicit solve of block index b (ExplicitSolver::solve_impl, explicit_solver.h:63-77). */
+int ppf_solve_block(ppf_handle h, int b);
+
+/* Operator apply of block b on host vectors (MFOperator::compute_operator / vmult,
+ * mf_operator.cc:17-32, 304-310). which: 0 rhs (compute_rhs, plain reads), 1 lhs
+ * (compute_lhs, src read with homogeneous constraints). src/dst: block fields concatenated
+ * in block order, lattice order. scale: 0 none, 1 invM, 2 invM^(1/2). */
+int ppf_apply(ppf_handle h, int b, int which, const double* src, double* dst, int scale);
+
+/* Same on device pointers (no host copies); stream-ordered on the handle's stream. */
+int ppf_apply_device(ppf_handle h, int b, int which, const double* d_src, double* d_dst, int scale);
+
+/* SimulationTimer state (simulation_timer.h). */
+int ppf_set_time(ppf_handle h, unsigned int increment, double time);
+int ppf_get_time(ppf_handle h, unsigned int* increment, double* time);
+
+/* Capture the explicit increment loop in a CUDA graph (on by default for ppf_run). */
+int ppf_set_use_graph(ppf_handle h, int on);
+
+/* Device pointer of a field state (for zero-copy callers), valid until the next rotation. */
+int ppf_state_device_ptr(ppf_handle h, int field, int age, double** out);
+
+/* Wait for all work queued on the handle's stream. */
+int ppf_synchronize(ppf_handle h);
+
+/* Run the handle's work on a caller-owned CUDA stream (a cudaStream_t passed as void*;
+ * NULL restores the handle's own stream). No counterpart in the reference, which has no
+ * device streams. */
+int ppf_set_stream(ppf_handle h, void* stream);
+
+/* Kernel timing for roofline measurements: while enabled, every cell-kernel launch is
+ * bracketed by CUDA events on its stream. ppf_kernel_stats returns the summed event time
+ * (ms) and launch count since the last reset, plus the launches of all engine kernels
+ * (cell, finalize, vector kernels) issued since the last reset. Replaces the reference's
+ * Timer::Scope sections (utilities/timer.cc:114-143) for the device path. */
+int ppf_kernel_timing(ppf_handle h, int enable);
+int ppf_kernel_stats(ppf_handle h, double* cell_ms, long long* cell_launches, long long* all_launches);
+int ppf_kernel_stats_reset(ppf_handle h);
+
+/* Measures the current GPU's FP64 FMA throughput (TFLOP/s, FMA = 2 flops) with a
+ * register-resident FMA loop; the denominator of FP64 roofline fractions. */
+int ppf_device_fp64_peak(double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPF_GB300_H */

@@ -1,0 +1,381 @@
+// Device-side FieldContainer: the variable container through which a user callback reads
+// dependency values/gradients/hessians and submits value and gradient terms at one
+// quadrature point. Same member names, template parameters and meaning as the reference
+// (include/prismspf/core/field_container.h:44-586, getters :1065-1256, setters :1258-1314).
+//
+// GB300 design: one CUDA thread owns one (cell, quadrature point). With Gauss-Lobatto
+// collocation the quadrature points are the cell nodes, so values are the gathered nodal
+// values and gradients are one 1-D derivative contraction per direction over the node line
+// through the point. Nodal values live in shared memory (written by the cell kernel's
+// gather); getters contract them on demand, so only what a callback actually asks for is
+// computed. Submitted terms are stored pre-multiplied by the integration weights
+// (JxW for values, JxW/h_d for gradient component d) for the kernel's integrate step.
+#pragma once
+
+#include <prismspf/config.h>
+#include <prismspf/core/simulation_timer.h>
+#include <prismspf/core/type_enums.h>
+#include <prismspf/dealii_shim.h>
+
+#include <type_traits>
+
+PRISMS_PF_BEGIN_NAMESPACE
+
+namespace gpu {
+
+constexpr int MAX_FIELDS = 8;
+constexpr int NAGE = 6;  // current, old_1..old_4, src
+constexpr int MAX_SLOTS = 8;
+constexpr int MAX_OUTS = 4;
+constexpr int MAX_N = 5;  // up to degree 4
+
+enum ErrorBits : int {
+  ERR_UNDECLARED_DEPENDENCY = 1,
+  ERR_UNDECLARED_SUBMISSION = 2,
+  ERR_NONFINITE = 4,
+};
+
+PPF_HD constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
+
+PPF_HD constexpr int age_of(DependencyType t) { return t == SRC ? 5 : (t >= Current ? int(t) : -1); }
+
+// Per-launch tables staged in shared memory by the cell kernel (sized for one dim/degree).
+template <int dim, int degree>
+struct CellTables {
+  static constexpr int n = degree + 1;
+  static constexpr int nq = ipow(n, dim);
+  double Dh[dim][n][n];   // D[q][j] / h_d: derivative of basis j at GL node q, direction d
+  double D2h[dim][n][n];  // (D D)[q][j] / h_d^2
+  double Dt[n][n];        // Dt[i][j] = D[j][i] (integration uses the transposed derivative)
+  double jxw[nq];         // JxW per quadrature point
+  double jxw_ih[dim][nq]; // JxW/h_d per quadrature point
+  double lo[3], h[3], gl_x[n];
+  double vol;
+  signed char slot_of[MAX_FIELDS][NAGE];  // dependency slot of (field, age), -1 if undeclared
+  signed char slot_comp0[MAX_SLOTS];      // first value row of a slot
+  signed char out_of[MAX_FIELDS];         // output index of a block field, -1 if not in block
+  signed char out_row0[MAX_OUTS];         // first output row (per comp: value, then dim grads)
+};
+
+template <int dim, int degree>
+struct CellCtx {
+  static constexpr int n = degree + 1;
+  static constexpr int nq = ipow(n, dim);
+  const CellTables<dim, degree>* tab;
+  const double* vals;  // [row][stride]
+  double* outs;        // [row][stride]
+  int stride;          // cells_per_block * nq
+  int lc;              // cell within the thread block
+  int q;               // quadrature point (= node) within the cell
+  int cell[3];         // global cell coordinates
+  int* err;
+  int submitted;       // bit 2*o: value of output o submitted, bit 2*o+1: gradient
+};
+
+}  // namespace gpu
+
+template <unsigned int dim, unsigned int degree, typename number>
+class FieldContainer {
+ public:
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using VectorValue = dealii::Tensor<1, dim, ScalarValue>;
+
+  template <TensorRank Rank>
+  using Value = std::conditional_t<Rank == TensorRank::Scalar || dim == 1, ScalarValue,
+                                   dealii::Tensor<int(Rank), dim, ScalarValue>>;
+  template <TensorRank Rank>
+  using Gradient = dealii::Tensor<int(Rank) + 1, dim, ScalarValue>;
+  template <TensorRank Rank>
+  using Hessian = dealii::Tensor<int(Rank) + 2, dim, ScalarValue>;
+
+  static constexpr int n = degree + 1;
+  static constexpr unsigned int dofs_per_component = gpu::ipow(n, dim);
+
+  using Ctx = gpu::CellCtx<dim, degree>;
+
+  PPF_HD explicit FieldContainer(Ctx& c) : ctx(c) {}
+
+  PPF_HD unsigned int get_n_q_points() const { return dofs_per_component; }
+
+  // --- values -------------------------------------------------------------------------
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD Value<Rank> get_value(unsigned int field_index) const { return get_value<Rank>(field_index, type); }
+
+  template <TensorRank Rank>
+  PPF_HD Value<Rank> get_value(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    if constexpr (Rank == TensorRank::Scalar || dim == 1) {
+      return ScalarValue(row < 0 ? number(0) : nodal(row, ctx.q));
+    } else {
+      Value<Rank> v;
+      if (row >= 0)
+        for (int c = 0; c < int(dim); ++c) v[c] = nodal(row + c, ctx.q);
+      return v;
+    }
+  }
+
+  // --- gradients ----------------------------------------------------------------------
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD Gradient<Rank> get_gradient(unsigned int field_index) const { return get_gradient<Rank>(field_index, type); }
+
+  template <TensorRank Rank>
+  PPF_HD Gradient<Rank> get_gradient(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    Gradient<Rank> g;
+    if (row < 0) return g;
+    if constexpr (Rank == TensorRank::Scalar) {
+      for (int d = 0; d < int(dim); ++d) g[d] = deriv(row, d);
+    } else {
+      for (int c = 0; c < int(dim); ++c)
+        for (int d = 0; d < int(dim); ++d) g[c][d] = deriv(row + c, d);
+    }
+    return g;
+  }
+
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD dealii::SymmetricTensor<2, dim, ScalarValue> get_symmetric_gradient(unsigned int field_index) const {
+    static_assert(Rank == TensorRank::Vector, "Symmetric gradients are only available for vector fields");
+    return get_symmetric_gradient<Rank>(field_index, type);
+  }
+
+  template <TensorRank Rank>
+  PPF_HD dealii::SymmetricTensor<2, dim, ScalarValue> get_symmetric_gradient(unsigned int field_index,
+                                                                             DependencyType type) const {
+    const Gradient<Rank> g = get_gradient<Rank>(field_index, type);
+    dealii::SymmetricTensor<2, dim, ScalarValue> s;
+    for (int i = 0; i < int(dim); ++i) {
+      s.a[i][i] = g[i][i];
+      for (int j = i + 1; j < int(dim); ++j) {
+        ScalarValue v = number(0.5) * (g[i][j] + g[j][i]);
+        s.a[i][j] = v;
+        s.a[j][i] = v;
+      }
+    }
+    return s;
+  }
+
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD ScalarValue get_divergence(unsigned int field_index) const {
+    static_assert(Rank == TensorRank::Vector, "Divergences are only available for vector fields");
+    return get_divergence<Rank>(field_index, type);
+  }
+
+  template <TensorRank Rank>
+  PPF_HD ScalarValue get_divergence(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    ScalarValue s(number(0));
+    if (row < 0) return s;
+    for (int d = 0; d < int(dim); ++d) s += deriv(row + d, d);
+    return s;
+  }
+
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD dealii::Tensor<1, (dim == 2 ? 1 : dim), ScalarValue> get_curl(unsigned int field_index) const {
+    static_assert(Rank == TensorRank::Vector, "Curl is only available for vector fields");
+    return get_curl<Rank>(field_index, type);
+  }
+
+  template <TensorRank Rank>
+  PPF_HD dealii::Tensor<1, (dim == 2 ? 1 : dim), ScalarValue> get_curl(unsigned int field_index,
+                                                                      DependencyType type) const {
+    const Gradient<Rank> g = get_gradient<Rank>(field_index, type);
+    dealii::Tensor<1, (dim == 2 ? 1 : dim), ScalarValue> c;
+    if constexpr (dim == 2) {
+      c[0] = g[1][0] - g[0][1];
+    } else if constexpr (dim == 3) {
+      c[0] = g[2][1] - g[1][2];
+      c[1] = g[0][2] - g[2][0];
+      c[2] = g[1][0] - g[0][1];
+    }
+    return c;
+  }
+
+  // --- second derivatives -------------------------------------------------------------
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD Hessian<Rank> get_hessian(unsigned int field_index) const { return get_hessian<Rank>(field_index, type); }
+
+  template <TensorRank Rank>
+  PPF_HD Hessian<Rank> get_hessian(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    Hessian<Rank> H;
+    if (row < 0) return H;
+    if constexpr (Rank == TensorRank::Scalar) {
+      for (int d = 0; d < int(dim); ++d)
+        for (int e = d; e < int(dim); ++e) {
+          ScalarValue v = second(row, d, e);
+          H[d][e] = v;
+          H[e][d] = v;
+        }
+    } else {
+      for (int c = 0; c < int(dim); ++c)
+        for (int d = 0; d < int(dim); ++d)
+          for (int e = d; e < int(dim); ++e) {
+            ScalarValue v = second(row + c, d, e);
+            H[c][d][e] = v;
+            H[c][e][d] = v;
+          }
+    }
+    return H;
+  }
+
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD Gradient<Rank> get_hessian_diagonal(unsigned int field_index) const {
+    return get_hessian_diagonal<Rank>(field_index, type);
+  }
+
+  template <TensorRank Rank>
+  PPF_HD Gradient<Rank> get_hessian_diagonal(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    Gradient<Rank> g;
+    if (row < 0) return g;
+    if constexpr (Rank == TensorRank::Scalar) {
+      for (int d = 0; d < int(dim); ++d) g[d] = second(row, d, d);
+    } else {
+      for (int c = 0; c < int(dim); ++c)
+        for (int d = 0; d < int(dim); ++d) g[c][d] = second(row + c, d, d);
+    }
+    return g;
+  }
+
+  template <TensorRank Rank, DependencyType type>
+  PPF_HD Value<Rank> get_laplacian(unsigned int field_index) const { return get_laplacian<Rank>(field_index, type); }
+
+  template <TensorRank Rank>
+  PPF_HD Value<Rank> get_laplacian(unsigned int field_index, DependencyType type) const {
+    const int row = row_of(field_index, type);
+    if constexpr (Rank == TensorRank::Scalar || dim == 1) {
+      ScalarValue s(number(0));
+      if (row < 0) return s;
+      for (int d = 0; d < int(dim); ++d) s += second(row, d, d);
+      return s;
+    } else {
+      Value<Rank> v;
+      if (row < 0) return v;
+      for (int c = 0; c < int(dim); ++c) {
+        ScalarValue s(number(0));
+        for (int d = 0; d < int(dim); ++d) s += second(row + c, d, d);
+        v[c] = s;
+      }
+      return v;
+    }
+  }
+
+  // --- geometry -----------------------------------------------------------------------
+  PPF_HD dealii::Point<dim, ScalarValue> get_q_point_location() const {
+    dealii::Point<dim, ScalarValue> p;
+    int qq = ctx.q;
+    for (int d = 0; d < int(dim); ++d) {
+      const int a = qq % n;
+      qq /= n;
+      p[d] = ctx.tab->lo[d] + (number(ctx.cell[d]) + ctx.tab->gl_x[a]) * ctx.tab->h[d];
+    }
+    return p;
+  }
+
+  PPF_HD ScalarValue get_element_volume() const { return ScalarValue(ctx.tab->vol); }
+
+  // --- submissions --------------------------------------------------------------------
+  PPF_HD void set_value_term(unsigned int field_index, const ScalarValue& val) {
+    const int o = out_row(field_index);
+    if (o < 0) return;
+    ctx.outs[o * ctx.stride + slot()] = val.v * ctx.tab->jxw[ctx.q];
+    ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
+  }
+
+  PPF_HD void set_value_term(unsigned int field_index, const dealii::Tensor<1, dim, ScalarValue>& val) {
+    const int o = out_row(field_index);
+    if (o < 0) return;
+    for (int c = 0; c < int(dim); ++c) ctx.outs[(o + c * (1 + dim)) * ctx.stride + slot()] = val[c].v * ctx.tab->jxw[ctx.q];
+    ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
+  }
+
+  PPF_HD void set_gradient_term(unsigned int field_index, const dealii::Tensor<1, dim, ScalarValue>& g) {
+    const int o = out_row(field_index);
+    if (o < 0) return;
+    for (int d = 0; d < int(dim); ++d) ctx.outs[(o + 1 + d) * ctx.stride + slot()] = g[d].v * ctx.tab->jxw_ih[d][ctx.q];
+    ctx.submitted |= 2 << (2 * ctx.tab->out_of[field_index]);
+  }
+
+  PPF_HD void set_gradient_term(unsigned int field_index, const dealii::Tensor<2, dim, ScalarValue>& g) {
+    const int o = out_row(field_index);
+    if (o < 0) return;
+    for (int c = 0; c < int(dim); ++c)
+      for (int d = 0; d < int(dim); ++d)
+        ctx.outs[(o + c * (1 + dim) + 1 + d) * ctx.stride + slot()] = g[c][d].v * ctx.tab->jxw_ih[d][ctx.q];
+    ctx.submitted |= 2 << (2 * ctx.tab->out_of[field_index]);
+  }
+
+  PPF_HD void set_gradient_term(unsigned int field_index, const dealii::SymmetricTensor<2, dim, ScalarValue>& g) {
+    set_gradient_term(field_index, dealii::Tensor<2, dim, ScalarValue>(g));
+  }
+
+ private:
+  Ctx& ctx;
+
+  PPF_HD int slot() const { return ctx.lc * int(dofs_per_component) + ctx.q; }
+
+  PPF_HD int row_of(unsigned int field_index, DependencyType type) const {
+    const int age = gpu::age_of(type);
+    int s = -1;
+    if (field_index < unsigned(gpu::MAX_FIELDS) && age >= 0) s = ctx.tab->slot_of[field_index][age];
+    if (s < 0) {
+#ifdef __CUDA_ARCH__
+      atomicOr(ctx.err, int(gpu::ERR_UNDECLARED_DEPENDENCY));
+#endif
+      return -1;
+    }
+    return ctx.tab->slot_comp0[s];
+  }
+
+  PPF_HD int out_row(unsigned int field_index) const {
+    int o = field_index < unsigned(gpu::MAX_FIELDS) ? ctx.tab->out_of[field_index] : -1;
+    if (o < 0) {
+#ifdef __CUDA_ARCH__
+      atomicOr(ctx.err, int(gpu::ERR_UNDECLARED_SUBMISSION));
+#endif
+      return -1;
+    }
+    return ctx.tab->out_row0[o];
+  }
+
+  PPF_HD number nodal(int row, int q) const { return ctx.vals[row * ctx.stride + ctx.lc * int(dofs_per_component) + q]; }
+
+  // first derivative along direction d at this thread's quadrature point
+  PPF_HD number deriv(int row, int d) const {
+    int stride_d = 1;
+    for (int e = 0; e < d; ++e) stride_d *= n;
+    const int qd = (ctx.q / stride_d) % n;
+    const double* u = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
+    const double* Dr = ctx.tab->Dh[d][qd];
+    number s = Dr[0] * u[0];
+#pragma unroll
+    for (int j = 1; j < n; ++j) s = fma(Dr[j], u[j * stride_d], s);
+    return s;
+  }
+
+  // second derivative d/dx_d d/dx_e at this thread's quadrature point
+  PPF_HD number second(int row, int d, int e) const {
+    int sd = 1, se = 1;
+    for (int k = 0; k < d; ++k) sd *= n;
+    for (int k = 0; k < e; ++k) se *= n;
+    const int qd = (ctx.q / sd) % n, qe = (ctx.q / se) % n;
+    const double* base = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component);
+    if (d == e) {
+      const double* u = base + (ctx.q - qd * sd);
+      const double* Dr = ctx.tab->D2h[d][qd];
+      number s = 0;
+      for (int j = 0; j < n; ++j) s = fma(Dr[j], u[j * sd], s);
+      return s;
+    }
+    const double* u = base + (ctx.q - qd * sd - qe * se);
+    number s = 0;
+    for (int j = 0; j < n; ++j) {
+      number t = 0;
+      for (int k = 0; k < n; ++k) t = fma(ctx.tab->Dh[e][qe][k], u[j * sd + k * se], t);
+      s = fma(ctx.tab->Dh[d][qd][j], t, s);
+    }
+    return s;
+  }
+};
+
+PRISMS_PF_END_NAMESPACE

@@ -1,0 +1,1084 @@
+// ORACLE — test infrastructure only.
+//
+// CPU restatement (FP64, C++17, OpenMP) of the PRISMS-PF matrix-free operator-evaluation
+// path and of the deal.II pieces it calls. Only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / reference legs of bench.py may load this library; the product path never
+// does.
+//
+// Parity status: the reference (deal.II >= 9.6 + MPI + p4est) cannot be built here and its
+// own tests hold no golden vectors for this path, so this restatement is "parity unpinned"
+// against the reference binary. It is pinned instead by analytic known answers (constant
+// fields, mass conservation, discrete-Laplacian eigenvectors, patch tests) in tests/.
+//
+// What it restates, with the reference file each part follows (paths inside
+// prisms-center/phaseField):
+//   * GL support points and GL quadrature with degree+1 points (collocation)
+//       include/prismspf/core/system_wide.h:40-61
+//   * subdivided hyper-rectangle + refine_global, boundary ids 0..2d-1
+//       src/user_inputs/spatial_discretization.cc:133-161,
+//       src/core/triangulation_manager.cc:107-118
+//   * DoF numbering in deal.II distribute_dofs order (cells in refinement order, per cell:
+//     vertices, lines, quads, hex interior; FESystem component-major per object)
+//       src/core/dof_manager.cc:12-26
+//   * periodic + Dirichlet AffineConstraints with chain closing
+//       src/core/constraint_manager.cc:143-304, spatial_discretization.cc:95-120,165-177
+//   * lumped inverse mass with generic (periodic-only) constraints
+//       include/prismspf/core/invm_manager.h:121-239
+//   * cell loop: read_dof_values(_plain) -> evaluate -> user callback per q ->
+//     integrate -> distribute_local_to_global with condensed constraints
+//       src/solvers/mf_operator.cc:17-80, include/prismspf/core/field_container.h:794-882,
+//       include/prismspf/core/field_container.h:1258-1314
+//   * explicit solve  include/prismspf/solvers/explicit_solver.h:63-77
+//   * time loop order, increment-0 handling, age rotation
+//       src/core/problem.cc:341-557, include/prismspf/solvers/solver_base.h:103-131,
+//       src/core/group_solution_handler.cc:356-403
+//   * application callbacks: allen_cahn/explicit/custom_pde.h:72-101,
+//     cahn_hilliard/explicit/custom_pde.h:91-131,
+//     mechanics/eshelby_inclusion/custom_pde.h:55-92 (+ utilities/mechanics.h:39-109),
+//     coupled_allen_cahn_cahn_hilliard/custom_pde.h:63-176
+#include "oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+// ---------------------------------------------------------------------------------------
+// 1-D Gauss-Lobatto rule on [0,1] and the Lagrange derivative matrix at its points.
+// system_wide.h:40-61 uses FE_Q(QGaussLobatto<1>(degree+1)) and QGaussLobatto(degree+1).
+// ---------------------------------------------------------------------------------------
+struct GL {
+  int n = 0;
+  double x[8] = {};
+  double w[8] = {};
+  double D[8][8] = {};  // D[q][j] = d/dx L_j (x_q) on [0,1]
+};
+
+static double legendre(int n, double x, double* dp) {
+  double p0 = 1.0, p1 = x;
+  if (n == 0) { if (dp) *dp = 0; return 1.0; }
+  for (int k = 2; k <= n; ++k) {
+    double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    p0 = p1; p1 = p2;
+  }
+  if (dp) *dp = n * (x * p1 - p0) / (x * x - 1.0);
+  return p1;
+}
+
+static GL make_gl(int n) {
+  GL g; g.n = n;
+  const int N = n - 1;  // Legendre degree
+  std::vector<double> t(n);
+  t[0] = -1.0; t[n - 1] = 1.0;
+  // interior points: roots of P'_N, Newton from Chebyshev-Gauss-Lobatto guesses
+  for (int i = 1; i < n - 1; ++i) {
+    double x = -std::cos(M_PI * i / N);
+    for (int it = 0; it < 100; ++it) {
+      // f = P'_N(x), f' = P''_N(x) from the Legendre ODE
+      double dp; double p = legendre(N, x, &dp);
+      double d2p = (2.0 * x * dp - N * (N + 1.0) * p) / (1.0 - x * x);
+      double dx = dp / d2p;
+      x -= dx;
+      if (std::fabs(dx) < 1e-17) break;
+    }
+    t[i] = x;
+  }
+  std::sort(t.begin(), t.end());
+  for (int i = 0; i < n; ++i) {
+    double p = legendre(N, t[i], nullptr);
+    double w = 2.0 / (N * (N + 1.0) * p * p);
+    g.x[i] = 0.5 * (t[i] + 1.0);
+    g.w[i] = 0.5 * w;
+  }
+  // symmetrise the nodes exactly
+  for (int i = 0; i < n / 2; ++i) {
+    double a = 0.5 * (g.x[i] + (1.0 - g.x[n - 1 - i]));
+    g.x[i] = a; g.x[n - 1 - i] = 1.0 - a;
+    double w = 0.5 * (g.w[i] + g.w[n - 1 - i]);
+    g.w[i] = w; g.w[n - 1 - i] = w;
+  }
+  if (n % 2 == 1) g.x[n / 2] = 0.5;
+  // barycentric derivative matrix
+  double bw[8];
+  for (int j = 0; j < n; ++j) {
+    double p = 1.0;
+    for (int k = 0; k < n; ++k) if (k != j) p *= (g.x[j] - g.x[k]);
+    bw[j] = 1.0 / p;
+  }
+  for (int q = 0; q < n; ++q) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j) {
+      if (j == q) continue;
+      g.D[q][j] = (bw[j] / bw[q]) / (g.x[q] - g.x[j]);
+      diag -= g.D[q][j];
+    }
+    g.D[q][q] = diag;
+  }
+  return g;
+}
+
+// ---------------------------------------------------------------------------------------
+// AffineConstraints restatement: a constrained dof i has entries (j, w) and inhomogeneity.
+// close() substitutes constrained masters until every master is unconstrained.
+// ---------------------------------------------------------------------------------------
+struct Constraints {
+  std::vector<char> constrained;
+  std::vector<std::vector<std::pair<long, double>>> entries;
+  std::vector<double> inhom;
+  void reinit(long n) { constrained.assign(n, 0); entries.assign(n, {}); inhom.assign(n, 0.0); }
+  bool is_constrained(long i) const { return constrained[i] != 0; }
+  void add_line(long i) { constrained[i] = 1; entries[i].clear(); inhom[i] = 0.0; }
+  void close() {
+    const long n = (long)constrained.size();
+    for (int pass = 0; pass < 16; ++pass) {
+      bool changed = false;
+      for (long i = 0; i < n; ++i) {
+        if (!constrained[i]) continue;
+        std::vector<std::pair<long, double>> out;
+        double inh = inhom[i];
+        bool any = false;
+        for (auto& e : entries[i]) {
+          if (constrained[e.first]) {
+            any = true;
+            inh += e.second * inhom[e.first];
+            for (auto& f : entries[e.first]) out.push_back({f.first, e.second * f.second});
+          } else {
+            out.push_back(e);
+          }
+        }
+        if (any) {
+          std::sort(out.begin(), out.end());
+          std::vector<std::pair<long, double>> merged;
+          for (auto& e : out) {
+            if (!merged.empty() && merged.back().first == e.first) merged.back().second += e.second;
+            else merged.push_back(e);
+          }
+          entries[i] = merged; inhom[i] = inh; changed = true;
+        }
+      }
+      if (!changed) break;
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------------------
+// Mesh + DoF handlers
+// ---------------------------------------------------------------------------------------
+struct DofHandler {
+  int ncomp = 1;
+  long ndofs = 0;
+  std::vector<long> cell_dofs;            // [cell][comp][local lexicographic node]
+  std::vector<std::array<int, 4>> lattice;  // per dof: global lattice I,J,K and component
+};
+
+struct Mesh {
+  int dim = 2, k = 1, n = 2, nloc = 4;  // nloc = n^dim
+  int nc[3] = {1, 1, 1};
+  double lo[3] = {0, 0, 0}, len[3] = {1, 1, 1}, h[3] = {1, 1, 1};
+  int periodic[3] = {0, 0, 0};
+  long ncells = 0;
+  std::vector<std::array<int, 3>> cells;  // cell integer coordinates, deal.II order
+  GL gl;
+  DofHandler dh[2];  // [0] scalar FE_Q, [1] FESystem(FE_Q, dim)
+  int nnode[3] = {1, 1, 1};
+};
+
+// refine_global: children of a cell ordered lexicographically (x fastest), recursively.
+static void build_cells(Mesh& m, const int* subdiv, int refine) {
+  const int dim = m.dim;
+  const int f = 1 << refine;
+  for (int d = 0; d < 3; ++d) m.nc[d] = d < dim ? subdiv[d] * f : 1;
+  m.cells.clear();
+  const int nchild = 1 << dim;
+  // coarse cells lexicographic (subdivided_hyper_rectangle), then recursive children
+  for (int cz = 0; cz < (dim == 3 ? subdiv[2] : 1); ++cz)
+    for (int cy = 0; cy < subdiv[1]; ++cy)
+      for (int cx = 0; cx < subdiv[0]; ++cx) {
+        std::vector<std::array<int, 3>> cur{{cx, cy, cz}};
+        for (int r = 0; r < refine; ++r) {
+          std::vector<std::array<int, 3>> nxt;
+          nxt.reserve(cur.size() * nchild);
+          for (auto& c : cur)
+            for (int ch = 0; ch < nchild; ++ch)
+              nxt.push_back({2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
+                             dim == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0});
+          cur.swap(nxt);
+        }
+        for (auto& c : cur) m.cells.push_back(c);
+      }
+  m.ncells = (long)m.cells.size();
+}
+
+// The cell-local lattice offsets of the dofs on each geometric object, in deal.II
+// distribute_dofs_on_cell order: vertices (v = x + 2y + 4z), lines, quads, hex interior.
+// Line numbering (GeometryInfo): 2D: 0:x=0, 1:x=1, 2:y=0, 3:y=1. 3D: lines 0-3 on z=0 as in
+// 2D, 4-7 on z=1, 8-11 along z at (x,y)=(0,0),(1,0),(0,1),(1,1). Dofs inside a line run
+// from its lower to its upper vertex; face-interior dofs are lexicographic in the face's
+// two tangential directions (lower axis fastest). Only degree >= 3 depends on these two
+// within-object orders.
+struct LocalObject { std::vector<std::array<int, 3>> nodes; };
+
+static std::vector<LocalObject> local_objects(int dim, int k) {
+  std::vector<LocalObject> objs;
+  auto vtx = [&](int v) { return std::array<int, 3>{(v & 1) * k, ((v >> 1) & 1) * k, dim == 3 ? ((v >> 2) & 1) * k : 0}; };
+  const int nv = 1 << dim;
+  for (int v = 0; v < nv; ++v) objs.push_back({{vtx(v)}});
+  // lines: (fixed coords, running axis)
+  struct L { int axis; int a, b; };  // running axis, fixed values of the other two axes (in units of k)
+  std::vector<std::array<int, 4>> lines;  // {axis, fx, fy, fz} fixed positions (0/1) for non-running axes
+  if (dim == 2) {
+    lines = {{1, 0, 0, 0}, {1, 1, 0, 0}, {0, 0, 0, 0}, {0, 0, 1, 0}};
+  } else {
+    lines = {{1, 0, 0, 0}, {1, 1, 0, 0}, {0, 0, 0, 0}, {0, 0, 1, 0},
+             {1, 0, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 1}, {0, 0, 1, 1},
+             {2, 0, 0, 0}, {2, 1, 0, 0}, {2, 0, 1, 0}, {2, 1, 1, 0}};
+  }
+  for (auto& l : lines) {
+    LocalObject o;
+    for (int t = 1; t < k; ++t) {
+      std::array<int, 3> p{l[1] * k, l[2] * k, l[3] * k};
+      p[l[0]] = t;
+      o.nodes.push_back(p);
+    }
+    objs.push_back(o);
+  }
+  if (dim == 2) {
+    LocalObject o;
+    for (int b = 1; b < k; ++b)
+      for (int a = 1; a < k; ++a) o.nodes.push_back({a, b, 0});
+    objs.push_back(o);
+  } else {
+    for (int f = 0; f < 6; ++f) {
+      const int nax = f / 2, side = (f % 2) * k;
+      int t0 = nax == 0 ? 1 : 0;
+      int t1 = nax == 2 ? 1 : 2;
+      LocalObject o;
+      for (int b = 1; b < k; ++b)
+        for (int a = 1; a < k; ++a) {
+          std::array<int, 3> p{0, 0, 0};
+          p[nax] = side; p[t0] = a; p[t1] = b;
+          o.nodes.push_back(p);
+        }
+      objs.push_back(o);
+    }
+    LocalObject o;
+    for (int c = 1; c < k; ++c)
+      for (int b = 1; b < k; ++b)
+        for (int a = 1; a < k; ++a) o.nodes.push_back({a, b, c});
+    objs.push_back(o);
+  }
+  return objs;
+}
+
+static void distribute_dofs(Mesh& m, int which) {
+  DofHandler& d = m.dh[which];
+  const int dim = m.dim, k = m.k, n = m.n;
+  d.ncomp = which == 0 ? 1 : dim;
+  const int nc = d.ncomp;
+  const long NX = m.nnode[0], NY = m.nnode[1], NZ = m.nnode[2];
+  std::vector<long> node_first(NX * NY * NZ, -1);  // first dof index of a lattice node
+  auto objs = local_objects(dim, k);
+  d.cell_dofs.assign((size_t)m.ncells * nc * m.nloc, -1);
+  d.lattice.clear();
+  long next = 0;
+  for (long c = 0; c < m.ncells; ++c) {
+    const auto& cc = m.cells[c];
+    for (auto& o : objs) {
+      // an object is numbered at once for all its nodes and components (component-major)
+      bool fresh = true;
+      for (auto& p : o.nodes) {
+        long I = (long)cc[0] * k + p[0], J = (long)cc[1] * k + p[1], K = dim == 3 ? (long)cc[2] * k + p[2] : 0;
+        if (node_first[(K * NY + J) * NX + I] >= 0) { fresh = false; break; }
+      }
+      if (o.nodes.empty() || !fresh) continue;
+      const long npts = (long)o.nodes.size();
+      long base = next;
+      for (long t = 0; t < npts; ++t) {
+        auto& p = o.nodes[t];
+        long I = (long)cc[0] * k + p[0], J = (long)cc[1] * k + p[1], K = dim == 3 ? (long)cc[2] * k + p[2] : 0;
+        node_first[(K * NY + J) * NX + I] = base + t;  // component 0 dof of this node
+      }
+      for (int comp = 0; comp < nc; ++comp)
+        for (long t = 0; t < npts; ++t) {
+          auto& p = o.nodes[t];
+          d.lattice.push_back({cc[0] * k + p[0], cc[1] * k + p[1], dim == 3 ? cc[2] * k + p[2] : 0, comp});
+        }
+      next += npts * nc;
+    }
+  }
+  d.ndofs = next;
+  // node -> dof of component comp: node_first + comp * npts(object). Recover via lattice.
+  std::vector<long> comp_dof((size_t)NX * NY * NZ * nc, -1);
+  for (long i = 0; i < d.ndofs; ++i) {
+    auto& L = d.lattice[i];
+    comp_dof[(((long)L[2] * NY + L[1]) * NX + L[0]) * nc + L[3]] = i;
+  }
+  for (long c = 0; c < m.ncells; ++c) {
+    const auto& cc = m.cells[c];
+    for (int comp = 0; comp < nc; ++comp)
+      for (int l = 0; l < m.nloc; ++l) {
+        int a = l % n, b = (l / n) % n, e = dim == 3 ? l / (n * n) : 0;
+        long I = (long)cc[0] * k + a, J = (long)cc[1] * k + b, K = (long)cc[2] * k + e;
+        if (dim == 2) K = 0;
+        d.cell_dofs[((size_t)c * nc + comp) * m.nloc + l] = comp_dof[((K * NY + J) * NX + I) * nc + comp];
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Problem: fields, constraints, states, blocks, model callback.
+// ---------------------------------------------------------------------------------------
+enum { DEP_VALUE = 1, DEP_GRAD = 2, DEP_HESS = 4 };
+enum { AGE_CURRENT = 0, AGE_OLD1 = 1, AGE_OLD2 = 2, AGE_OLD3 = 3, AGE_OLD4 = 4, AGE_SRC = 5 };
+constexpr int NAGE = 6;
+
+struct Field {
+  int rank = 0;  // 0 scalar, 1 vector
+  // dirichlet[comp][boundary_id] = {is_dirichlet, value}
+  int dir_on[3][6] = {};
+  double dir_val[3][6] = {};
+  Constraints cons;
+  std::vector<double> cur;
+  std::vector<double> old[4];
+  int n_old = 0;
+};
+
+struct Block {
+  int id = 0, solve_type = 1, timing = 0;
+  std::vector<int> fields;
+  std::vector<std::array<int, NAGE>> dep_rhs, dep_lhs;  // [field][age] flags
+};
+
+struct Model;
+
+struct Problem {
+  Mesh m;
+  std::vector<Field> fields;
+  std::vector<Block> blocks;
+  Constraints generic[2];
+  std::vector<double> jxw[2], invm[2], invm_sqrt[2];
+  double dt = 0.0, time = 0.0;
+  unsigned increment = 0;
+  int model = 0;
+  std::vector<double> params;
+  int nthreads = 0;
+  std::string err;
+};
+
+// Per-q view handed to the model callbacks (restates FieldContainer getters/setters,
+// field_container.h:1065-1314).
+struct QData {
+  int dim;
+  // value/gradient per (field, age, comp)
+  const double* val;   // [field][age][comp]
+  const double* grad;  // [field][age][comp][dir]
+  double* out_val;     // [field][comp]
+  double* out_grad;    // [field][comp][dir]
+  char* out_flags;     // [field] bit0 value submitted, bit1 gradient submitted
+  int nf;
+  double x[3];         // quadrature point location
+  double vol;          // element volume
+  double v(int f, int age, int comp = 0) const { return val[(f * NAGE + age) * 3 + comp]; }
+  double g(int f, int age, int comp, int dir) const { return grad[((f * NAGE + age) * 3 + comp) * 3 + dir]; }
+  void set_value(int f, int comp, double x_) { out_val[f * 3 + comp] = x_; out_flags[f] |= 1; }
+  void set_grad(int f, int comp, int dir, double x_) { out_grad[(f * 3 + comp) * 3 + dir] = x_; out_flags[f] |= 2; }
+};
+
+typedef void (*Callback)(const Problem& P, QData& q, int block_id, bool lhs);
+
+// ---------------------------------------------------------------------------------------
+// Model callbacks (the reference applications' compute_rhs / compute_lhs).
+// ---------------------------------------------------------------------------------------
+// allen_cahn/explicit/custom_pde.h:72-101. params: m_well, kappa. fields n(0), mg_n(1), f_tot(2)
+static void cb_allen_cahn(const Problem& P, QData& q, int block_id, bool) {
+  const double m_well = P.params[0], kappa = P.params[1];
+  const int dim = q.dim;
+  if (block_id == 1) {
+    double n = q.v(0, AGE_OLD1);
+    double f_well = 4.0 * n * (n - 1.0) * (n - 0.5);
+    q.set_value(0, 0, n - P.dt * m_well * f_well);
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, -P.dt * kappa * m_well * q.g(0, AGE_OLD1, 0, d));
+  } else if (block_id == 2) {
+    double n = q.v(0, AGE_CURRENT);
+    double g2 = 0;
+    for (int d = 0; d < dim; ++d) g2 += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
+    double f_chem = n * n * n * n - 2.0 * n * n * n + n * n;
+    double f_grad = 0.5 * kappa * g2;
+    q.set_value(1, 0, std::sqrt(g2));
+    q.set_value(2, 0, f_chem + f_grad);
+  }
+}
+
+// cahn_hilliard/explicit/custom_pde.h:91-131. params: McV, KcV, WcV. fields c(0), mu(1), f_tot(2)
+static void cb_cahn_hilliard(const Problem& P, QData& q, int block_id, bool) {
+  const double McV = P.params[0], KcV = P.params[1], WcV = P.params[2];
+  const int dim = q.dim;
+  if (block_id == 0) {
+    q.set_value(0, 0, q.v(0, AGE_OLD1));
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, -McV * P.dt * q.g(1, AGE_OLD1, 0, d));
+  } else if (block_id == 1) {
+    double c = q.v(0, AGE_CURRENT);
+    q.set_value(1, 0, WcV * c * (c - 1.0) * (c - 0.5));
+    for (int d = 0; d < dim; ++d) q.set_grad(1, 0, d, KcV * q.g(0, AGE_CURRENT, 0, d));
+  } else if (block_id == 2) {
+    double c = q.v(0, AGE_CURRENT);
+    double g2 = 0;
+    for (int d = 0; d < dim; ++d) g2 += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
+    q.set_value(2, 0, c * c * c * c - 2.0 * c * c * c + c * c + 0.5 * KcV * g2);
+  }
+}
+
+// Voigt stress (utilities/mechanics.h:39-109): sigma = C : eps with engineering shears.
+static void voigt_stress(int dim, const double* C, const double eps[3][3], double sig[3][3]) {
+  const int nv = dim == 3 ? 6 : (dim == 2 ? 3 : 1);
+  double e[6] = {}, s[6] = {};
+  if (dim == 3) {
+    e[0] = eps[0][0]; e[1] = eps[1][1]; e[2] = eps[2][2];
+    e[3] = eps[1][2] + eps[2][1]; e[4] = eps[0][2] + eps[2][0]; e[5] = eps[0][1] + eps[1][0];
+  } else if (dim == 2) {
+    e[0] = eps[0][0]; e[1] = eps[1][1]; e[2] = eps[0][1] + eps[1][0];
+  } else {
+    e[0] = eps[0][0];
+  }
+  for (int i = 0; i < nv; ++i) { double a = 0; for (int j = 0; j < nv; ++j) a += C[i * 6 + j] * e[j]; s[i] = a; }
+  for (int i = 0; i < 3; ++i) for (int j = 0; j < 3; ++j) sig[i][j] = 0;
+  if (dim == 3) {
+    sig[0][0] = s[0]; sig[1][1] = s[1]; sig[2][2] = s[2];
+    sig[1][2] = sig[2][1] = s[3]; sig[0][2] = sig[2][0] = s[4]; sig[0][1] = sig[1][0] = s[5];
+  } else if (dim == 2) {
+    sig[0][0] = s[0]; sig[1][1] = s[1]; sig[0][1] = sig[1][0] = s[2];
+  } else {
+    sig[0][0] = C[0] * eps[0][0];
+  }
+}
+
+// Eigenstrain field of seeded spherical inclusions: eps* = e0 * sum_i 0.5(1 - tanh((r_i - R_i)/w)),
+// capped at e0. params layout: [0..35] C (6x6 Voigt), [36] e0, [37] width, [38] n_incl,
+// then 4 doubles per inclusion (cx, cy, cz, R). With n_incl == 0 the reference's single
+// centred-at-origin inclusion of eshelby_inclusion/custom_pde.h:60-77 is used.
+static double eigenstrain(const Problem& P, const double* x, int dim) {
+  const double* p = P.params.data();
+  const double e0 = p[36], width = p[37];
+  const int ni = (int)p[38];
+  if (ni == 0) {
+    double r = 0; for (int d = 0; d < dim; ++d) r += x[d] * x[d];
+    r = std::sqrt(r);
+    return 0.01 * (0.5 + 0.5 * std::tanh(10.0 * (r - 10.0)));
+  }
+  double s = 0;
+  for (int i = 0; i < ni; ++i) {
+    const double* c = p + 39 + 4 * i;
+    double r = 0; for (int d = 0; d < dim; ++d) r += (x[d] - c[d]) * (x[d] - c[d]);
+    r = std::sqrt(r);
+    s += 0.5 * (1.0 - std::tanh((r - c[3]) / width));
+  }
+  return e0 * std::min(s, 1.0);
+}
+
+// mechanics/eshelby_inclusion/custom_pde.h:55-92: block 1, field u (vector).
+static void cb_eshelby(const Problem& P, QData& q, int block_id, bool lhs) {
+  if (block_id != 1) return;
+  const int dim = q.dim;
+  const double* C = P.params.data();
+  double eps[3][3] = {}, sig[3][3];
+  if (lhs) {
+    for (int i = 0; i < dim; ++i)
+      for (int j = 0; j < dim; ++j) eps[i][j] = 0.5 * (q.g(0, AGE_SRC, i, j) + q.g(0, AGE_SRC, j, i));
+    voigt_stress(dim, C, eps, sig);
+    for (int i = 0; i < dim; ++i) for (int j = 0; j < dim; ++j) q.set_grad(0, i, j, sig[i][j]);
+  } else {
+    double s = eigenstrain(P, q.x, dim);
+    for (int i = 0; i < dim; ++i) eps[i][i] = s;
+    voigt_stress(dim, C, eps, sig);
+    for (int i = 0; i < dim; ++i) for (int j = 0; j < dim; ++j) q.set_grad(0, i, j, -sig[i][j]);
+  }
+}
+
+// coupled_allen_cahn_cahn_hilliard/custom_pde.h:63-176. params: Mc, Mn, Kn.
+// fields c(0), n(1), f_tot(2), mag_grad_c(3)
+static void cb_coupled(const Problem& P, QData& q, int block_id, bool) {
+  const double Mc = P.params[0], Mn = P.params[1], Kn = P.params[2];
+  const double dt = P.dt;
+  const double a0 = -1.6704, a1 = -4.776, a2 = 5.1622, a3 = -2.7375, a4 = 1.3687;
+  const double b0 = -1.5924, b1 = -5.9746, b2 = 5.0;
+  const int dim = q.dim;
+  if (block_id == 0) {
+    const double c = q.v(0, AGE_OLD1), n = q.v(1, AGE_OLD1);
+    const double c2 = c * c, c3 = c * c2, c4 = c2 * c2;
+    const double n2 = n * n, n3 = n * n2, n4 = n2 * n2, n5 = n * n4;
+    const double fa = a0 + a1 * c + a2 * c2 + a3 * c3 + a4 * c4;
+    const double fa_c = a1 + 2 * a2 * c + 3 * a3 * c2 + 4 * a4 * c3;
+    const double fa_cc = 2 * a2 + 6 * a3 * c + 12 * a4 * c2;
+    const double fb = b0 + b1 * c + b2 * c2;
+    const double fb_c = b1 + 2 * b2 * c;
+    const double fb_cc = 2 * b2;
+    const double h = 10.0 * n3 - 15.0 * n4 + 6.0 * n5;
+    const double hn = 30.0 * n2 - 60.0 * n3 + 30.0 * n4;
+    const double dndt_val = -Mn * (fb - fa) * hn;
+    for (int d = 0; d < dim; ++d) {
+      const double cx = q.g(0, AGE_OLD1, 0, d), nx = q.g(1, AGE_OLD1, 0, d);
+      const double mu_grad = -(cx * ((1.0 - h) * fa_cc + h * fb_cc) + nx * ((fb_c - fa_c) * hn));
+      const double dcdt_vec = Mc * -mu_grad;
+      q.set_grad(0, 0, d, -dt * dcdt_vec);
+      q.set_grad(1, 0, d, -dt * (Kn * Mn * nx));
+    }
+    q.set_value(0, 0, c);
+    q.set_value(1, 0, n + dt * dndt_val);
+  } else if (block_id == 1) {
+    const double c = q.v(0, AGE_CURRENT), n = q.v(1, AGE_CURRENT);
+    const double c2 = c * c, c3 = c * c2, c4 = c2 * c2;
+    const double n2 = n * n, n3 = n * n2, n4 = n2 * n2, n5 = n * n4;
+    const double fa = a0 + a1 * c + a2 * c2 + a3 * c3 + a4 * c4;
+    const double fb = b0 + b1 * c + b2 * c2;
+    const double h = 10.0 * n3 - 15.0 * n4 + 6.0 * n5;
+    double nn = 0, cc = 0;
+    for (int d = 0; d < dim; ++d) {
+      nn += q.g(1, AGE_CURRENT, 0, d) * q.g(1, AGE_CURRENT, 0, d);
+      cc += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
+    }
+    q.set_value(2, 0, (1.0 - h) * fa + h * fb + 0.5 * Kn * nn);
+    q.set_value(3, 0, std::sqrt(cc));
+  }
+}
+
+static Callback callback_for(int model) {
+  switch (model) {
+    case ORC_MODEL_ALLEN_CAHN: return cb_allen_cahn;
+    case ORC_MODEL_CAHN_HILLIARD: return cb_cahn_hilliard;
+    case ORC_MODEL_ESHELBY: return cb_eshelby;
+    case ORC_MODEL_COUPLED_ACCH: return cb_coupled;
+    default: return nullptr;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Constraints construction.
+// ---------------------------------------------------------------------------------------
+static long lattice_dof(const Mesh& m, int which, const std::vector<long>& node2dof, long I, long J, long K, int comp) {
+  const int nc = m.dh[which].ncomp;
+  return node2dof[(((K * m.nnode[1] + J) * m.nnode[0]) + I) * nc + comp];
+}
+
+static std::vector<long> node_to_dof(const Mesh& m, int which) {
+  const DofHandler& d = m.dh[which];
+  std::vector<long> out((size_t)m.nnode[0] * m.nnode[1] * m.nnode[2] * d.ncomp, -1);
+  for (long i = 0; i < d.ndofs; ++i) {
+    auto& L = d.lattice[i];
+    out[((((long)L[2] * m.nnode[1]) + L[1]) * m.nnode[0] + L[0]) * d.ncomp + L[3]] = i;
+  }
+  return out;
+}
+
+// make_periodicity_constraints restated: the dof on the face with boundary id 2d+1 is
+// constrained to the matching dof on boundary id 2d, weight 1 (chains closed later).
+static void make_periodic(const Mesh& m, int which, Constraints& C) {
+  const DofHandler& d = m.dh[which];
+  auto n2d = node_to_dof(m, which);
+  for (long i = 0; i < d.ndofs; ++i) {
+    auto& L = d.lattice[i];
+    for (int dir = 0; dir < m.dim; ++dir) {
+      if (!m.periodic[dir]) continue;
+      if (L[dir] != m.nnode[dir] - 1) continue;
+      long I = L[0], J = L[1], K = L[2];
+      if (dir == 0) I = 0; else if (dir == 1) J = 0; else K = 0;
+      long master = lattice_dof(m, which, n2d, I, J, K, L[3]);
+      if (!C.is_constrained(i)) {
+        C.add_line(i);
+        C.entries[i].push_back({master, 1.0});
+      } else {
+        // a second periodic direction for an already-constrained dof: keep the first
+        // line (deal.II resolves the corner through the chain of the other direction)
+      }
+      break;
+    }
+  }
+}
+
+static bool on_boundary(const Mesh& m, const std::array<int, 4>& L, int bid) {
+  const int dir = bid / 2;
+  if (dir >= m.dim) return false;
+  return (bid % 2 == 0) ? L[dir] == 0 : L[dir] == m.nnode[dir] - 1;
+}
+
+static void make_field_constraints(Problem& P, int f) {
+  Field& F = P.fields[f];
+  const int which = F.rank;
+  const DofHandler& d = P.m.dh[which];
+  F.cons.reinit(d.ndofs);
+  make_periodic(P.m, which, F.cons);
+  // interpolate_boundary_values: boundary ids in ascending order, dofs not yet constrained
+  for (int comp = 0; comp < d.ncomp; ++comp)
+    for (int bid = 0; bid < 2 * P.m.dim; ++bid) {
+      if (!F.dir_on[comp][bid]) continue;
+      for (long i = 0; i < d.ndofs; ++i) {
+        auto& L = d.lattice[i];
+        if (L[3] != comp || !on_boundary(P.m, L, bid)) continue;
+        if (F.cons.is_constrained(i)) continue;
+        F.cons.add_line(i);
+        F.cons.inhom[i] = F.dir_val[comp][bid];
+      }
+    }
+  F.cons.close();
+}
+
+// ---------------------------------------------------------------------------------------
+// Cell loop (the MFOperator::compute_local_operator restatement).
+// ---------------------------------------------------------------------------------------
+struct DepSlot { int field, age, flags; const double* vec; const Constraints* cons; bool constrained_read; int ncomp; };
+
+// dst[field] vectors are indexed by block position
+static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<const double*>& src,
+                      std::vector<double*>& dst, const std::vector<const Constraints*>& dst_cons,
+                      Callback cb) {
+  Mesh& m = P.m;
+  const int dim = m.dim, n = m.n, nloc = m.nloc;
+  const auto& deps = lhs ? B.dep_lhs : B.dep_rhs;
+  const int nf = (int)P.fields.size();
+  std::vector<DepSlot> slots;
+  for (int f = 0; f < nf; ++f)
+    for (int age = 0; age < NAGE; ++age) {
+      int fl = deps[f][age];
+      if (!fl) continue;
+      Field& F = P.fields[f];
+      const double* vec = nullptr;
+      bool cread = false;
+      if (age == AGE_CURRENT) vec = F.cur.data();
+      else if (age == AGE_SRC) {
+        int pos = -1;
+        for (size_t b = 0; b < B.fields.size(); ++b) if (B.fields[b] == f) pos = (int)b;
+        if (pos < 0 || !src[pos]) continue;
+        vec = src[pos];
+        cread = lhs;  // LHS reads src with homogeneous constraints (field_container.h:817-832)
+      } else vec = F.old[age - 1].data();
+      slots.push_back({f, age, fl, vec, &F.cons, cread, F.rank == 0 ? 1 : dim});
+    }
+  const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
+  const GL& gl = m.gl;
+  // colouring for thread safety of the scatter: cell parity per axis
+  int ncol = 1 << dim;
+  bool serial = false;
+  for (int d = 0; d < dim; ++d) if (m.periodic[d] && (m.nc[d] % 2)) serial = true;
+  std::vector<std::vector<long>> colours(ncol);
+  for (long c = 0; c < m.ncells; ++c) {
+    auto& cc = m.cells[c];
+    int col = (cc[0] & 1) | ((cc[1] & 1) << 1) | (dim == 3 ? ((cc[2] & 1) << 2) : 0);
+    colours[serial ? 0 : col].push_back(c);
+  }
+  const int nbf = (int)B.fields.size();
+  for (int col = 0; col < ncol; ++col) {
+    const auto& cl = colours[col];
+    const long ncl = (long)cl.size();
+#pragma omp parallel if (!serial) num_threads(P.nthreads > 0 ? P.nthreads : omp_get_max_threads())
+    {
+      std::vector<double> loc((size_t)slots.size() * 3 * nloc);
+      std::vector<double> qval((size_t)nf * NAGE * 3, 0.0), qgrad((size_t)nf * NAGE * 9, 0.0);
+      std::vector<double> ov((size_t)nloc * nf * 3), og((size_t)nloc * nf * 9);
+      std::vector<char> oflag(nf);
+      std::vector<double> vals((size_t)slots.size() * 3 * nloc), grads((size_t)slots.size() * 9 * nloc);
+      std::vector<double> res((size_t)nloc * 3);
+#pragma omp for schedule(static)
+      for (long ci = 0; ci < ncl; ++ci) {
+        const long c = cl[ci];
+        const auto& cc = m.cells[c];
+        // gather + evaluate each dependency
+        for (size_t s = 0; s < slots.size(); ++s) {
+          const DepSlot& S = slots[s];
+          const DofHandler& dh = m.dh[S.ncomp == 1 ? 0 : 1];
+          for (int comp = 0; comp < S.ncomp; ++comp)
+            for (int l = 0; l < nloc; ++l) {
+              long gdof = dh.cell_dofs[((size_t)c * S.ncomp + comp) * nloc + l];
+              double v;
+              if (S.constrained_read && S.cons->is_constrained(gdof)) {
+                v = 0.0;
+                for (auto& e : S.cons->entries[gdof]) v += e.second * S.vec[e.first];
+              } else {
+                v = S.vec[gdof];
+              }
+              loc[(s * 3 + comp) * nloc + l] = v;
+            }
+          for (int comp = 0; comp < S.ncomp; ++comp) {
+            const double* u = &loc[(s * 3 + comp) * nloc];
+            for (int l = 0; l < nloc; ++l) {
+              vals[(s * 3 + comp) * nloc + l] = u[l];
+              int a = l % n, b = (l / n) % n, e = l / (n * n);
+              int idx[3] = {a, b, e};
+              int stride[3] = {1, n, n * n};
+              for (int d = 0; d < dim; ++d) {
+                double acc = 0.0;
+                int base = l - idx[d] * stride[d];
+                for (int j = 0; j < n; ++j) acc += gl.D[idx[d]][j] * u[base + j * stride[d]];
+                grads[((s * 3 + comp) * 3 + d) * nloc + l] = acc / m.h[d];
+              }
+            }
+          }
+        }
+        // quadrature loop with the user callback
+        std::fill(ov.begin(), ov.end(), 0.0);
+        std::fill(og.begin(), og.end(), 0.0);
+        std::fill(oflag.begin(), oflag.end(), 0);
+        for (int l = 0; l < nloc; ++l) {
+          for (size_t s = 0; s < slots.size(); ++s) {
+            const DepSlot& S = slots[s];
+            for (int comp = 0; comp < S.ncomp; ++comp) {
+              qval[(S.field * NAGE + S.age) * 3 + comp] = vals[(s * 3 + comp) * nloc + l];
+              for (int d = 0; d < dim; ++d)
+                qgrad[((S.field * NAGE + S.age) * 3 + comp) * 3 + d] = grads[((s * 3 + comp) * 3 + d) * nloc + l];
+            }
+          }
+          QData q;
+          q.dim = dim; q.val = qval.data(); q.grad = qgrad.data();
+          q.out_val = &ov[(size_t)l * nf * 3]; q.out_grad = &og[(size_t)l * nf * 9];
+          q.out_flags = oflag.data(); q.nf = nf;
+          int a = l % n, b = (l / n) % n, e = l / (n * n);
+          q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * m.h[0];
+          q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * m.h[1];
+          q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * m.h[2] : 0.0;
+          q.vol = detJ;
+          cb(P, q, B.id, lhs);
+        }
+        // integrate + distribute for each block field
+        for (int bf = 0; bf < nbf; ++bf) {
+          const int f = B.fields[bf];
+          const int ncomp = P.fields[f].rank == 0 ? 1 : dim;
+          const DofHandler& dh = m.dh[ncomp == 1 ? 0 : 1];
+          for (int comp = 0; comp < ncomp; ++comp) {
+            for (int l = 0; l < nloc; ++l) {
+              int a = l % n, b = (l / n) % n, e = l / (n * n);
+              int idx[3] = {a, b, e};
+              int stride[3] = {1, n, n * n};
+              double wq = gl.w[a] * gl.w[b] * (dim == 3 ? gl.w[e] : 1.0);
+              double r = 0.0;
+              if (oflag[f] & 1) r += ov[((size_t)l * nf + f) * 3 + comp] * wq * detJ;
+              if (oflag[f] & 2) {
+                for (int d = 0; d < dim; ++d) {
+                  int base = l - idx[d] * stride[d];
+                  double acc = 0.0;
+                  for (int qd = 0; qd < n; ++qd) {
+                    int lq = base + qd * stride[d];
+                    int aq = lq % n, bq = (lq / n) % n, eq = lq / (n * n);
+                    double wqq = gl.w[aq] * gl.w[bq] * (dim == 3 ? gl.w[eq] : 1.0);
+                    acc += og[(((size_t)lq * nf + f) * 3 + comp) * 3 + d] * gl.D[qd][idx[d]] * wqq;
+                  }
+                  r += acc * detJ / m.h[d];
+                }
+              }
+              res[comp * nloc + l] = r;
+            }
+          }
+          // distribute_local_to_global with constraints condensed
+          const Constraints* C = dst_cons[bf];
+          double* out = dst[bf];
+          for (int comp = 0; comp < ncomp; ++comp)
+            for (int l = 0; l < nloc; ++l) {
+              long gdof = dh.cell_dofs[((size_t)c * ncomp + comp) * nloc + l];
+              double r = res[comp * nloc + l];
+              if (C && C->is_constrained(gdof)) {
+                for (auto& e2 : C->entries[gdof]) out[e2.first] += e2.second * r;
+              } else {
+                out[gdof] += r;
+              }
+            }
+        }
+      }
+    }
+  }
+}
+
+static void compute_invm(Problem& P) {
+  Mesh& m = P.m;
+  for (int which = 0; which < 2; ++which) {
+    if (which == 1 && m.dim == 1) { }
+    DofHandler& d = m.dh[which];
+    Constraints& C = P.generic[which];
+    C.reinit(d.ndofs);
+    make_periodic(m, which, C);
+    C.close();
+    P.jxw[which].assign(d.ndofs, 0.0);
+    const int dim = m.dim, n = m.n, nloc = m.nloc;
+    const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
+    for (long c = 0; c < m.ncells; ++c)
+      for (int comp = 0; comp < d.ncomp; ++comp)
+        for (int l = 0; l < nloc; ++l) {
+          int a = l % n, b = (l / n) % n, e = l / (n * n);
+          double r = m.gl.w[a] * m.gl.w[b] * (dim == 3 ? m.gl.w[e] : 1.0) * detJ;
+          long g = d.cell_dofs[((size_t)c * d.ncomp + comp) * nloc + l];
+          if (C.is_constrained(g)) { for (auto& e2 : C.entries[g]) P.jxw[which][e2.first] += e2.second * r; }
+          else P.jxw[which][g] += r;
+        }
+    P.invm[which].resize(d.ndofs);
+    P.invm_sqrt[which].resize(d.ndofs);
+    for (long i = 0; i < d.ndofs; ++i) {
+      double s = P.jxw[which][i];
+      P.invm[which][i] = s == 0.0 ? 0.0 : 1.0 / s;
+      P.invm_sqrt[which][i] = std::sqrt(P.invm[which][i]);
+    }
+  }
+}
+
+// AffineConstraints::distribute: constrained entries set from their masters + inhomogeneity
+static void distribute(const Constraints& C, double* v) {
+  const long n = (long)C.constrained.size();
+  for (long i = 0; i < n; ++i) {
+    if (!C.constrained[i]) continue;
+    double s = C.inhom[i];
+    for (auto& e : C.entries[i]) s += e.second * v[e.first];
+    v[i] = s;
+  }
+}
+
+// ExplicitSolver::solve_impl: u = invM (.) A_rhs, then constraints.
+static void explicit_solve(Problem& P, const Block& B) {
+  std::vector<double*> dst;
+  std::vector<const Constraints*> cons;
+  std::vector<const double*> src(B.fields.size(), nullptr);
+  for (int f : B.fields) {
+    Field& F = P.fields[f];
+    std::fill(F.cur.begin(), F.cur.end(), 0.0);
+    dst.push_back(F.cur.data());
+    cons.push_back(&F.cons);
+  }
+  cell_loop(P, B, false, src, dst, cons, callback_for(P.model));
+  for (int f : B.fields) {
+    Field& F = P.fields[f];
+    const auto& im = P.invm[F.rank];
+    for (size_t i = 0; i < F.cur.size(); ++i) F.cur[i] *= im[i];
+    distribute(F.cons, F.cur.data());
+  }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+// ---------------------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+void* orc_create(int dim, int degree, const int* subdiv, const double* lower, const double* size,
+                 int refine, const int* periodic) {
+  if (dim < 1 || dim > 3 || degree < 1 || degree > 6) return nullptr;
+  auto* P = new Problem();
+  Mesh& m = P->m;
+  m.dim = dim; m.k = degree; m.n = degree + 1;
+  m.nloc = 1; for (int d = 0; d < dim; ++d) m.nloc *= m.n;
+  int sd[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) { sd[d] = subdiv[d]; m.lo[d] = lower[d]; m.len[d] = size[d]; m.periodic[d] = periodic[d]; }
+  build_cells(m, sd, refine);
+  for (int d = 0; d < 3; ++d) {
+    m.h[d] = d < dim ? m.len[d] / m.nc[d] : 1.0;
+    m.nnode[d] = d < dim ? m.k * m.nc[d] + 1 : 1;
+  }
+  m.gl = make_gl(m.n);
+  distribute_dofs(m, 0);
+  distribute_dofs(m, 1);
+  compute_invm(*P);
+  return P;
+}
+
+void orc_destroy(void* h) { delete (Problem*)h; }
+
+void orc_set_threads(void* h, int n) { ((Problem*)h)->nthreads = n; }
+
+long orc_n_dofs(void* h, int rank) { return ((Problem*)h)->m.dh[rank].ndofs; }
+long orc_n_cells(void* h) { return ((Problem*)h)->m.ncells; }
+
+void orc_gl(int n, double* x, double* w, double* D) {
+  GL g = make_gl(n);
+  for (int i = 0; i < n; ++i) { x[i] = g.x[i]; w[i] = g.w[i]; for (int j = 0; j < n; ++j) D[i * n + j] = g.D[i][j]; }
+}
+
+void orc_lattice(void* h, int rank, int* out) {
+  auto& d = ((Problem*)h)->m.dh[rank];
+  for (long i = 0; i < d.ndofs; ++i) for (int k = 0; k < 4; ++k) out[i * 4 + k] = d.lattice[i][k];
+}
+
+void orc_cell_dofs(void* h, int rank, long* out) {
+  auto& d = ((Problem*)h)->m.dh[rank];
+  std::memcpy(out, d.cell_dofs.data(), d.cell_dofs.size() * sizeof(long));
+}
+
+void orc_cell_coords(void* h, int* out) {
+  auto& m = ((Problem*)h)->m;
+  for (long c = 0; c < m.ncells; ++c) for (int k = 0; k < 3; ++k) out[c * 3 + k] = m.cells[c][k];
+}
+
+void orc_invm(void* h, int rank, double* out) {
+  auto* P = (Problem*)h;
+  std::memcpy(out, P->invm[rank].data(), P->invm[rank].size() * sizeof(double));
+}
+
+int orc_add_field(void* h, int rank) {
+  auto* P = (Problem*)h;
+  Field F; F.rank = rank;
+  P->fields.push_back(F);
+  return (int)P->fields.size() - 1;
+}
+
+void orc_set_dirichlet(void* h, int field, int comp, int boundary_id, double value) {
+  auto* P = (Problem*)h;
+  P->fields[field].dir_on[comp][boundary_id] = 1;
+  P->fields[field].dir_val[comp][boundary_id] = value;
+}
+
+// deps: nfields * 6 flags (ages: current, old1..old4, src) for rhs then lhs
+int orc_add_block(void* h, int id, int solve_type, int timing, const int* fields, int nf,
+                  const int* dep_rhs, const int* dep_lhs) {
+  auto* P = (Problem*)h;
+  Block B; B.id = id; B.solve_type = solve_type; B.timing = timing;
+  for (int i = 0; i < nf; ++i) B.fields.push_back(fields[i]);
+  const int NF = (int)P->fields.size();
+  B.dep_rhs.assign(NF, {}); B.dep_lhs.assign(NF, {});
+  for (int f = 0; f < NF; ++f)
+    for (int a = 0; a < NAGE; ++a) {
+      B.dep_rhs[f][a] = dep_rhs ? dep_rhs[f * NAGE + a] : 0;
+      B.dep_lhs[f][a] = dep_lhs ? dep_lhs[f * NAGE + a] : 0;
+    }
+  P->blocks.push_back(B);
+  return (int)P->blocks.size() - 1;
+}
+
+int orc_finalize(void* h, int model, const double* params, int nparams, double dt) {
+  auto* P = (Problem*)h;
+  P->model = model;
+  P->params.assign(params, params + nparams);
+  P->dt = dt;
+  if (!callback_for(model)) return -1;
+  // number of old ages needed per field = max old age referenced by any block
+  for (size_t f = 0; f < P->fields.size(); ++f) {
+    Field& F = P->fields[f];
+    const long nd = P->m.dh[F.rank].ndofs;
+    int n_old = 0;
+    for (auto& B : P->blocks)
+      for (int a = AGE_OLD1; a <= AGE_OLD4; ++a)
+        if (B.dep_rhs[f][a] || B.dep_lhs[f][a]) n_old = std::max(n_old, a);
+    F.n_old = n_old;
+    F.cur.assign(nd, 0.0);
+    for (int a = 0; a < 4; ++a) F.old[a].assign(a < n_old ? nd : 0, 0.0);
+    make_field_constraints(*P, (int)f);
+  }
+  return 0;
+}
+
+// constraint export: kind (0 free, 1 constrained), master (first entry or -1), inhomogeneity
+void orc_constraints(void* h, int field, int* kind, long* master, double* inhom) {
+  auto* P = (Problem*)h;
+  auto& C = P->fields[field].cons;
+  for (size_t i = 0; i < C.constrained.size(); ++i) {
+    kind[i] = C.constrained[i];
+    master[i] = (C.constrained[i] && !C.entries[i].empty()) ? C.entries[i][0].first : -1;
+    inhom[i] = C.inhom[i];
+  }
+}
+
+int orc_set_vector(void* h, int field, int age, const double* v) {
+  auto* P = (Problem*)h;
+  Field& F = P->fields[field];
+  std::vector<double>& dst = age == 0 ? F.cur : F.old[age - 1];
+  if (dst.empty()) return -1;
+  std::memcpy(dst.data(), v, dst.size() * sizeof(double));
+  return 0;
+}
+
+int orc_get_vector(void* h, int field, int age, double* v) {
+  auto* P = (Problem*)h;
+  Field& F = P->fields[field];
+  std::vector<double>& src = age == 0 ? F.cur : F.old[age - 1];
+  if (src.empty()) return -1;
+  std::memcpy(v, src.data(), src.size() * sizeof(double));
+  return 0;
+}
+
+void orc_set_time(void* h, unsigned increment, double time) {
+  auto* P = (Problem*)h;
+  P->increment = increment; P->time = time;
+}
+
+// One explicit solve of block index b (ExplicitSolver::solve_impl)
+int orc_explicit_block(void* h, int b) {
+  auto* P = (Problem*)h;
+  explicit_solve(*P, P->blocks[b]);
+  return 0;
+}
+
+// The Problem::solve increment loop (explicit blocks only); output_every > 0 makes
+// PostProcess blocks run on increments that are multiples of it.
+int orc_run(void* h, unsigned n_increments, int output_every) {
+  auto* P = (Problem*)h;
+  while (P->increment <= n_increments) {
+    for (auto& B : P->blocks) {
+      if (B.timing == ORC_TIMING_POSTPROCESS) {
+        if (output_every <= 0 || (P->increment % (unsigned)output_every) != 0) continue;
+      }
+      if (P->increment == 0 && B.timing == ORC_TIMING_PRIMARY) {
+        // initial condition already uploaded into `cur`; like
+        // SolverBase::set_initial_condition (solver_base.h:178-229) no constraints are
+        // distributed on it at increment 0
+      } else {
+        explicit_solve(*P, B);
+      }
+      if (P->increment == 0) {
+        for (int f : B.fields) {
+          Field& F = P->fields[f];
+          for (int a = 0; a < F.n_old; ++a) F.old[a] = F.cur;
+        }
+      }
+    }
+    for (auto& F : P->fields) {
+      if (!std::isfinite(F.cur.empty() ? 0.0 : F.cur[0])) return ORC_ERR_NAN;
+    }
+    // rotation by swap (group_solution_handler.cc:369-403)
+    for (auto& F : P->fields)
+      for (int age = F.n_old - 1; age >= 0; --age) {
+        if (age > 0) F.old[age].swap(F.old[age - 1]);
+        else F.old[0].swap(F.cur);
+      }
+    P->increment++;
+    P->time += P->dt;
+  }
+  return 0;
+}
+
+// Operator apply of block b: which = 0 rhs (plain read), 1 lhs (src read with constraints).
+// src/dst are per block-field vectors concatenated in block field order. scale: 0 none,
+// 1 invM, 2 invM^1/2.
+int orc_apply(void* h, int b, int which, const double* src, double* dst, int scale) {
+  auto* P = (Problem*)h;
+  Block& B = P->blocks[b];
+  std::vector<const double*> s;
+  std::vector<double*> d;
+  std::vector<const Constraints*> cons;
+  size_t off = 0;
+  for (int f : B.fields) {
+    Field& F = P->fields[f];
+    const size_t nd = F.cur.size();
+    s.push_back(src ? src + off : nullptr);
+    std::fill(dst + off, dst + off + nd, 0.0);
+    d.push_back(dst + off);
+    cons.push_back(&F.cons);
+    off += nd;
+  }
+  cell_loop(*P, B, which == 1, s, d, cons, callback_for(P->model));
+  off = 0;
+  for (int f : B.fields) {
+    Field& F = P->fields[f];
+    const size_t nd = F.cur.size();
+    if (scale == 1) for (size_t i = 0; i < nd; ++i) dst[off + i] *= P->invm[F.rank][i];
+    if (scale == 2) for (size_t i = 0; i < nd; ++i) dst[off + i] *= P->invm_sqrt[F.rank][i];
+    off += nd;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""ctypes bindings of the C ABI declared in ``include/ppf_gb300.h``.
+
+The library is the in-tree ``phasefield_gb300/lib/libppf_gb300.so``. Loading fails loudly if it
+is missing: there is no CPU fallback on the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libppf_gb300.so"
+
+PPF_MAX_FIELDS = 8
+PPF_NAGE = 6
+
+PPF_OK = 0
+PPF_ERR_ARG = 1
+PPF_ERR_NAN = 2
+PPF_ERR_CUDA = 3
+PPF_ERR_NOCONV = 4
+PPF_ERR_DEPENDENCY = 5
+PPF_ERR_UNSUPPORTED = 6
+PPF_ERR_TIMEOUT = 7
+
+ORDER_LATTICE = 0
+ORDER_DEALII = 1
+
+# exported symbols of include/ppf_gb300.h (checked by the CPU test suite)
+EXPORTED = [
+    "ppf_create", "ppf_destroy", "ppf_last_error", "ppf_n_nodes", "ppf_field_length", "ppf_n_cells",
+    "ppf_dof_map", "ppf_constraint_map", "ppf_invm", "ppf_upload_state", "ppf_download_state",
+    "ppf_apply_constraints", "ppf_run", "ppf_solve_block", "ppf_apply", "ppf_apply_device",
+    "ppf_set_time", "ppf_get_time", "ppf_set_use_graph", "ppf_state_device_ptr", "ppf_synchronize",
+    "ppf_set_stream", "ppf_kernel_timing", "ppf_kernel_stats", "ppf_kernel_stats_reset",
+    "ppf_device_fp64_peak",
+]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("degree", C.c_int), ("subdivisions", C.c_int * 3),
+        ("lower", C.c_double * 3), ("size", C.c_double * 3), ("global_refinement", C.c_int),
+        ("periodic", C.c_int * 3),
+    ]
+
+
+class FieldDesc(C.Structure):
+    _fields_ = [
+        ("rank", C.c_int), ("dirichlet", (C.c_int * 6) * 3), ("dirichlet_value", (C.c_double * 6) * 3),
+    ]
+
+
+class BlockDesc(C.Structure):
+    _fields_ = [
+        ("id", C.c_int), ("solve_type", C.c_int), ("solve_timing", C.c_int), ("n_fields", C.c_int),
+        ("field_indices", C.c_int * PPF_MAX_FIELDS),
+        ("dep_rhs", (C.c_ubyte * PPF_NAGE) * PPF_MAX_FIELDS),
+        ("dep_lhs", (C.c_ubyte * PPF_NAGE) * PPF_MAX_FIELDS),
+    ]
+
+
+class PPFError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ppf error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.POINTER
+    dp = P(C.c_double)
+    H = C.c_void_p
+    lib.ppf_create.argtypes = [P(MeshDesc), P(FieldDesc), C.c_int, P(BlockDesc), C.c_int, C.c_char_p, dp, C.c_int,
+                               C.c_double, P(H)]
+    lib.ppf_destroy.argtypes = [H]
+    lib.ppf_destroy.restype = None
+    lib.ppf_last_error.argtypes = [H]
+    lib.ppf_last_error.restype = C.c_char_p
+    for name in ("ppf_n_nodes", "ppf_n_cells"):
+        getattr(lib, name).argtypes = [H]
+        getattr(lib, name).restype = C.c_longlong
+    lib.ppf_field_length.argtypes = [H, C.c_int]
+    lib.ppf_field_length.restype = C.c_longlong
+    lib.ppf_dof_map.argtypes = [H, C.c_int, P(C.c_longlong)]
+    lib.ppf_constraint_map.argtypes = [H, C.c_int, P(C.c_int)]
+    lib.ppf_invm.argtypes = [H, dp]
+    lib.ppf_upload_state.argtypes = [H, C.c_int, C.c_int, dp, C.c_int]
+    lib.ppf_download_state.argtypes = [H, C.c_int, C.c_int, dp, C.c_int]
+    lib.ppf_apply_constraints.argtypes = [H, C.c_int]
+    lib.ppf_run.argtypes = [H, C.c_uint, C.c_int]
+    lib.ppf_solve_block.argtypes = [H, C.c_int]
+    lib.ppf_apply.argtypes = [H, C.c_int, C.c_int, dp, dp, C.c_int]
+    lib.ppf_apply_device.argtypes = [H, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+    lib.ppf_set_time.argtypes = [H, C.c_uint, C.c_double]
+    lib.ppf_get_time.argtypes = [H, P(C.c_uint), dp]
+    lib.ppf_set_use_graph.argtypes = [H, C.c_int]
+    lib.ppf_state_device_ptr.argtypes = [H, C.c_int, C.c_int, P(C.c_void_p)]
+    lib.ppf_synchronize.argtypes = [H]
+    lib.ppf_set_stream.argtypes = [H, C.c_void_p]
+    lib.ppf_kernel_timing.argtypes = [H, C.c_int]
+    lib.ppf_kernel_stats.argtypes = [H, dp, P(C.c_longlong), P(C.c_longlong)]
+    lib.ppf_kernel_stats_reset.argtypes = [H]
+    lib.ppf_device_fp64_peak.argtypes = [dp]
+    _lib = lib
+    return lib
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))

@@ -1,0 +1,210 @@
+// Built-in PDE operators: the compute_rhs / compute_lhs callbacks of the reference
+// applications, written against the device FieldContainer API exactly as an application
+// writes them (same getters, setters, dependency types and block ids). Each class is
+// trivially copyable and travels to the GPU as a kernel argument.
+//
+//   AllenCahn        applications/allen_cahn/explicit/custom_pde.h:72-101
+//   CahnHilliard     applications/cahn_hilliard/explicit/custom_pde.h:91-131
+//   Eshelby          applications/mechanics/eshelby_inclusion/custom_pde.h:55-92, with the
+//                    eigenstrain of seeded spherical inclusions used by the 3-D elasticity
+//                    workload (a sum of tanh profiles capped at one)
+//   CoupledACCH      applications/coupled_allen_cahn_cahn_hilliard/custom_pde.h:63-176
+#pragma once
+
+#include <prismspf/core/field_container.h>
+#include <prismspf/utilities/mechanics.h>
+
+namespace ppf {
+
+using namespace prismspf;
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct AllenCahn {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number m_well;
+  number kappa;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 1) {
+      ScalarValue n_val = variable_list.template get_value<Scalar, OldOne>(0);
+      ScalarGrad n_grad = variable_list.template get_gradient<Scalar, OldOne>(0);
+      ScalarValue f_well = 4.0 * n_val * (n_val - 1.0) * (n_val - 0.5);
+      ScalarValue eq_n = n_val - sim_timer.get_timestep() * m_well * f_well;
+      ScalarGrad eqx_n = -sim_timer.get_timestep() * kappa * m_well * n_grad;
+      variable_list.set_value_term(0, eq_n);
+      variable_list.set_gradient_term(0, eqx_n);
+    } else if (solve_block_id == 2) {
+      ScalarValue n_val = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad n_grad = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue f_chem = n_val * n_val * n_val * n_val - 2.0 * n_val * n_val * n_val + n_val * n_val;
+      ScalarValue f_grad = 0.5 * kappa * n_grad.norm_square();
+      variable_list.set_value_term(1, n_grad.norm());
+      variable_list.set_value_term(2, f_chem + f_grad);
+    }
+  }
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
+};
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct CahnHilliard {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number McV;
+  number KcV;
+  number WcV;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 0) {
+      ScalarValue c = variable_list.template get_value<Scalar, OldOne>(0);
+      ScalarGrad mux = variable_list.template get_gradient<Scalar, OldOne>(1);
+      ScalarValue eq_c = c;
+      ScalarGrad eqx_c = -McV * sim_timer.get_timestep() * mux;
+      variable_list.set_value_term(0, eq_c);
+      variable_list.set_gradient_term(0, eqx_c);
+    } else if (solve_block_id == 1) {
+      ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad cx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue fcV = WcV * c * (c - 1.0) * (c - 0.5);
+      ScalarGrad eqx_mu = KcV * cx;
+      variable_list.set_value_term(1, fcV);
+      variable_list.set_gradient_term(1, eqx_mu);
+    } else if (solve_block_id == 2) {
+      ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad cx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue f_chem = c * c * c * c - 2.0 * c * c * c + c * c;
+      ScalarValue f_grad = 0.5 * KcV * cx.norm_square();
+      variable_list.set_value_term(2, f_chem + f_grad);
+    }
+  }
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
+};
+
+constexpr int ESHELBY_MAX_INCLUSIONS = 64;
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct Eshelby {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using VectorGrad = dealii::Tensor<2, dim, ScalarValue>;
+  static constexpr unsigned int nv = Mechanics::voigt_tensor_size<dim>;
+  dealii::Tensor<2, nv, number> stiffness;
+  number e0;      // eigenstrain magnitude
+  number width;   // tanh interface width
+  int n_incl;     // 0: the application's single inclusion of radius 10 at the origin
+  number incl[ESHELBY_MAX_INCLUSIONS][4];  // centre xyz, radius
+
+  PPF_HD ScalarValue strain_magnitude(const dealii::Point<dim, ScalarValue>& p) const {
+    if (n_incl == 0) {
+      ScalarValue dist_from_inclusion = p.norm();
+      ScalarValue inclusion_radius(10.0);
+      return 0.01 * (0.5 + 0.5 * std::tanh(10.0 * (dist_from_inclusion - inclusion_radius)));
+    }
+    ScalarValue s(0.0);
+    for (int i = 0; i < n_incl; ++i) {
+      ScalarValue r2(0.0);
+      for (unsigned int d = 0; d < dim; ++d) {
+        ScalarValue dx = p[d] - incl[i][d];
+        r2 += dx * dx;
+      }
+      s += 0.5 * (1.0 - std::tanh((std::sqrt(r2) - incl[i][3]) / width));
+    }
+    return e0 * std::min(s, ScalarValue(1.0));
+  }
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer&,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 1) {
+      ScalarValue strain_value = strain_magnitude(variable_list.get_q_point_location());
+      VectorGrad transformation_strain;
+      for (unsigned int i = 0; i < dim; i++) transformation_strain[i][i] = strain_value;
+      VectorGrad stress;
+      Mechanics::compute_stress<dim, ScalarValue>(stiffness, transformation_strain, stress);
+      variable_list.set_gradient_term(0, -stress);
+    }
+  }
+
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer&,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 1) {
+      VectorGrad ux = variable_list.template get_symmetric_gradient<Vector, LHS>(0);
+      VectorGrad stress;
+      Mechanics::compute_stress<dim, ScalarValue>(stiffness, ux, stress);
+      variable_list.set_gradient_term(0, stress);
+    }
+  }
+};
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct CoupledACCH {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number Mc;
+  number Mn;
+  number Kn;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    const double dt = sim_timer.get_timestep();
+    constexpr double a0 = -1.6704;
+    constexpr double a1 = -4.776;
+    constexpr double a2 = 5.1622;
+    constexpr double a3 = -2.7375;
+    constexpr double a4 = 1.3687;
+    constexpr double b0 = -1.5924;
+    constexpr double b1 = -5.9746;
+    constexpr double b2 = 5.0;
+    if (solve_block_id == 0) {
+      const ScalarValue c = variable_list.template get_value<Scalar, OldOne>(0);
+      const ScalarGrad cx = variable_list.template get_gradient<Scalar, OldOne>(0);
+      const ScalarValue n = variable_list.template get_value<Scalar, OldOne>(1);
+      const ScalarGrad nx = variable_list.template get_gradient<Scalar, OldOne>(1);
+      const ScalarValue c2 = c * c;
+      const ScalarValue c3 = c * c2;
+      const ScalarValue c4 = c2 * c2;
+      const ScalarValue n2 = n * n;
+      const ScalarValue n3 = n * n2;
+      const ScalarValue n4 = n2 * n2;
+      const ScalarValue n5 = n * n4;
+      ScalarValue fa = a0 + a1 * c + a2 * c2 + a3 * c3 + a4 * c4;
+      ScalarValue fa_c = a1 + 2 * a2 * c + 3 * a3 * c2 + 4 * a4 * c3;
+      ScalarValue fa_cc = 2 * a2 + 6 * a3 * c + 12 * a4 * c2;
+      ScalarValue fb = b0 + b1 * c + b2 * c2;
+      ScalarValue fb_c = b1 + 2 * b2 * c;
+      ScalarValue fb_cc = ScalarValue(2 * b2);
+      ScalarValue h = 10.0 * n3 - 15.0 * n4 + 6.0 * n5;
+      ScalarValue hn = 30.0 * n2 - 60.0 * n3 + 30.0 * n4;
+      ScalarGrad mu_grad = -(cx * ((1.0 - h) * fa_cc + h * fb_cc) + nx * ((fb_c - fa_c) * hn));
+      ScalarGrad dcdt_vec = ScalarValue(Mc) * -mu_grad;
+      ScalarValue dndt_val = -Mn * (fb - fa) * hn;
+      ScalarGrad dndt_vec = ScalarValue(Kn * Mn) * nx;
+      variable_list.set_value_term(0, c);
+      variable_list.set_gradient_term(0, -dt * dcdt_vec);
+      variable_list.set_value_term(1, n + dt * dndt_val);
+      variable_list.set_gradient_term(1, -dt * dndt_vec);
+    } else if (solve_block_id == 1) {
+      const ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      const ScalarGrad cx = variable_list.template get_gradient<Scalar, Current>(0);
+      const ScalarValue n = variable_list.template get_value<Scalar, Current>(1);
+      const ScalarGrad nx = variable_list.template get_gradient<Scalar, Current>(1);
+      const ScalarValue c2 = c * c;
+      const ScalarValue c3 = c * c2;
+      const ScalarValue c4 = c2 * c2;
+      const ScalarValue n2 = n * n;
+      const ScalarValue n3 = n * n2;
+      const ScalarValue n4 = n2 * n2;
+      const ScalarValue n5 = n * n4;
+      ScalarValue fa = a0 + a1 * c + a2 * c2 + a3 * c3 + a4 * c4;
+      ScalarValue fb = b0 + b1 * c + b2 * c2;
+      ScalarValue h = 10.0 * n3 - 15.0 * n4 + 6.0 * n5;
+      ScalarValue f_chem = (1.0 - h) * fa + h * fb;
+      ScalarValue f_grad = 0.5 * Kn * nx * nx;
+      variable_list.set_value_term(2, f_chem + f_grad);
+      variable_list.set_value_term(3, cx.norm());
+    }
+  }
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
+};
+
+}  // namespace ppf

@@ -1,0 +1,1126 @@
+// Host runtime + C ABI of the GB300 matrix-free engine.
+//
+// Host side (built once per handle, then uploaded):
+//   * mesh: uniform hyper-rectangle of nc[d] = subdivisions[d] * 2^refinement cells,
+//     node lattice nn[d] = k*nc[d] + 1 (RectangularMesh + refine_global,
+//     src/user_inputs/spatial_discretization.cc:133-177, src/core/triangulation_manager.cc:107-118);
+//   * deal.II DoF numbering as a map to lattice order, used only at the ABI boundary
+//     (src/core/dof_manager.cc:12-26);
+//   * constraint maps (periodic images -> master, Dirichlet rows, chains closed)
+//     (src/core/constraint_manager.cc:143-304);
+//   * inverse lumped mass with periodic-only constraints (include/prismspf/core/invm_manager.h:121-239);
+//   * per solve block: dependency slots and CellTables for the cell kernel.
+// Device side per explicit solve: zero accumulator -> cell kernel -> finalize kernel
+// (invM scale + constraints + non-finite flag), i.e. ExplicitSolver::solve_impl
+// (include/prismspf/solvers/explicit_solver.h:63-77). The increment loop follows
+// Problem::solve_increment (src/core/problem.cc:416-557) and rotates ages by pointer swap
+// (src/core/group_solution_handler.cc:369-403).
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ppf_gb300.h"
+#include "runtime.h"
+
+namespace ppf {
+
+// ------------------------------------------------------------------------------------------
+// model registry
+// ------------------------------------------------------------------------------------------
+static std::vector<const ModelOps*>& registry() {
+  static std::vector<const ModelOps*> r;
+  return r;
+}
+void register_model(const ModelOps* ops) { registry().push_back(ops); }
+const ModelOps* find_model(const char* name) {
+  for (auto* m : registry())
+    if (name && std::strcmp(m->name, name) == 0) return m;
+  return nullptr;
+}
+
+// ------------------------------------------------------------------------------------------
+// Gauss-Lobatto rule on [0,1]: nodes are the endpoints and the roots of P'_{n-1}; the
+// derivative matrix is built from barycentric weights.
+// ------------------------------------------------------------------------------------------
+struct GLRule {
+  int n;
+  double x[pg::MAX_N], w[pg::MAX_N], D[pg::MAX_N][pg::MAX_N];
+};
+
+static void legendre_pd(int N, double t, double& p, double& dp, double& d2p) {
+  // P_N and its first two derivatives at t in (-1,1) by the three-term recurrence
+  double p0 = 1.0, p1 = t;
+  if (N == 0) { p = 1; dp = 0; d2p = 0; return; }
+  for (int m = 2; m <= N; ++m) {
+    const double p2 = ((2 * m - 1) * t * p1 - (m - 1) * p0) / m;
+    p0 = p1;
+    p1 = p2;
+  }
+  p = p1;
+  dp = N * (p0 - t * p1) / (1.0 - t * t);
+  d2p = (2.0 * t * dp - N * (N + 1.0) * p) / (1.0 - t * t);
+}
+
+static GLRule gauss_lobatto(int n) {
+  GLRule r{};
+  r.n = n;
+  const int N = n - 1;
+  double t[pg::MAX_N];
+  t[0] = -1.0;
+  t[n - 1] = 1.0;
+  for (int i = 1; i < n - 1; ++i) {
+    double z = std::cos(M_PI * (N - i) / N);  // ascending Chebyshev-Lobatto start
+    for (int it = 0; it < 64; ++it) {
+      double p, dp, d2p;
+      legendre_pd(N, z, p, dp, d2p);
+      const double step = dp / d2p;
+      z -= step;
+      if (std::fabs(step) <= 1e-16) break;
+    }
+    t[i] = z;
+  }
+  for (int i = 0; i < n; ++i) {
+    double p, dp, d2p;
+    if (i == 0 || i == n - 1) {
+      p = (i == 0 && (N % 2)) ? -1.0 : 1.0;
+    } else {
+      legendre_pd(N, t[i], p, dp, d2p);
+    }
+    r.x[i] = 0.5 * (1.0 + t[i]);
+    r.w[i] = 1.0 / (N * (N + 1.0) * p * p);  // half of 2/(N(N+1)P^2) for [0,1]
+  }
+  for (int i = 0; i < n / 2; ++i) {  // exact symmetry
+    const double a = 0.5 * (r.x[i] + 1.0 - r.x[n - 1 - i]);
+    r.x[i] = a;
+    r.x[n - 1 - i] = 1.0 - a;
+    const double w = 0.5 * (r.w[i] + r.w[n - 1 - i]);
+    r.w[i] = r.w[n - 1 - i] = w;
+  }
+  if (n % 2) r.x[n / 2] = 0.5;
+  double bw[pg::MAX_N];
+  for (int j = 0; j < n; ++j) {
+    double prod = 1.0;
+    for (int m = 0; m < n; ++m)
+      if (m != j) prod *= r.x[j] - r.x[m];
+    bw[j] = 1.0 / prod;
+  }
+  for (int i = 0; i < n; ++i) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        r.D[i][j] = bw[j] / (bw[i] * (r.x[i] - r.x[j]));
+        diag -= r.D[i][j];
+      }
+    r.D[i][i] = diag;
+  }
+  return r;
+}
+
+// ------------------------------------------------------------------------------------------
+// cell tables
+// ------------------------------------------------------------------------------------------
+template <int dim, int degree>
+static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
+                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
+                                              const signed char* slot_comp0, const signed char* out_of,
+                                              const signed char* out_row0) {
+  using Tab = pg::CellTables<dim, degree>;
+  constexpr int n = degree + 1, nq = Tab::nq;
+  Tab t;
+  std::memset(&t, 0, sizeof(t));
+  const GLRule g = gauss_lobatto(n);
+  double detJ = 1.0;
+  for (int d = 0; d < dim; ++d) detJ *= h[d];
+  for (int d = 0; d < dim; ++d)
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        t.Dh[d][i][j] = g.D[i][j] / h[d];
+        double s = 0.0;
+        for (int m = 0; m < n; ++m) s += g.D[i][m] * g.D[m][j];
+        t.D2h[d][i][j] = s / (h[d] * h[d]);
+      }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) t.Dt[i][j] = g.D[j][i];
+  for (int q = 0; q < nq; ++q) {
+    double w = detJ;
+    int r = q;
+    for (int d = 0; d < dim; ++d) {
+      w *= g.w[r % n];
+      r /= n;
+    }
+    t.jxw[q] = w;
+    for (int d = 0; d < dim; ++d) t.jxw_ih[d][q] = w / h[d];
+  }
+  for (int d = 0; d < 3; ++d) {
+    t.lo[d] = d < dim ? lo[d] : 0.0;
+    t.h[d] = d < dim ? h[d] : 1.0;
+  }
+  for (int i = 0; i < n; ++i) t.gl_x[i] = g.x[i];
+  t.vol = detJ;
+  std::memcpy(t.slot_of, slot_of, sizeof(t.slot_of));
+  std::memcpy(t.slot_comp0, slot_comp0, sizeof(t.slot_comp0));
+  std::memcpy(t.out_of, out_of, sizeof(t.out_of));
+  std::memcpy(t.out_row0, out_row0, sizeof(t.out_row0));
+  std::vector<unsigned char> out(sizeof(Tab));
+  std::memcpy(out.data(), &t, sizeof(Tab));
+  return out;
+}
+
+#define PPF_DD_SWITCH(F, ...)                                  \
+  switch (dim * 10 + degree) {                                 \
+    case 21: return F<2, 1>(__VA_ARGS__);                       \
+    case 22: return F<2, 2>(__VA_ARGS__);                       \
+    case 23: return F<2, 3>(__VA_ARGS__);                       \
+    case 24: return F<2, 4>(__VA_ARGS__);                       \
+    case 31: return F<3, 1>(__VA_ARGS__);                       \
+    case 32: return F<3, 2>(__VA_ARGS__);                       \
+    case 33: return F<3, 3>(__VA_ARGS__);                       \
+    case 34: return F<3, 4>(__VA_ARGS__);                       \
+    default: break;                                            \
+  }
+
+std::vector<unsigned char> build_cell_tables(int dim, int degree, const double* lo, const double* h,
+                                             const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
+                                             const signed char* slot_comp0, const signed char* out_of,
+                                             const signed char* out_row0) {
+  PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0)
+  return {};
+}
+
+template <int dim, int degree>
+static int threads_impl() { return CellShape<dim, degree>::threads; }
+int cell_threads(int dim, int degree) {
+  PPF_DD_SWITCH(threads_impl)
+  return 0;
+}
+template <int dim, int degree>
+static size_t smem_impl(int a, int b) { return cell_smem_bytes<dim, degree>(a, b); }
+size_t cell_smem(int dim, int degree, int nrows_in, int nrows_out) {
+  PPF_DD_SWITCH(smem_impl, nrows_in, nrows_out)
+  return 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// device kernels of the runtime
+// ------------------------------------------------------------------------------------------
+
+// u = invM (.) acc with constraints: masters/free rows scale their own accumulator, periodic
+// images copy their master's result, Dirichlet rows take their value.
+__global__ void finalize_explicit_kernel(double* __restrict__ u, const double* __restrict__ acc,
+                                         const double* __restrict__ invm, const int* __restrict__ cmap,
+                                         const double* __restrict__ dvals, long long N, int* err) {
+  const int c = blockIdx.y;
+  const long long base = c * N;
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const long long gi = base + i;
+    const int cm = cmap ? cmap[gi] : (int)gi;
+    double v;
+    if (cm >= 0) v = invm[cm - base] * acc[cm];
+    else v = dvals[-1 - cm];
+    bad |= !isfinite(v);
+    u[gi] = v;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(err, int(pg::ERR_NONFINITE));
+}
+
+// dst = scale (.) acc on unconstrained rows, 0 on constrained rows (MFOperator::compute_operator
+// leaves constrained rows of dst untouched after zeroing, then scales).
+__global__ void finalize_apply_kernel(double* __restrict__ dst, const double* __restrict__ acc,
+                                      const double* __restrict__ scale, const int* __restrict__ cmap, long long N) {
+  const int c = blockIdx.y;
+  const long long base = c * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const long long gi = base + i;
+    const int cm = cmap ? cmap[gi] : (int)gi;
+    double v = 0.0;
+    if (cm == (int)gi) v = scale ? acc[gi] * scale[i] : acc[gi];
+    dst[gi] = v;
+  }
+}
+
+// AffineConstraints::distribute on a lattice vector
+__global__ void distribute_kernel(double* __restrict__ u, const int* __restrict__ cmap,
+                                  const double* __restrict__ dvals, long long len) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const int cm = cmap[i];
+    if (cm == (int)i) continue;
+    u[i] = cm >= 0 ? u[cm] : dvals[-1 - cm];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// handle
+// ------------------------------------------------------------------------------------------
+struct FieldState {
+  int rank = 0, ncomp = 1;
+  long long len = 0;
+  int n_old = 0;
+  double* cur = nullptr;
+  double* old[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* acc = nullptr;
+  int* cmap = nullptr;  // nullptr when the field has no constraints
+  double* dvals = nullptr;
+  std::vector<int> h_cmap;
+  std::vector<double> h_dvals;
+  bool constrained = false;
+};
+
+struct BlockPlan {
+  int nslots = 0;
+  int slot_field[pg::MAX_SLOTS];
+  int slot_age[pg::MAX_SLOTS];
+  int nrows_in = 0, nrows_out = 0;
+  void* d_tables = nullptr;
+  bool valid = false;
+};
+
+struct BlockState {
+  ppf_block_desc desc;
+  BlockPlan plan[2];  // rhs, lhs
+};
+
+}  // namespace ppf
+
+struct ppf_handle_s {
+  ppf_mesh_desc mesh;
+  int dim = 2, k = 1, n = 2;
+  int nc[3] = {1, 1, 1}, nn[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  long long N = 0, ncells = 0;
+  std::vector<ppf::FieldState> fields;
+  std::vector<ppf::BlockState> blocks;
+  const ppf::ModelOps* model = nullptr;
+  std::vector<unsigned char> model_obj;
+  double* d_invm = nullptr;
+  double* d_invm_sqrt = nullptr;
+  std::vector<double> h_invm;
+  int* d_err = nullptr;
+  cudaStream_t stream = nullptr;      // stream all work is queued on
+  cudaStream_t own_stream = nullptr;  // the handle's own stream
+  prismspf::SimulationTimer timer;
+  double dt = 0.0;
+  std::string err;
+  bool use_graph = true;
+  double* d_scratch_src = nullptr;  // ppf_apply host-path staging
+  double* d_scratch_dst = nullptr;
+  long long scratch_len = 0;
+  // kernel timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  long long cell_launches = 0;
+  long long all_launches = 0;
+};
+
+namespace ppf {
+
+static int fail(ppf_handle h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define PPF_CUDA(h, call)                                                                    \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// lattice node index of periodic master (images folded onto the lower face)
+static long long periodic_master(const ppf_handle h, long long node) {
+  long long I = node % h->nn[0];
+  long long J = (node / h->nn[0]) % h->nn[1];
+  long long K = node / ((long long)h->nn[0] * h->nn[1]);
+  if (h->mesh.periodic[0] && I == h->nn[0] - 1) I = 0;
+  if (h->dim > 1 && h->mesh.periodic[1] && J == h->nn[1] - 1) J = 0;
+  if (h->dim > 2 && h->mesh.periodic[2] && K == h->nn[2] - 1) K = 0;
+  return (K * h->nn[1] + J) * h->nn[0] + I;
+}
+
+static bool node_on_boundary(const ppf_handle h, long long node, int bid) {
+  const int d = bid / 2;
+  if (d >= h->dim) return false;
+  long long c[3] = {node % h->nn[0], (node / h->nn[0]) % h->nn[1], node / ((long long)h->nn[0] * h->nn[1])};
+  return (bid % 2 == 0) ? c[d] == 0 : c[d] == h->nn[d] - 1;
+}
+
+static void build_constraints(ppf_handle h, FieldState& F, const ppf_field_desc& fd) {
+  const long long N = h->N;
+  F.h_cmap.resize(F.len);
+  F.h_dvals.clear();
+  bool any = false;
+  for (int c = 0; c < F.ncomp; ++c)
+    for (long long i = 0; i < N; ++i) {
+      const long long m = periodic_master(h, i);
+      F.h_cmap[c * N + i] = (int)(c * N + m);
+      any |= (m != i);
+    }
+  for (int c = 0; c < F.ncomp; ++c)
+    for (int b = 0; b < 2 * h->dim; ++b) {
+      if (!fd.dirichlet[c][b]) continue;
+      for (long long i = 0; i < N; ++i) {
+        const long long gi = c * N + i;
+        if (!node_on_boundary(h, i, b) || F.h_cmap[gi] != (int)gi) continue;
+        F.h_cmap[gi] = -1 - (int)F.h_dvals.size();
+        F.h_dvals.push_back(fd.dirichlet_value[c][b]);
+        any = true;
+      }
+    }
+  // close chains: an image whose master is a Dirichlet row becomes that Dirichlet row
+  for (long long gi = 0; gi < F.len; ++gi) {
+    const int m = F.h_cmap[gi];
+    if (m >= 0 && m != (int)gi && F.h_cmap[m] < 0) F.h_cmap[gi] = F.h_cmap[m];
+  }
+  F.constrained = any;
+}
+
+static void build_invm(ppf_handle h) {
+  const int dim = h->dim, n = h->n, k = h->k;
+  const GLRule g = gauss_lobatto(n);
+  double detJ = 1.0;
+  for (int d = 0; d < dim; ++d) detJ *= h->h[d];
+  std::vector<double> jxw(h->N, 0.0);
+  // lumped mass: sum over cells of GL weight x detJ at each cell node, periodic images
+  // condensed onto their masters
+  const int nq = dim == 2 ? n * n : n * n * n;
+  for (long long cell = 0; cell < h->ncells; ++cell) {
+    const long long cx = cell % h->nc[0];
+    const long long cy = dim > 1 ? (cell / h->nc[0]) % h->nc[1] : 0;
+    const long long cz = dim > 2 ? cell / ((long long)h->nc[0] * h->nc[1]) : 0;
+    for (int q = 0; q < nq; ++q) {
+      const int a = q % n, b = (q / n) % n, c = dim > 2 ? q / (n * n) : 0;
+      const double w = detJ * g.w[a] * g.w[b] * (dim > 2 ? g.w[c] : 1.0);
+      const long long node = ((k * cz + c) * h->nn[1] + (k * cy + b)) * h->nn[0] + (k * cx + a);
+      jxw[periodic_master(h, node)] += w;
+    }
+  }
+  h->h_invm.resize(h->N);
+  std::vector<double> isq(h->N);
+  for (long long i = 0; i < h->N; ++i) {
+    h->h_invm[i] = jxw[i] == 0.0 ? 0.0 : 1.0 / jxw[i];
+    isq[i] = std::sqrt(h->h_invm[i]);
+  }
+  cudaMalloc(&h->d_invm, sizeof(double) * h->N);
+  cudaMalloc(&h->d_invm_sqrt, sizeof(double) * h->N);
+  cudaMemcpy(h->d_invm, h->h_invm.data(), sizeof(double) * h->N, cudaMemcpyHostToDevice);
+  cudaMemcpy(h->d_invm_sqrt, isq.data(), sizeof(double) * h->N, cudaMemcpyHostToDevice);
+}
+
+// deal.II distribute_dofs order as a map dealii index -> lattice index (component-major).
+// Cells: coarse cells lexicographic, fine cells of each coarse cell in Morton order with the
+// x bit lowest at every level (refine_global child order). Per cell the geometric objects
+// come in deal.II order: vertices (x + 2y + 4z), lines (2-D: x=0, x=1, y=0, y=1; 3-D: those
+// four at z=0, again at z=1, then the four z-lines at (0,0),(1,0),(0,1),(1,1)), faces
+// (x=0, x=1, y=0, y=1, z=0, z=1), interior. An object is numbered the first time a cell
+// reaches it; a vector element numbers all components of an object one after the other.
+static std::vector<long long> dealii_dof_map(const ppf_handle h, int ncomp) {
+  const int dim = h->dim, k = h->k;
+  const int r = h->mesh.global_refinement;
+  const long long N = h->N;
+  std::vector<long long> map;
+  map.reserve(N * ncomp);
+  std::vector<char> seen(N, 0);
+  // object list in cell-local lattice offsets
+  std::vector<std::vector<std::array<int, 3>>> objs;
+  const int nv = 1 << dim;
+  for (int v = 0; v < nv; ++v) objs.push_back({{(v & 1) * k, ((v >> 1) & 1) * k, ((v >> 2) & 1) * k}});
+  int lines[12][4];  // running axis, fixed x/y/z in units of k
+  int nlines = 0;
+  auto add_line = [&](int ax, int fx, int fy, int fz) {
+    lines[nlines][0] = ax; lines[nlines][1] = fx; lines[nlines][2] = fy; lines[nlines][3] = fz; ++nlines;
+  };
+  for (int zz = 0; zz < (dim == 3 ? 2 : 1); ++zz) {
+    add_line(1, 0, 0, zz);
+    add_line(1, 1, 0, zz);
+    add_line(0, 0, 0, zz);
+    add_line(0, 0, 1, zz);
+  }
+  if (dim == 3) {
+    add_line(2, 0, 0, 0);
+    add_line(2, 1, 0, 0);
+    add_line(2, 0, 1, 0);
+    add_line(2, 1, 1, 0);
+  }
+  for (int l = 0; l < nlines; ++l) {
+    std::vector<std::array<int, 3>> o;
+    for (int t = 1; t < k; ++t) {
+      std::array<int, 3> p = {lines[l][1] * k, lines[l][2] * k, lines[l][3] * k};
+      p[lines[l][0]] = t;
+      o.push_back(p);
+    }
+    objs.push_back(o);
+  }
+  if (dim == 3) {
+    for (int f = 0; f < 6; ++f) {
+      const int ax = f / 2;
+      const int t0 = ax == 0 ? 1 : 0, t1 = ax == 2 ? 1 : 2;
+      std::vector<std::array<int, 3>> o;
+      for (int b = 1; b < k; ++b)
+        for (int a = 1; a < k; ++a) {
+          std::array<int, 3> p = {0, 0, 0};
+          p[ax] = (f % 2) * k;
+          p[t0] = a;
+          p[t1] = b;
+          o.push_back(p);
+        }
+      objs.push_back(o);
+    }
+  }
+  {
+    std::vector<std::array<int, 3>> o;
+    for (int c = 1; c < (dim == 3 ? k : 2); ++c)
+      for (int b = 1; b < k; ++b)
+        for (int a = 1; a < k; ++a) o.push_back({a, b, dim == 3 ? c : 0});
+    objs.push_back(o);
+  }
+  const long long per_coarse = 1LL << (r * dim);
+  const int sub[3] = {h->mesh.subdivisions[0], dim > 1 ? h->mesh.subdivisions[1] : 1,
+                      dim > 2 ? h->mesh.subdivisions[2] : 1};
+  for (int CZ = 0; CZ < sub[2]; ++CZ)
+    for (int CY = 0; CY < sub[1]; ++CY)
+      for (int CX = 0; CX < sub[0]; ++CX)
+        for (long long m = 0; m < per_coarse; ++m) {
+          long long f[3] = {0, 0, 0};
+          for (int lvl = 0; lvl < r; ++lvl)
+            for (int d = 0; d < dim; ++d) f[d] |= ((m >> (lvl * dim + d)) & 1LL) << lvl;
+          const long long cx = (long long)CX * (1LL << r) + f[0];
+          const long long cy = (long long)CY * (1LL << r) + f[1];
+          const long long cz = (long long)CZ * (1LL << r) + f[2];
+          for (auto& o : objs) {
+            if (o.empty()) continue;
+            const auto& p0 = o[0];
+            const long long n0 = ((cz * k + p0[2]) * h->nn[1] + (cy * k + p0[1])) * h->nn[0] + (cx * k + p0[0]);
+            if (seen[n0]) continue;
+            for (int c = 0; c < ncomp; ++c)
+              for (auto& p : o) {
+                const long long nd = ((cz * k + p[2]) * h->nn[1] + (cy * k + p[1])) * h->nn[0] + (cx * k + p[0]);
+                seen[nd] = 1;
+                map.push_back(c * N + nd);
+              }
+          }
+        }
+  return map;
+}
+
+static int plan_block(ppf_handle h, BlockState& B, int which) {
+  BlockPlan& P = B.plan[which];
+  const ppf_block_desc& d = B.desc;
+  signed char slot_of[pg::MAX_FIELDS][pg::NAGE];
+  signed char slot_comp0[pg::MAX_SLOTS];
+  signed char out_of[pg::MAX_FIELDS];
+  signed char out_row0[pg::MAX_OUTS];
+  std::memset(slot_of, -1, sizeof(slot_of));
+  std::memset(slot_comp0, 0, sizeof(slot_comp0));
+  std::memset(out_of, -1, sizeof(out_of));
+  std::memset(out_row0, 0, sizeof(out_row0));
+  const int nf = (int)h->fields.size();
+  P.nslots = 0;
+  P.nrows_in = 0;
+  for (int f = 0; f < nf; ++f)
+    for (int a = 0; a < pg::NAGE; ++a) {
+      const int fl = which == 0 ? d.dep_rhs[f][a] : d.dep_lhs[f][a];
+      if (!fl) continue;
+      if (P.nslots >= pg::MAX_SLOTS) return fail(h, PPF_ERR_UNSUPPORTED, "too many dependencies in one block");
+      slot_of[f][a] = (signed char)P.nslots;
+      slot_comp0[P.nslots] = (signed char)P.nrows_in;
+      P.slot_field[P.nslots] = f;
+      P.slot_age[P.nslots] = a;
+      P.nrows_in += h->fields[f].ncomp;
+      P.nslots++;
+    }
+  P.nrows_out = 0;
+  if (d.n_fields > pg::MAX_OUTS) return fail(h, PPF_ERR_UNSUPPORTED, "too many fields in one block");
+  for (int i = 0; i < d.n_fields; ++i) {
+    const int f = d.field_indices[i];
+    out_of[f] = (signed char)i;
+    out_row0[i] = (signed char)P.nrows_out;
+    P.nrows_out += h->fields[f].ncomp * (1 + h->dim);
+  }
+  if (P.nrows_in + P.nrows_out > 127) return fail(h, PPF_ERR_UNSUPPORTED, "block too large");
+  double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
+  auto tab = build_cell_tables(h->dim, h->k, lo, h->h, slot_of, slot_comp0, out_of, out_row0);
+  if (tab.empty()) return fail(h, PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
+  PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
+  PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+  P.valid = true;
+  return PPF_OK;
+}
+
+static double* state_ptr(ppf_handle h, int f, int age) {
+  FieldState& F = h->fields[f];
+  if (age == 0) return F.cur;
+  if (age >= 1 && age <= 4) return F.old[age - 1];
+  return nullptr;
+}
+
+// Launches the cell kernel of block b (which: 0 rhs, 1 lhs) accumulating into each block
+// field's acc. `src` supplies the SRC dependency per block field (may be null).
+static int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
+  BlockState& B = h->blocks[b];
+  BlockPlan& P = B.plan[which];
+  if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
+  CellLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  for (int d = 0; d < 3; ++d) {
+    L.nc[d] = h->nc[d];
+    L.nn[d] = h->nn[d];
+  }
+  L.N = h->N;
+  L.ncells = h->ncells;
+  L.nslots = P.nslots;
+  for (int s = 0; s < P.nslots; ++s) {
+    const int f = P.slot_field[s], a = P.slot_age[s];
+    FieldState& F = h->fields[f];
+    SlotDesc& sd = L.slots[s];
+    sd.ncomp = F.ncomp;
+    if (a == 5) {
+      int pos = -1;
+      for (int i = 0; i < B.desc.n_fields; ++i)
+        if (B.desc.field_indices[i] == f) pos = i;
+      if (pos < 0 || !src || !src[pos]) return fail(h, PPF_ERR_ARG, "src dependency without a src vector");
+      sd.ptr = src[pos];
+      sd.constrained_read = which == 1 && F.constrained;
+      sd.cmap = F.cmap;
+    } else {
+      sd.ptr = state_ptr(h, f, a);
+      if (!sd.ptr) return fail(h, PPF_ERR_ARG, "dependency on an age that is not stored");
+      sd.constrained_read = 0;
+      sd.cmap = nullptr;
+    }
+  }
+  L.nout = B.desc.n_fields;
+  for (int i = 0; i < B.desc.n_fields; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    L.outs[i].acc = F.acc;
+    L.outs[i].cmap = F.constrained ? F.cmap : nullptr;
+    L.outs[i].ncomp = F.ncomp;
+  }
+  L.nrows_in = P.nrows_in;
+  L.nrows_out = P.nrows_out;
+  L.tables = P.d_tables;
+  L.timer = h->timer;
+  L.block_id = (unsigned)B.desc.id;
+  L.err = h->d_err;
+  const size_t smem = cell_smem(h->dim, h->k, P.nrows_in, P.nrows_out);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (h->timing) {
+    while (h->ev_pool.size() < h->ev_used + 2) {
+      cudaEvent_t ev;
+      PPF_CUDA(h, cudaEventCreate(&ev));
+      h->ev_pool.push_back(ev);
+    }
+    e0 = h->ev_pool[h->ev_used++];
+    e1 = h->ev_pool[h->ev_used++];
+    PPF_CUDA(h, cudaEventRecord(e0, h->stream));
+  }
+  cudaError_t e = h->model->launch(h->dim, h->k, which == 1, L, h->model_obj.data(), smem, h->stream);
+  if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("cell kernel launch: ") + cudaGetErrorString(e));
+  if (h->timing) PPF_CUDA(h, cudaEventRecord(e1, h->stream));
+  h->cell_launches++;
+  h->all_launches++;
+  return PPF_OK;
+}
+
+static unsigned grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+static int explicit_solve(ppf_handle h, int b) {
+  BlockState& B = h->blocks[b];
+  for (int i = 0; i < B.desc.n_fields; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * F.len, h->stream));
+  }
+  int rc = launch_cell(h, b, 0, nullptr);
+  if (rc) return rc;
+  for (int i = 0; i < B.desc.n_fields; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    dim3 grid(grid_for(h->N), F.ncomp);
+    finalize_explicit_kernel<<<grid, 256, 0, h->stream>>>(F.cur, F.acc, h->d_invm, F.constrained ? F.cmap : nullptr,
+                                                          F.dvals, h->N, h->d_err);
+    PPF_CUDA(h, cudaGetLastError());
+    h->all_launches++;
+  }
+  return PPF_OK;
+}
+
+static int check_err(ppf_handle h) {
+  int e = 0;
+  PPF_CUDA(h, cudaMemcpyAsync(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (e) {
+    PPF_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream));
+    if (e & pg::ERR_NONFINITE) return fail(h, PPF_ERR_NAN, "non-finite value in a solution field");
+    if (e & pg::ERR_UNDECLARED_DEPENDENCY)
+      return fail(h, PPF_ERR_DEPENDENCY, "a callback read a dependency its solve block does not declare");
+    if (e & pg::ERR_UNDECLARED_SUBMISSION)
+      return fail(h, PPF_ERR_DEPENDENCY, "a callback submitted a term for a field outside its solve block");
+    return fail(h, PPF_ERR_CUDA, "device error flag set");
+  }
+  return PPF_OK;
+}
+
+static void rotate(ppf_handle h) {
+  for (auto& F : h->fields)
+    for (int age = F.n_old - 1; age >= 0; --age) {
+      if (age > 0) std::swap(F.old[age], F.old[age - 1]);
+      else std::swap(F.old[0], F.cur);
+    }
+}
+
+static int solve_increment(ppf_handle h, int output_every) {
+  const unsigned inc = h->timer.get_increment();
+  for (size_t b = 0; b < h->blocks.size(); ++b) {
+    const ppf_block_desc& d = h->blocks[b].desc;
+    if (d.solve_timing == PPF_POSTPROCESS || d.solve_timing == PPF_NUCLEATION_RATE) {
+      if (output_every <= 0 || inc % (unsigned)output_every != 0) continue;
+    }
+    if (inc == 0 && d.solve_timing == PPF_PRIMARY) {
+      // initial condition is the uploaded current vector (SolverBase::solve at increment 0)
+    } else if (d.solve_type == PPF_EXPLICIT) {
+      int rc = explicit_solve(h, (int)b);
+      if (rc) return rc;
+    } else if (d.solve_type == PPF_CONSTANT) {
+      // constant fields keep their values
+    } else {
+      return fail(h, PPF_ERR_UNSUPPORTED, "linear/Newton blocks are driven through the solver entry points");
+    }
+    if (inc == 0) {
+      for (int i = 0; i < d.n_fields; ++i) {
+        FieldState& F = h->fields[d.field_indices[i]];
+        for (int a = 0; a < F.n_old; ++a)
+          PPF_CUDA(h, cudaMemcpyAsync(F.old[a], F.cur, sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
+      }
+    }
+  }
+  rotate(h);
+  h->timer.increment(h->dt);
+  return PPF_OK;
+}
+
+}  // namespace ppf
+
+using namespace ppf;
+
+// ------------------------------------------------------------------------------------------
+// C ABI
+// ------------------------------------------------------------------------------------------
+extern "C" {
+
+static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields, const ppf_block_desc* blocks,
+               int n_blocks, const char* model, const double* constants, int n_constants, double dt,
+               std::unique_ptr<ppf_handle_s>& h, std::string& cerr) {
+  if (!mesh || mesh->dim < 2 || mesh->dim > 3 || mesh->degree < 1 || mesh->degree > 4) {
+    cerr = "mesh: dim must be 2 or 3 and degree 1..4";
+    return PPF_ERR_ARG;
+  }
+  if (n_fields < 1 || n_fields > PPF_MAX_FIELDS || n_blocks < 0 || n_blocks > PPF_MAX_BLOCKS) return PPF_ERR_ARG;
+  h->mesh = *mesh;
+  h->dim = mesh->dim;
+  h->k = mesh->degree;
+  h->n = h->k + 1;
+  h->ncells = 1;
+  h->N = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (d < h->dim) {
+      if (mesh->subdivisions[d] < 1 || mesh->size[d] <= 0 || mesh->global_refinement < 0) return PPF_ERR_ARG;
+      h->nc[d] = mesh->subdivisions[d] << mesh->global_refinement;
+      h->nn[d] = h->k * h->nc[d] + 1;
+      h->h[d] = mesh->size[d] / h->nc[d];
+    } else {
+      h->nc[d] = 1;
+      h->nn[d] = 1;
+      h->h[d] = 1.0;
+    }
+    h->ncells *= h->nc[d];
+    h->N *= h->nn[d];
+  }
+  if (h->N * 3 >= (1LL << 31)) return PPF_ERR_UNSUPPORTED;  // int32 constraint maps
+  h->model = find_model(model);
+  if (!h->model) {
+    cerr = std::string("unknown model: ") + (model ? model : "(null)");
+    return PPF_ERR_ARG;
+  }
+  h->dt = dt;
+  h->timer = prismspf::SimulationTimer(dt, 0.0);
+  h->model_obj.resize(8192);
+  std::string merr;
+  const size_t osz = h->model->make_object(h->dim, h->k, constants, n_constants, h->model_obj.data(),
+                                           h->model_obj.size(), &merr);
+  if (!osz) {
+    cerr = merr;
+    return PPF_ERR_ARG;
+  }
+  h->model_obj.resize(osz);
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cerr = "no CUDA device available";
+    return PPF_ERR_CUDA;
+  }
+  h->stream = h->own_stream;
+  if (cudaMalloc(&h->d_err, sizeof(int)) != cudaSuccess) return PPF_ERR_CUDA;
+  cudaMemset(h->d_err, 0, sizeof(int));
+  // fields
+  h->fields.resize(n_fields);
+  for (int f = 0; f < n_fields; ++f) {
+    FieldState& F = h->fields[f];
+    F.rank = fields[f].rank;
+    F.ncomp = F.rank == 0 ? 1 : h->dim;
+    F.len = F.ncomp * h->N;
+    build_constraints(h.get(), F, fields[f]);
+  }
+  // blocks and the ages each field must keep
+  h->blocks.resize(n_blocks);
+  for (int b = 0; b < n_blocks; ++b) {
+    h->blocks[b].desc = blocks[b];
+    const ppf_block_desc& d = blocks[b];
+    if (d.n_fields < 1 || d.n_fields > PPF_MAX_FIELDS) return PPF_ERR_ARG;
+    for (int i = 0; i < d.n_fields; ++i)
+      if (d.field_indices[i] < 0 || d.field_indices[i] >= n_fields) return PPF_ERR_ARG;
+    for (int f = 0; f < n_fields; ++f)
+      for (int a = 1; a <= 4; ++a)
+        if (d.dep_rhs[f][a] || d.dep_lhs[f][a]) h->fields[f].n_old = std::max(h->fields[f].n_old, a);
+  }
+  for (auto& F : h->fields) {
+    if (cudaMalloc(&F.cur, sizeof(double) * F.len) != cudaSuccess) return PPF_ERR_CUDA;
+    cudaMemset(F.cur, 0, sizeof(double) * F.len);
+    for (int a = 0; a < F.n_old; ++a) {
+      if (cudaMalloc(&F.old[a], sizeof(double) * F.len) != cudaSuccess) return PPF_ERR_CUDA;
+      cudaMemset(F.old[a], 0, sizeof(double) * F.len);
+    }
+    if (cudaMalloc(&F.acc, sizeof(double) * F.len) != cudaSuccess) return PPF_ERR_CUDA;
+    if (cudaMalloc(&F.cmap, sizeof(int) * F.len) != cudaSuccess) return PPF_ERR_CUDA;
+    cudaMemcpy(F.cmap, F.h_cmap.data(), sizeof(int) * F.len, cudaMemcpyHostToDevice);
+    if (!F.h_dvals.empty()) {
+      if (cudaMalloc(&F.dvals, sizeof(double) * F.h_dvals.size()) != cudaSuccess) return PPF_ERR_CUDA;
+      cudaMemcpy(F.dvals, F.h_dvals.data(), sizeof(double) * F.h_dvals.size(), cudaMemcpyHostToDevice);
+    }
+  }
+  build_invm(h.get());
+  for (int b = 0; b < n_blocks; ++b) {
+    const ppf_block_desc& d = blocks[b];
+    bool any_rhs = false, any_lhs = false;
+    for (int f = 0; f < n_fields; ++f)
+      for (int a = 0; a < PPF_NAGE; ++a) {
+        any_rhs |= d.dep_rhs[f][a] != 0;
+        any_lhs |= d.dep_lhs[f][a] != 0;
+      }
+    if (plan_block(h.get(), h->blocks[b], 0) || (any_lhs && h->model->has_lhs && plan_block(h.get(), h->blocks[b], 1))) {
+      cerr = h->err;
+      return PPF_ERR_UNSUPPORTED;
+    }
+    (void)any_rhs;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    cerr = "CUDA error during set-up";
+    return PPF_ERR_CUDA;
+  }
+  return PPF_OK;
+}
+
+
+static thread_local std::string g_create_error;
+
+int ppf_create(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields, const ppf_block_desc* blocks,
+               int n_blocks, const char* model, const double* constants, int n_constants, double dt,
+               ppf_handle* out) {
+  if (!out) return PPF_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<ppf_handle_s> h(new ppf_handle_s());
+  g_create_error.clear();
+  const int rc = create_impl(mesh, fields, n_fields, blocks, n_blocks, model, constants, n_constants, dt, h, g_create_error);
+  if (rc != PPF_OK) {
+    if (g_create_error.empty()) g_create_error = "invalid problem description";
+    ppf_destroy(h.release());
+    return rc;
+  }
+  *out = h.release();
+  return PPF_OK;
+}
+
+void ppf_destroy(ppf_handle h) {
+  if (!h) return;
+  if (!h->own_stream) {  // set-up failed before any device work
+    delete h;
+    return;
+  }
+  cudaStreamSynchronize(h->stream);
+  for (auto& F : h->fields) {
+    cudaFree(F.cur);
+    for (int a = 0; a < 4; ++a) cudaFree(F.old[a]);
+    cudaFree(F.acc);
+    cudaFree(F.cmap);
+    cudaFree(F.dvals);
+  }
+  for (auto& B : h->blocks)
+    for (auto& P : B.plan) cudaFree(P.d_tables);
+  cudaFree(h->d_invm);
+  cudaFree(h->d_invm_sqrt);
+  cudaFree(h->d_err);
+  cudaFree(h->d_scratch_src);
+  cudaFree(h->d_scratch_dst);
+  for (auto ev : h->ev_pool) cudaEventDestroy(ev);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+}
+
+const char* ppf_last_error(ppf_handle h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+long long ppf_n_nodes(ppf_handle h) { return h ? h->N : -1; }
+long long ppf_n_cells(ppf_handle h) { return h ? h->ncells : -1; }
+long long ppf_field_length(ppf_handle h, int f) {
+  if (!h || f < 0 || f >= (int)h->fields.size()) return -1;
+  return h->fields[f].len;
+}
+
+int ppf_dof_map(ppf_handle h, int rank, long long* out) {
+  if (!h || !out || rank < 0 || rank > 1) return PPF_ERR_ARG;
+  auto m = dealii_dof_map(h, rank == 0 ? 1 : h->dim);
+  std::memcpy(out, m.data(), sizeof(long long) * m.size());
+  return PPF_OK;
+}
+
+int ppf_constraint_map(ppf_handle h, int f, int* out) {
+  if (!h || !out || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  std::memcpy(out, h->fields[f].h_cmap.data(), sizeof(int) * h->fields[f].len);
+  return PPF_OK;
+}
+
+int ppf_invm(ppf_handle h, double* out) {
+  if (!h || !out) return PPF_ERR_ARG;
+  std::memcpy(out, h->h_invm.data(), sizeof(double) * h->N);
+  return PPF_OK;
+}
+
+static int permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
+                      bool upload) {
+  FieldState& F = h->fields[f];
+  std::vector<double> tmp(F.len);
+  if (ordering == PPF_ORDER_LATTICE) {
+    if (upload) PPF_CUDA(h, cudaMemcpyAsync(dev_dst, host, sizeof(double) * F.len, cudaMemcpyHostToDevice, h->stream));
+    else PPF_CUDA(h, cudaMemcpyAsync(host, dev_src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->stream));
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PPF_OK;
+  }
+  if (ordering != PPF_ORDER_DEALII) return fail(h, PPF_ERR_ARG, "unknown ordering");
+  auto m = dealii_dof_map(h, F.ncomp);
+  if (upload) {
+    for (long long i = 0; i < F.len; ++i) tmp[m[i]] = host[i];
+    PPF_CUDA(h, cudaMemcpyAsync(dev_dst, tmp.data(), sizeof(double) * F.len, cudaMemcpyHostToDevice, h->stream));
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  } else {
+    PPF_CUDA(h, cudaMemcpyAsync(tmp.data(), dev_src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->stream));
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (long long i = 0; i < F.len; ++i) host[i] = tmp[m[i]];
+  }
+  return PPF_OK;
+}
+
+int ppf_upload_state(ppf_handle h, int f, int age, const double* host, int ordering) {
+  if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  double* p = state_ptr(h, f, age);
+  if (!p) return fail(h, PPF_ERR_ARG, "age not stored for this field");
+  return permute_io(h, f, const_cast<double*>(host), nullptr, p, ordering, true);
+}
+
+int ppf_download_state(ppf_handle h, int f, int age, double* host, int ordering) {
+  if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  double* p = state_ptr(h, f, age);
+  if (!p) return fail(h, PPF_ERR_ARG, "age not stored for this field");
+  return permute_io(h, f, host, p, nullptr, ordering, false);
+}
+
+int ppf_apply_constraints(ppf_handle h, int f) {
+  if (!h || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  FieldState& F = h->fields[f];
+  if (!F.constrained) return PPF_OK;
+  distribute_kernel<<<grid_for(F.len), 256, 0, h->stream>>>(F.cur, F.cmap, F.dvals, F.len);
+  PPF_CUDA(h, cudaGetLastError());
+  h->all_launches++;
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return PPF_OK;
+}
+
+int ppf_solve_block(ppf_handle h, int b) {
+  if (!h || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  int rc = explicit_solve(h, b);
+  if (rc) return rc;
+  return check_err(h);
+}
+
+int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
+  if (!h) return PPF_ERR_ARG;
+  while (h->timer.get_increment() <= n_increments) {
+    int rc = solve_increment(h, output_every);
+    if (rc) return rc;
+  }
+  return check_err(h);
+}
+
+int ppf_apply_device(ppf_handle h, int b, int which, const double* d_src, double* d_dst, int scale) {
+  if (!h || b < 0 || b >= (int)h->blocks.size() || which < 0 || which > 1) return PPF_ERR_ARG;
+  BlockState& B = h->blocks[b];
+  const double* srcs[PPF_MAX_FIELDS] = {};
+  long long off = 0;
+  for (int i = 0; i < B.desc.n_fields; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    srcs[i] = d_src ? d_src + off : nullptr;
+    PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * F.len, h->stream));
+    off += F.len;
+  }
+  int rc = launch_cell(h, b, which, srcs);
+  if (rc) return rc;
+  off = 0;
+  for (int i = 0; i < B.desc.n_fields; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    const double* sc = scale == 1 ? h->d_invm : (scale == 2 ? h->d_invm_sqrt : nullptr);
+    dim3 grid(grid_for(h->N), F.ncomp);
+    finalize_apply_kernel<<<grid, 256, 0, h->stream>>>(d_dst + off, F.acc, sc, F.constrained ? F.cmap : nullptr, h->N);
+    PPF_CUDA(h, cudaGetLastError());
+    h->all_launches++;
+    off += F.len;
+  }
+  return PPF_OK;
+}
+
+int ppf_apply(ppf_handle h, int b, int which, const double* src, double* dst, int scale) {
+  if (!h || b < 0 || b >= (int)h->blocks.size() || !dst) return PPF_ERR_ARG;
+  BlockState& B = h->blocks[b];
+  long long len = 0;
+  for (int i = 0; i < B.desc.n_fields; ++i) len += h->fields[B.desc.field_indices[i]].len;
+  if (len > h->scratch_len) {
+    cudaFree(h->d_scratch_src);
+    cudaFree(h->d_scratch_dst);
+    PPF_CUDA(h, cudaMalloc(&h->d_scratch_src, sizeof(double) * len));
+    PPF_CUDA(h, cudaMalloc(&h->d_scratch_dst, sizeof(double) * len));
+    h->scratch_len = len;
+  }
+  if (src) PPF_CUDA(h, cudaMemcpyAsync(h->d_scratch_src, src, sizeof(double) * len, cudaMemcpyHostToDevice, h->stream));
+  int rc = ppf_apply_device(h, b, which, src ? h->d_scratch_src : nullptr, h->d_scratch_dst, scale);
+  if (rc) return rc;
+  PPF_CUDA(h, cudaMemcpyAsync(dst, h->d_scratch_dst, sizeof(double) * len, cudaMemcpyDeviceToHost, h->stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return check_err(h);
+}
+
+int ppf_set_time(ppf_handle h, unsigned int increment, double time) {
+  if (!h) return PPF_ERR_ARG;
+  h->timer.set_increment(increment);
+  h->timer.set_time(time);
+  return PPF_OK;
+}
+
+int ppf_get_time(ppf_handle h, unsigned int* increment, double* time) {
+  if (!h) return PPF_ERR_ARG;
+  if (increment) *increment = h->timer.get_increment();
+  if (time) *time = h->timer.get_time();
+  return PPF_OK;
+}
+
+int ppf_set_use_graph(ppf_handle h, int on) {
+  if (!h) return PPF_ERR_ARG;
+  h->use_graph = on != 0;
+  return PPF_OK;
+}
+
+int ppf_state_device_ptr(ppf_handle h, int f, int age, double** out) {
+  if (!h || !out || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  *out = state_ptr(h, f, age);
+  return *out ? PPF_OK : PPF_ERR_ARG;
+}
+
+int ppf_synchronize(ppf_handle h) {
+  if (!h) return PPF_ERR_ARG;
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return PPF_OK;
+}
+
+int ppf_set_stream(ppf_handle h, void* stream) {
+  if (!h) return PPF_ERR_ARG;
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : h->own_stream;
+  return PPF_OK;
+}
+
+int ppf_kernel_timing(ppf_handle h, int enable) {
+  if (!h) return PPF_ERR_ARG;
+  h->timing = enable != 0;
+  return PPF_OK;
+}
+
+int ppf_kernel_stats(ppf_handle h, double* cell_ms, long long* cell_launches, long long* all_launches) {
+  if (!h) return PPF_ERR_ARG;
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  double total = 0.0;
+  for (size_t i = 0; i + 1 < h->ev_used; i += 2) {
+    float ms = 0.f;
+    PPF_CUDA(h, cudaEventElapsedTime(&ms, h->ev_pool[i], h->ev_pool[i + 1]));
+    total += ms;
+  }
+  if (cell_ms) *cell_ms = total;
+  if (cell_launches) *cell_launches = h->cell_launches;
+  if (all_launches) *all_launches = h->all_launches;
+  return PPF_OK;
+}
+
+int ppf_kernel_stats_reset(ppf_handle h) {
+  if (!h) return PPF_ERR_ARG;
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->ev_used = 0;
+  h->cell_launches = 0;
+  h->all_launches = 0;
+  return PPF_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// FP64 throughput probe (roofline denominator)
+// ------------------------------------------------------------------------------------------
+namespace ppf {
+__global__ void fp64_fma_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+  }
+  const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == -12345.678) out[0] = s;  // keeps the loop alive; never true
+}
+}  // namespace ppf
+
+extern "C" int ppf_device_fp64_peak(double* tflops) {
+  if (!tflops) return PPF_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PPF_ERR_CUDA;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double* d = nullptr;
+  if (cudaMalloc(&d, 64) != cudaSuccess) return PPF_ERR_CUDA;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, threads = 256, iters = 400;
+  ppf::fp64_fma_probe_kernel<<<blocks, threads>>>(d, 20, 0.999999, 1e-7);
+  cudaEventRecord(e0);
+  ppf::fp64_fma_probe_kernel<<<blocks, threads>>>(d, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0.f) return PPF_ERR_CUDA;
+  *tflops = 2.0 * 8 * 16 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
+  return PPF_OK;
+}

@@ -1,0 +1,39 @@
+// Internal host runtime of the GB300 engine (not part of the public ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "cell_kernel.cuh"
+
+namespace ppf {
+
+// A compiled PDE operator set (one user CustomPDE): how to build its device object from the
+// Model constants and how to launch its cell kernel for a (dim, degree, rhs|lhs).
+struct ModelOps {
+  const char* name;
+  bool has_lhs;
+  // fills `out` (capacity `cap` bytes) with the device object; returns its size, 0 on error
+  size_t (*make_object)(int dim, int degree, const double* c, int nc, void* out, size_t cap, std::string* err);
+  // launches cell_kernel<PDE,dim,degree,lhs>; grid = number of thread blocks
+  cudaError_t (*launch)(int dim, int degree, bool lhs, const CellLaunch& P, const void* obj, size_t smem,
+                        cudaStream_t s);
+  // max resident blocks per SM for the kernel at this smem size
+  int (*occupancy)(int dim, int degree, bool lhs, size_t smem);
+};
+
+const ModelOps* find_model(const char* name);
+void register_model(const ModelOps* ops);
+
+// threads per block of the cell kernel for (dim, degree)
+int cell_threads(int dim, int degree);
+size_t cell_smem(int dim, int degree, int nrows_in, int nrows_out);
+// builds CellTables<dim,degree> bytes
+std::vector<unsigned char> build_cell_tables(int dim, int degree, const double* lo, const double* h,
+                                             const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
+                                             const signed char* slot_comp0, const signed char* out_of,
+                                             const signed char* out_row0);
+
+}  // namespace ppf

@@ -1,0 +1,241 @@
+"""Host-side mirror of the PRISMS-PF problem-description API over the C ABI.
+
+Names and meaning follow the reference: ``FieldAttributes`` (include/prismspf/core/field_attributes.h),
+``SolveBlock`` (include/prismspf/core/solve_block.h:56-127), ``make_dependency_set``
+(include/prismspf/core/dependencies.h:134-213, same dependency-string grammar: ``n``,
+``grad(n)``, ``hess(n)``, ``lap(n)``, ``hessdiag(n)``, ``div(u)``, ``symgrad(u)``, ``curl(u)``,
+``old_k(...)`` and ``src(...)/change(...)/trial(...)/lhs(...)``), and ``Problem``
+(include/prismspf/core/problem.h) whose ``solve`` runs the increment loop of
+src/core/problem.cc:341-557 on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field as dfield
+
+import numpy as np
+
+from . import capi
+
+# enums (include/prismspf/core/type_enums.h, solve_block.h)
+Scalar, Vector = 0, 1
+Constant, Explicit, Linear, Newton = 0, 1, 2, 3
+Primary = Initialized = 0
+Secondary = Uninitialized = 1
+PostProcess = 2
+NucleationRate = 3
+
+VALUES, GRADIENTS, HESSIANS = 1, 2, 4
+AGE_CURRENT, AGE_SRC = 0, 5
+
+
+@dataclass
+class FieldAttributes:
+    name: str
+    field_type: int = Scalar
+    # {(component, boundary_id): value} Dirichlet conditions (constraint_parameters.cc:41-107)
+    dirichlet: dict = dfield(default_factory=dict)
+
+
+@dataclass
+class Dependency:
+    flag: int = 0
+    src_flag: int = 0
+    old_flags: list = dfield(default_factory=list)
+
+
+def make_dependency_set(fields: list[FieldAttributes], dependency_strings, max_checked_age: int = 6) -> dict:
+    """Parses dependency strings into {field_index: Dependency}; unknown strings raise."""
+    reg = [("", "", VALUES), ("grad(", ")", GRADIENTS), ("hess(", ")", HESSIANS), ("hessdiag(", ")", HESSIANS),
+           ("lap(", ")", HESSIANS), ("div(", ")", GRADIENTS), ("symgrad(", ")", GRADIENTS), ("curl(", ")", GRADIENTS)]
+    srcs = [("src(", ")"), ("change(", ")"), ("trial(", ")"), ("lhs(", ")")]
+    remaining = set(dependency_strings)
+    result: dict[int, Dependency] = {}
+    for i, attr in enumerate(fields):
+        for pre, post, flag in reg:
+            s = pre + attr.name + post
+            if s in remaining:
+                result.setdefault(i, Dependency()).flag |= flag
+                remaining.discard(s)
+            for s1, s2 in srcs:
+                s = pre + s1 + attr.name + s2 + post
+                if s in remaining:
+                    result.setdefault(i, Dependency()).src_flag |= flag
+                    remaining.discard(s)
+            for age in range(max_checked_age):
+                s = f"{pre}old_{age + 1}({attr.name}){post}"
+                if s in remaining:
+                    d = result.setdefault(i, Dependency())
+                    while len(d.old_flags) < age + 1:
+                        d.old_flags.append(0)
+                    d.old_flags[age] |= flag
+                    remaining.discard(s)
+    if remaining:
+        raise ValueError("The following dependencies were not recognized: " + ", ".join(sorted(remaining)))
+    return result
+
+
+@dataclass
+class SolveBlock:
+    id: int = 0
+    solve_type: int = Explicit
+    solve_timing: int = Primary
+    field_indices: list = dfield(default_factory=list)
+    dependencies_rhs: dict = dfield(default_factory=dict)
+    dependencies_lhs: dict = dfield(default_factory=dict)
+
+
+@dataclass
+class RectangularMesh:
+    dim: int
+    degree: int
+    size: tuple
+    subdivisions: tuple = (1, 1, 1)
+    lower: tuple = (0.0, 0.0, 0.0)
+    global_refinement: int = 0
+    periodic: tuple = (0, 0, 0)
+
+    @property
+    def cells(self) -> list[int]:
+        return [self.subdivisions[d] << self.global_refinement for d in range(self.dim)]
+
+    @property
+    def nodes(self) -> list[int]:
+        return [self.degree * c + 1 for c in self.cells]
+
+
+def dep_table(deps: dict) -> np.ndarray:
+    """{field: Dependency} -> [field][age] flag table (ages current, old_1..old_4, src)."""
+    t = np.zeros((capi.PPF_MAX_FIELDS, capi.PPF_NAGE), dtype=np.uint8)
+    for f, d in deps.items():
+        t[f, AGE_CURRENT] |= d.flag
+        t[f, AGE_SRC] |= d.src_flag
+        for a, fl in enumerate(d.old_flags[:4]):
+            t[f, 1 + a] |= fl
+    return t
+
+
+class Problem:
+    """GPU problem handle: fields, solve blocks, mesh and a compiled operator set."""
+
+    def __init__(self, fields: list[FieldAttributes], blocks: list[SolveBlock], mesh: RectangularMesh,
+                 model: str, constants, dt: float):
+        self.lib = capi.load()
+        self.fields, self.blocks, self.mesh = fields, blocks, mesh
+        m = capi.MeshDesc()
+        m.dim, m.degree, m.global_refinement = mesh.dim, mesh.degree, mesh.global_refinement
+        for d in range(3):
+            m.subdivisions[d] = mesh.subdivisions[d] if d < mesh.dim else 1
+            m.lower[d] = mesh.lower[d] if d < mesh.dim else 0.0
+            m.size[d] = mesh.size[d] if d < mesh.dim else 1.0
+            m.periodic[d] = int(mesh.periodic[d]) if d < mesh.dim else 0
+        fds = (capi.FieldDesc * len(fields))()
+        for i, fa in enumerate(fields):
+            fds[i].rank = fa.field_type
+            for (comp, bid), val in fa.dirichlet.items():
+                fds[i].dirichlet[comp][bid] = 1
+                fds[i].dirichlet_value[comp][bid] = float(val)
+        bds = (capi.BlockDesc * max(1, len(blocks)))()
+        for i, b in enumerate(blocks):
+            bd = bds[i]
+            bd.id, bd.solve_type, bd.solve_timing = b.id, b.solve_type, b.solve_timing
+            bd.n_fields = len(b.field_indices)
+            for j, f in enumerate(b.field_indices):
+                bd.field_indices[j] = f
+            tr, tl = dep_table(b.dependencies_rhs), dep_table(b.dependencies_lhs)
+            for f in range(capi.PPF_MAX_FIELDS):
+                for a in range(capi.PPF_NAGE):
+                    bd.dep_rhs[f][a] = int(tr[f, a])
+                    bd.dep_lhs[f][a] = int(tl[f, a])
+        consts = np.ascontiguousarray(np.asarray(constants, dtype=np.float64))
+        h = C.c_void_p()
+        rc = self.lib.ppf_create(C.byref(m), fds, len(fields), bds, len(blocks), model.encode(), capi.dptr(consts),
+                                 len(consts), float(dt), C.byref(h))
+        if rc != capi.PPF_OK:
+            raise capi.PPFError(rc, self.lib.ppf_last_error(None).decode())
+        self.h = h
+
+    # --- lifetime -------------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ppf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != capi.PPF_OK:
+            raise capi.PPFError(rc, self.lib.ppf_last_error(self.h).decode())
+
+    # --- sizes ----------------------------------------------------------------------------
+    @property
+    def n_nodes(self) -> int:
+        return int(self.lib.ppf_n_nodes(self.h))
+
+    def field_length(self, f: int) -> int:
+        return int(self.lib.ppf_field_length(self.h, f))
+
+    # --- maps -----------------------------------------------------------------------------
+    def dof_map(self, rank: int) -> np.ndarray:
+        n = self.n_nodes * (1 if rank == 0 else self.mesh.dim)
+        out = np.empty(n, dtype=np.int64)
+        self._check(self.lib.ppf_dof_map(self.h, rank, out.ctypes.data_as(C.POINTER(C.c_longlong))))
+        return out
+
+    def constraint_map(self, f: int) -> np.ndarray:
+        out = np.empty(self.field_length(f), dtype=np.int32)
+        self._check(self.lib.ppf_constraint_map(self.h, f, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def invm(self) -> np.ndarray:
+        out = np.empty(self.n_nodes, dtype=np.float64)
+        self._check(self.lib.ppf_invm(self.h, capi.dptr(out)))
+        return out
+
+    # --- state ----------------------------------------------------------------------------
+    def upload(self, f: int, values: np.ndarray, age: int = 0, ordering: int = capi.ORDER_LATTICE):
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        if v.size != self.field_length(f):
+            raise ValueError("wrong vector length")
+        self._check(self.lib.ppf_upload_state(self.h, f, age, capi.dptr(v), ordering))
+
+    def download(self, f: int, age: int = 0, ordering: int = capi.ORDER_LATTICE) -> np.ndarray:
+        out = np.empty(self.field_length(f), dtype=np.float64)
+        self._check(self.lib.ppf_download_state(self.h, f, age, capi.dptr(out), ordering))
+        return out
+
+    def apply_constraints(self, f: int):
+        self._check(self.lib.ppf_apply_constraints(self.h, f))
+
+    # --- solves ---------------------------------------------------------------------------
+    def solve(self, n_increments: int, output_every: int = 0):
+        """Problem::solve: increments from the current one through n_increments."""
+        self._check(self.lib.ppf_run(self.h, n_increments, output_every))
+
+    def solve_block(self, b: int):
+        self._check(self.lib.ppf_solve_block(self.h, b))
+
+    def apply(self, b: int, which: int, src: np.ndarray | None, scale: int = 0) -> np.ndarray:
+        n = sum(self.field_length(f) for f in self.blocks[b].field_indices)
+        dst = np.empty(n, dtype=np.float64)
+        sp = None
+        if src is not None:
+            src = np.ascontiguousarray(src, dtype=np.float64)
+            sp = capi.dptr(src)
+        self._check(self.lib.ppf_apply(self.h, b, which, sp, capi.dptr(dst), scale))
+        return dst
+
+    def set_time(self, increment: int, time: float):
+        self._check(self.lib.ppf_set_time(self.h, increment, time))
+
+    def get_time(self) -> tuple[int, float]:
+        inc, t = C.c_uint(), C.c_double()
+        self._check(self.lib.ppf_get_time(self.h, C.byref(inc), C.byref(t)))
+        return inc.value, t.value
+
+    def synchronize(self):
+        self._check(self.lib.ppf_synchronize(self.h))
