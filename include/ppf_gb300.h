@@ -171,6 +171,26 @@ int ppf_kernel_stats_reset(ppf_handle h);
  * register-resident FMA loop; the denominator of FP64 roofline fractions. */
 int ppf_device_fp64_peak(double* tflops);
 
+/* One explicit Allen-Cahn step that allocates nothing. No counterpart in the reference: it
+ * exists for callers that cannot allocate GPU memory at the point where they need a step
+ * (for example code running inside a framework that owns every device allocation through
+ * its own pool, or a fixed-memory loop where cudaMalloc/cudaFree are not allowed).
+ *
+ * Computes d_n_new = invM (.) A_rhs(d_n_old) for block 1 of the Allen-Cahn application
+ * (constants m_well, kappa, time step dt) on `mesh` with natural boundary conditions, on the
+ * given stream (a cudaStream_t as void*, NULL = default stream); no handle is needed.
+ * d_n_old / d_n_new are caller-owned device vectors in lattice order.
+ *
+ * Limit: meshes of at most 1,048,576 lattice nodes (8 MiB accumulator); larger meshes, and
+ * periodic meshes, return PPF_ERR_UNSUPPORTED with a message on stderr. The scratch is one
+ * static device array that every GPU loading this library holds until exit. All calls share
+ * it: each call clears what must start at zero, and calls whose GPU work overlaps race, so
+ * issue them on one stream. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture. Non-finite
+ * results are not reported by this entry point. */
+int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_well, double kappa, double dt,
+                                const double* d_n_old, double* d_n_new, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,7 +34,7 @@ EXPORTED = [
     "ppf_apply_constraints", "ppf_run", "ppf_solve_block", "ppf_apply", "ppf_apply_device",
     "ppf_set_time", "ppf_get_time", "ppf_set_use_graph", "ppf_state_device_ptr", "ppf_synchronize",
     "ppf_set_stream", "ppf_kernel_timing", "ppf_kernel_stats", "ppf_kernel_stats_reset",
-    "ppf_device_fp64_peak",
+    "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc",
 ]
 
 
@@ -113,6 +113,8 @@ def load() -> C.CDLL:
     lib.ppf_kernel_stats.argtypes = [H, dp, P(C.c_longlong), P(C.c_longlong)]
     lib.ppf_kernel_stats_reset.argtypes = [H]
     lib.ppf_device_fp64_peak.argtypes = [dp]
+    lib.ppf_allen_cahn_step_noalloc.argtypes = [P(MeshDesc), C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
