@@ -38,6 +38,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "DoF-updates/s (explicit Cahn-Hilliard Q2 3-D step, FP64)"
 UNIT = "DoF-updates/s"
 WORKLOAD = dict(refine=6, degree=2, size=64.0, dt=1e-4)
+# dram__bytes_read.sum + dram__bytes_write.sum of the cell kernel from one ncu capture of
+# this workload, mean of the c-block (59.94 MB) and mu-block (42.73 MB) launches
+TRAFFIC_PER_LAUNCH = 51.34e6
 
 
 def workload_config(extra=None):
@@ -287,7 +290,8 @@ def run_ours(args):
                 "config": workload_config({"parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}),
                 "e2e": e2e, "gpu_launches": int(all_n.value), "clocks": clk.summary(),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                             "frac": achieved / peak, "traffic": TRAFFIC_PER_LAUNCH,
+                             "traffic_unit": "bytes/launch", "peak_source": peak_src,
                              "kernel": "cell_kernel<CahnHilliard<3,2>>", "bytes_per_launch": bytes_per_launch,
                              "avg_launch_ms": avg_launch_s * 1e3},
                 "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
