@@ -144,6 +144,39 @@ int ppf_apply_device(ppf_handle h, int b, int which, const double* d_src, double
 int ppf_set_time(ppf_handle h, unsigned int increment, double time);
 int ppf_get_time(ppf_handle h, unsigned int* increment, double* time);
 
+/* LinearSolverParameters (src/user_inputs/solve_parameters.cc:10-187, same defaults): CG
+ * preconditioned by nothing, Chebyshev (Jacobi-Chebyshev on the fine operator) or a GMG
+ * V-cycle with Chebyshev smoothing and the smoother as coarse solve
+ * (include/prismspf/solvers/linear_solver.h:47-213). The convergence test is
+ * ||invM^1/2 (b - A x)|| < tolerance * normalisation (linear_solver.h:414-427).
+ * mixed_precision = 1 runs the V-cycle's smoother, level operators and transfers in FP32
+ * under the FP64 CG (GMG only); the coarse level, residuals and inner products stay FP64. */
+typedef struct {
+  int tolerance_type;      /* 0 AbsoluteResidual, 1 RMSEPerField, 2 IntegratedPerField, 3 RMSETotal, 4 IntegratedTotal */
+  double tolerance;        /* default 1e-10 */
+  int max_iterations;      /* default 100 */
+  int preconditioner;      /* 0 None, 1 Chebyshev, 2 GMG */
+  int mg_depth;            /* levels of the GMG hierarchy, finest included (default 1) */
+  int smoother_degree;     /* Chebyshev polynomial degree (default 5) */
+  double smoothing_range;  /* lambda_max / lambda_min of the Chebyshev interval (default 15) */
+  int eig_cg_iterations;   /* CG steps of the largest-eigenvalue estimate (default 10) */
+  int mixed_precision;     /* see above (default 0) */
+} ppf_linear_params;
+
+int ppf_default_linear_params(ppf_linear_params* p);
+int ppf_set_linear_params(ppf_handle h, int block, const ppf_linear_params* p);
+
+/* LinearSolver::solve_impl (linear_solver.h:305-345) for Linear block b: rhs from
+ * compute_rhs, inhomogeneous Dirichlet values lifted with the plain-read LHS, CG from the
+ * previous homogeneous solution, then constraints. Returns PPF_ERR_NOCONV when max_iterations
+ * is reached (the solution is still written, as the reference logs and continues). */
+int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual);
+
+/* Matrix diagonal of the LHS of block b by unit probes, scaled by invM^1/2 when the
+ * tolerance type is not AbsoluteResidual, zero entries set to one
+ * (MFOperator::compute_diagonal, mf_operator.cc:82-101); lattice order, host output. */
+int ppf_lhs_diagonal(ppf_handle h, int b, double* out);
+
 /* Capture the explicit increment loop in a CUDA graph (on by default for ppf_run). */
 int ppf_set_use_graph(ppf_handle h, int on);
 

@@ -39,31 +39,32 @@ PPF_HD constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1)
 
 PPF_HD constexpr int age_of(DependencyType t) { return t == SRC ? 5 : (t >= Current ? int(t) : -1); }
 
-// Per-launch tables staged in shared memory by the cell kernel (sized for one dim/degree).
-template <int dim, int degree>
+// Per-launch tables staged in shared memory by the cell kernel (sized for one dim/degree,
+// stored in the arithmetic type of the kernel).
+template <int dim, int degree, typename number = double>
 struct CellTables {
   static constexpr int n = degree + 1;
   static constexpr int nq = ipow(n, dim);
-  double Dh[dim][n][n];   // D[q][j] / h_d: derivative of basis j at GL node q, direction d
-  double D2h[dim][n][n];  // (D D)[q][j] / h_d^2
-  double Dt[n][n];        // Dt[i][j] = D[j][i] (integration uses the transposed derivative)
-  double jxw[nq];         // JxW per quadrature point
-  double jxw_ih[dim][nq]; // JxW/h_d per quadrature point
-  double lo[3], h[3], gl_x[n];
-  double vol;
+  number Dh[dim][n][n];   // D[q][j] / h_d: derivative of basis j at GL node q, direction d
+  number D2h[dim][n][n];  // (D D)[q][j] / h_d^2
+  number Dt[n][n];        // Dt[i][j] = D[j][i] (integration uses the transposed derivative)
+  number jxw[nq];         // JxW per quadrature point
+  number jxw_ih[dim][nq]; // JxW/h_d per quadrature point
+  number lo[3], h[3], gl_x[n];
+  number vol;
   signed char slot_of[MAX_FIELDS][NAGE];  // dependency slot of (field, age), -1 if undeclared
   signed char slot_comp0[MAX_SLOTS];      // first value row of a slot
   signed char out_of[MAX_FIELDS];         // output index of a block field, -1 if not in block
   signed char out_row0[MAX_OUTS];         // first output row (per comp: value, then dim grads)
 };
 
-template <int dim, int degree>
+template <int dim, int degree, typename number = double>
 struct CellCtx {
   static constexpr int n = degree + 1;
   static constexpr int nq = ipow(n, dim);
-  const CellTables<dim, degree>* tab;
-  const double* vals;  // [row][stride]
-  double* outs;        // [row][stride]
+  const CellTables<dim, degree, number>* tab;
+  const number* vals;  // [row][stride]
+  number* outs;        // [row][stride]
   int stride;          // cells_per_block * nq
   int lc;              // cell within the thread block
   int q;               // quadrature point (= node) within the cell
@@ -91,7 +92,7 @@ class FieldContainer {
   static constexpr int n = degree + 1;
   static constexpr unsigned int dofs_per_component = gpu::ipow(n, dim);
 
-  using Ctx = gpu::CellCtx<dim, degree>;
+  using Ctx = gpu::CellCtx<dim, degree, number>;
 
   PPF_HD explicit FieldContainer(Ctx& c) : ctx(c) {}
 
@@ -345,8 +346,8 @@ class FieldContainer {
     int stride_d = 1;
     for (int e = 0; e < d; ++e) stride_d *= n;
     const int qd = (ctx.q / stride_d) % n;
-    const double* u = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
-    const double* Dr = ctx.tab->Dh[d][qd];
+    const number* u = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
+    const number* Dr = ctx.tab->Dh[d][qd];
     number s = Dr[0] * u[0];
 #pragma unroll
     for (int j = 1; j < n; ++j) s = fma(Dr[j], u[j * stride_d], s);
@@ -359,15 +360,15 @@ class FieldContainer {
     for (int k = 0; k < d; ++k) sd *= n;
     for (int k = 0; k < e; ++k) se *= n;
     const int qd = (ctx.q / sd) % n, qe = (ctx.q / se) % n;
-    const double* base = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component);
+    const number* base = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component);
     if (d == e) {
-      const double* u = base + (ctx.q - qd * sd);
-      const double* Dr = ctx.tab->D2h[d][qd];
+      const number* u = base + (ctx.q - qd * sd);
+      const number* Dr = ctx.tab->D2h[d][qd];
       number s = 0;
       for (int j = 0; j < n; ++j) s = fma(Dr[j], u[j * sd], s);
       return s;
     }
-    const double* u = base + (ctx.q - qd * sd - qe * se);
+    const number* u = base + (ctx.q - qd * sd - qe * se);
     number s = 0;
     for (int j = 0; j < n; ++j) {
       number t = 0;

@@ -54,6 +54,15 @@ template <typename N> PPF_HD VectorizedArray<N> operator/(N a, VectorizedArray<N
 // integer literals (e.g. `2 * a2 * c`) promote to Number
 template <typename N> PPF_HD VectorizedArray<N> operator*(int a, VectorizedArray<N> b) { return N(a) * b.v; }
 template <typename N> PPF_HD VectorizedArray<N> operator*(VectorizedArray<N> a, int b) { return a.v * N(b); }
+// double literals with single-precision lanes (as deal.II's VectorizedArray<float> accepts)
+PPF_HD VectorizedArray<float> operator+(VectorizedArray<float> a, double b) { return a.v + float(b); }
+PPF_HD VectorizedArray<float> operator+(double a, VectorizedArray<float> b) { return float(a) + b.v; }
+PPF_HD VectorizedArray<float> operator-(VectorizedArray<float> a, double b) { return a.v - float(b); }
+PPF_HD VectorizedArray<float> operator-(double a, VectorizedArray<float> b) { return float(a) - b.v; }
+PPF_HD VectorizedArray<float> operator*(VectorizedArray<float> a, double b) { return a.v * float(b); }
+PPF_HD VectorizedArray<float> operator*(double a, VectorizedArray<float> b) { return float(a) * b.v; }
+PPF_HD VectorizedArray<float> operator/(VectorizedArray<float> a, double b) { return a.v / float(b); }
+PPF_HD VectorizedArray<float> operator/(double a, VectorizedArray<float> b) { return float(a) / b.v; }
 
 template <typename Number>
 PPF_HD VectorizedArray<Number> make_vectorized_array(Number x) { return VectorizedArray<Number>(x); }

@@ -354,10 +354,42 @@ struct Field {
   int n_old = 0;
 };
 
+struct Problem;
+
+// LinearSolverParameters (src/user_inputs/solve_parameters.cc:10-187)
+struct LinParams {
+  int tol_type = 0;          // 0 AbsoluteResidual, 1 RMSEPerField, 2 IntegratedPerField, 3 RMSETotal, 4 IntegratedTotal
+  double tol = 1e-10;
+  int max_its = 100;
+  int precond = 0;           // 0 None, 1 Chebyshev, 2 GMG
+  int mg_depth = 1;
+  int degree = 5;
+  double range = 15.0;
+  int eig_its = 10;
+};
+
+struct OLevel {
+  Problem* P = nullptr;      // problem at this refinement (the finest level is the problem itself)
+  bool owned = false;
+  std::vector<double> inv_diag, x, b, r, u, Ax, t;
+  double lmax = 0, lmin = 0;
+  bool eig_done = false;
+  // prolongation to the next finer level as triplets (fine dof, coarse dof, weight)
+  std::vector<long> pf, pc;
+  std::vector<double> pw;
+};
+
 struct Block {
   int id = 0, solve_type = 1, timing = 0;
   std::vector<int> fields;
   std::vector<std::array<int, NAGE>> dep_rhs, dep_lhs;  // [field][age] flags
+  // linear solves
+  LinParams lin;
+  bool lin_init = false;
+  std::vector<double> x_hom;
+  std::vector<OLevel> levels;
+  int last_its = 0;
+  double last_res = 0.0;
 };
 
 struct Model;
@@ -374,6 +406,9 @@ struct Problem {
   std::vector<double> params;
   int nthreads = 0;
   std::string err;
+  int subdiv[3] = {1, 1, 1};
+  int refine = 0;
+  ~Problem();
 };
 
 // Per-q view handed to the model callbacks (restates FieldContainer getters/setters,
@@ -640,7 +675,7 @@ struct DepSlot { int field, age, flags; const double* vec; const Constraints* co
 // dst[field] vectors are indexed by block position
 static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<const double*>& src,
                       std::vector<double*>& dst, const std::vector<const Constraints*>& dst_cons,
-                      Callback cb) {
+                      Callback cb, bool plain_src = false) {
   Mesh& m = P.m;
   const int dim = m.dim, n = m.n, nloc = m.nloc;
   const auto& deps = lhs ? B.dep_lhs : B.dep_rhs;
@@ -659,7 +694,9 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
         for (size_t b = 0; b < B.fields.size(); ++b) if (B.fields[b] == f) pos = (int)b;
         if (pos < 0 || !src[pos]) continue;
         vec = src[pos];
-        cread = lhs;  // LHS reads src with homogeneous constraints (field_container.h:817-832)
+        // LHS reads src with homogeneous constraints (field_container.h:817-832) unless the
+        // operator is set to read plain (linear_solver.h:322-324)
+        cread = lhs && !plain_src;
       } else vec = F.old[age - 1].data();
       slots.push_back({f, age, fl, vec, &F.cons, cread, F.rank == 0 ? 1 : dim});
     }
@@ -795,6 +832,102 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
   }
 }
 
+// Operator diagonal by per-cell unit probes (MFOperator::compute_local_field_diagonal,
+// src/solvers/mf_operator.cc:147-218): for each cell and local node i, the src dof values are
+// the identity at node i (every component of a vector field, as identity<Rank>() submits),
+// the callback runs at every quadrature point, the integrated entry at node i is kept, and
+// the cell diagonal is distributed with the field's constraints. Single-field LHS blocks.
+static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
+  Mesh& m = P.m;
+  const int dim = m.dim, n = m.n, nloc = m.nloc;
+  const int f0 = B.fields[0];
+  Field& F0 = P.fields[f0];
+  const int ncomp = F0.rank == 0 ? 1 : dim;
+  const DofHandler& dh = m.dh[ncomp == 1 ? 0 : 1];
+  const int nf = (int)P.fields.size();
+  const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
+  const GL& gl = m.gl;
+  Callback cb = callback_for(P.model);
+  diag.assign(dh.ndofs, 0.0);
+  std::vector<double> qval((size_t)nf * NAGE * 3, 0.0), qgrad((size_t)nf * NAGE * 9, 0.0);
+  std::vector<double> ov((size_t)nloc * nf * 3), og((size_t)nloc * nf * 9);
+  std::vector<char> oflag(nf);
+  std::vector<double> grads((size_t)3 * 3 * nloc), vals((size_t)3 * nloc), cdiag((size_t)3 * nloc);
+  for (long c = 0; c < m.ncells; ++c) {
+    const auto& cc = m.cells[c];
+    for (int i = 0; i < nloc; ++i) {
+      // probe: identity at node i for every component
+      for (int comp = 0; comp < ncomp; ++comp)
+        for (int l = 0; l < nloc; ++l) vals[comp * nloc + l] = (l == i) ? 1.0 : 0.0;
+      for (int comp = 0; comp < ncomp; ++comp)
+        for (int l = 0; l < nloc; ++l) {
+          int a = l % n, b = (l / n) % n, e = l / (n * n);
+          int idx[3] = {a, b, e};
+          int stride[3] = {1, n, n * n};
+          for (int d = 0; d < dim; ++d) {
+            double acc = 0.0;
+            int base = l - idx[d] * stride[d];
+            for (int j = 0; j < n; ++j) acc += gl.D[idx[d]][j] * vals[comp * nloc + base + j * stride[d]];
+            grads[(comp * 3 + d) * nloc + l] = acc / m.h[d];
+          }
+        }
+      std::fill(ov.begin(), ov.end(), 0.0);
+      std::fill(og.begin(), og.end(), 0.0);
+      std::fill(oflag.begin(), oflag.end(), 0);
+      for (int l = 0; l < nloc; ++l) {
+        for (int comp = 0; comp < ncomp; ++comp) {
+          qval[(f0 * NAGE + AGE_SRC) * 3 + comp] = vals[comp * nloc + l];
+          for (int d = 0; d < dim; ++d)
+            qgrad[((f0 * NAGE + AGE_SRC) * 3 + comp) * 3 + d] = grads[(comp * 3 + d) * nloc + l];
+        }
+        QData q;
+        q.dim = dim; q.val = qval.data(); q.grad = qgrad.data();
+        q.out_val = &ov[(size_t)l * nf * 3]; q.out_grad = &og[(size_t)l * nf * 9];
+        q.out_flags = oflag.data(); q.nf = nf;
+        int a = l % n, b = (l / n) % n, e = l / (n * n);
+        q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * m.h[0];
+        q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * m.h[1];
+        q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * m.h[2] : 0.0;
+        q.vol = detJ;
+        cb(P, q, B.id, true);
+      }
+      // integrate and keep the entry at node i
+      int a = i % n, b = (i / n) % n, e = i / (n * n);
+      int idx[3] = {a, b, e};
+      int stride[3] = {1, n, n * n};
+      for (int comp = 0; comp < ncomp; ++comp) {
+        double r = 0.0;
+        double wq = gl.w[a] * gl.w[b] * (dim == 3 ? gl.w[e] : 1.0);
+        if (oflag[f0] & 1) r += ov[((size_t)i * nf + f0) * 3 + comp] * wq * detJ;
+        if (oflag[f0] & 2)
+          for (int d = 0; d < dim; ++d) {
+            int base = i - idx[d] * stride[d];
+            double acc = 0.0;
+            for (int qd = 0; qd < n; ++qd) {
+              int lq = base + qd * stride[d];
+              int aq = lq % n, bq = (lq / n) % n, eq = lq / (n * n);
+              double wqq = gl.w[aq] * gl.w[bq] * (dim == 3 ? gl.w[eq] : 1.0);
+              acc += og[(((size_t)lq * nf + f0) * 3 + comp) * 3 + d] * gl.D[qd][idx[d]] * wqq;
+            }
+            r += acc * detJ / m.h[d];
+          }
+        cdiag[comp * nloc + i] = r;
+      }
+    }
+    // distribute the cell diagonal with the field's constraints
+    for (int comp = 0; comp < ncomp; ++comp)
+      for (int l = 0; l < nloc; ++l) {
+        long g = dh.cell_dofs[((size_t)c * ncomp + comp) * nloc + l];
+        double r = cdiag[comp * nloc + l];
+        if (F0.cons.is_constrained(g)) {
+          for (auto& e2 : F0.cons.entries[g]) diag[e2.first] += e2.second * r;
+        } else {
+          diag[g] += r;
+        }
+      }
+  }
+}
+
 static void compute_invm(Problem& P) {
   Mesh& m = P.m;
   for (int which = 0; which < 2; ++which) {
@@ -857,6 +990,399 @@ static void explicit_solve(Problem& P, const Block& B) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Linear solves (LinearSolver + MGContext, include/prismspf/solvers/linear_solver.h:47-553)
+// for single-field Linear blocks.
+// ---------------------------------------------------------------------------------------
+Problem* make_problem(int dim, int degree, const int* subdiv, const double* lower, const double* size, int refine,
+                      const int* periodic);
+void finalize_fields(Problem& P);
+
+Problem::~Problem() {
+  for (auto& B : blocks)
+    for (auto& L : B.levels)
+      if (L.owned) delete L.P;
+}
+
+static bool scaled(const LinParams& p) { return p.tol_type != 0; }
+
+// dst = S A src (S = invM^1/2 unless AbsoluteResidual); constrained rows stay zero
+static void lhs_op(Problem& P, const Block& B, const double* src, double* dst, bool plain) {
+  Field& F = P.fields[B.fields[0]];
+  const size_t nd = F.cur.size();
+  std::fill(dst, dst + nd, 0.0);
+  std::vector<const double*> s{src};
+  std::vector<double*> d{dst};
+  std::vector<const Constraints*> c{&F.cons};
+  cell_loop(P, B, true, s, d, c, callback_for(P.model), plain);
+  if (scaled(B.lin))
+    for (size_t i = 0; i < nd; ++i) dst[i] *= P.invm_sqrt[F.rank][i];
+}
+
+static long lattice_index(const Problem& P, int rank, long dof) {
+  const auto& L = P.m.dh[rank].lattice[dof];
+  const long N = (long)P.m.nnode[0] * P.m.nnode[1] * P.m.nnode[2];
+  return (long)L[3] * N + ((long)L[2] * P.m.nnode[1] + L[1]) * P.m.nnode[0] + L[0];
+}
+
+static double dotp(const std::vector<double>& a, const std::vector<double>& b) {
+  double s = 0.0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+
+static void compute_inv_diag(Problem& P, const Block& B, std::vector<double>& inv) {
+  std::vector<double> d;
+  diag_loop(P, B, d);
+  Field& F = P.fields[B.fields[0]];
+  inv.resize(d.size());
+  for (size_t i = 0; i < d.size(); ++i) {
+    double v = scaled(B.lin) ? d[i] * P.invm_sqrt[F.rank][i] : d[i];
+    if (v == 0.0) v = 1.0;  // set_zero_entries_to_one
+    inv[i] = 1.0 / v;
+  }
+}
+
+static double tridiag_max(const std::vector<double>& a, const std::vector<double>& b) {
+  const int m = (int)a.size();
+  if (!m) return 1.0;
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < m; ++i) {
+    double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  auto below = [&](double x) {
+    int cnt = 0;
+    double q = a[0] - x;
+    if (q < 0) cnt++;
+    for (int i = 1; i < m; ++i) {
+      double qq = q == 0.0 ? 1e-300 : q;
+      q = a[i] - x - b[i - 1] * b[i - 1] / qq;
+      if (q < 0) cnt++;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (below(mid) >= m) hi = mid; else lo = mid;
+    if (hi - lo <= 1e-14 * std::max(1.0, std::fabs(hi))) break;
+  }
+  return hi;
+}
+
+// largest eigenvalue estimate of P A on a level: eig_its CG steps on A x = pattern, x0 = 0,
+// pattern (lattice index mod 11) minus its mean over the unconstrained rows
+static void estimate_eig(OLevel& L, const Block& B) {
+  Problem& P = *L.P;
+  Field& F = P.fields[B.fields[0]];
+  const size_t n = F.cur.size();
+  std::vector<double> b(n, 0.0), x(n, 0.0), r, z(n), p, q(n);
+  double mean = 0.0;
+  long nfree = 0;
+  for (size_t i = 0; i < n; ++i)
+    if (!F.cons.is_constrained(i)) { mean += double(lattice_index(P, F.rank, i) % 11); nfree++; }
+  mean /= std::max(1L, nfree);
+  for (size_t i = 0; i < n; ++i)
+    b[i] = F.cons.is_constrained(i) ? 0.0 : double(lattice_index(P, F.rank, i) % 11) - mean;
+  r = b;
+  for (size_t i = 0; i < n; ++i) z[i] = L.inv_diag[i] * r[i];
+  p = z;
+  double rz = dotp(r, z), r0 = dotp(r, r);
+  std::vector<double> al, be;
+  for (int it = 0; it < B.lin.eig_its; ++it) {
+    lhs_op(P, B, p.data(), q.data(), false);
+    double pq = dotp(p, q);
+    if (pq <= 0.0 || !std::isfinite(pq)) break;
+    double alpha = rz / pq;
+    for (size_t i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+    al.push_back(alpha);
+    if (std::sqrt(dotp(r, r)) < 1e-10 * std::sqrt(r0)) break;
+    for (size_t i = 0; i < n; ++i) z[i] = L.inv_diag[i] * r[i];
+    double rzn = dotp(r, z);
+    double beta = rzn / rz;
+    rz = rzn;
+    be.push_back(beta);
+    for (size_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+  }
+  const int m = (int)al.size();
+  std::vector<double> a(m), o(m > 0 ? m - 1 : 0);
+  for (int i = 0; i < m; ++i) {
+    a[i] = 1.0 / al[i] + (i > 0 ? be[i - 1] / al[i - 1] : 0.0);
+    if (i + 1 < m) o[i] = std::sqrt(std::max(0.0, be[i])) / al[i];
+  }
+  L.lmax = 1.2 * tridiag_max(a, o);
+  L.lmin = L.lmax / B.lin.range;
+  L.eig_done = true;
+}
+
+// Chebyshev smoother (first kind) on L.x with right-hand side L.b
+static void chebyshev(OLevel& L, const Block& B, bool zero_start) {
+  Problem& P = *L.P;
+  const size_t n = L.b.size();
+  const double theta = 0.5 * (L.lmax + L.lmin), delta = 0.5 * (L.lmax - L.lmin), sigma = theta / delta;
+  if (zero_start) std::fill(L.x.begin(), L.x.end(), 0.0);
+  std::fill(L.u.begin(), L.u.end(), 0.0);
+  double rho_prev = 1.0 / sigma;
+  for (int k = 0; k < B.lin.degree; ++k) {
+    bool have_ax = !(zero_start && k == 0);
+    if (have_ax) lhs_op(P, B, L.x.data(), L.Ax.data(), false);
+    double c1, c2;
+    if (k == 0) { c1 = 0.0; c2 = 1.0 / theta; }
+    else {
+      double rho = 1.0 / (2.0 * sigma - rho_prev);
+      c1 = rho * rho_prev;
+      c2 = 2.0 * rho / delta;
+      rho_prev = rho;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      double r = have_ax ? L.b[i] - L.Ax[i] : L.b[i];
+      L.u[i] = c1 * L.u[i] + c2 * L.inv_diag[i] * r;
+      L.x[i] += L.u[i];
+    }
+  }
+}
+
+// prolongation weights from level c to level c+1 (GL nodal interpolation, tensor product)
+static void build_prolongation(OLevel& cl, OLevel& fl, int f) {
+  Problem& C = *cl.P;
+  Problem& Fp = *fl.P;
+  const int rank = Fp.fields[f].rank;
+  const Mesh& mc = C.m;
+  const Mesh& mf = Fp.m;
+  const int dim = mf.dim, k = mf.k, n = mf.n;
+  auto n2d = node_to_dof(mc, rank);
+  const DofHandler& dhf = mf.dh[rank];
+  cl.pf.clear(); cl.pc.clear(); cl.pw.clear();
+  for (long i = 0; i < dhf.ndofs; ++i) {
+    const auto& Lf = dhf.lattice[i];
+    int cidx[3][8]; double cw[3][8]; int cnt[3] = {1, 1, 1};
+    cidx[1][0] = cidx[2][0] = 0; cw[1][0] = cw[2][0] = 1.0;
+    for (int d = 0; d < dim; ++d) {
+      const int I = Lf[d];
+      const int ncf = mf.nc[d];
+      const int cf = std::min(I / k, ncf - 1);
+      const double xf = mf.gl.x[I - k * cf];
+      const int cc = cf / 2;
+      const double xc = ((cf % 2) + xf) * 0.5;
+      cnt[d] = 0;
+      for (int j = 0; j < n; ++j) {
+        double Lj = 1.0;
+        for (int mm = 0; mm < n; ++mm) if (mm != j) Lj *= (xc - mf.gl.x[mm]) / (mf.gl.x[j] - mf.gl.x[mm]);
+        if (std::fabs(Lj) > 1e-14) { cidx[d][cnt[d]] = k * cc + j; cw[d][cnt[d]] = Lj; cnt[d]++; }
+      }
+    }
+    for (int a = 0; a < cnt[0]; ++a)
+      for (int b = 0; b < cnt[1]; ++b)
+        for (int c = 0; c < cnt[2]; ++c) {
+          long I = cidx[0][a], J = dim > 1 ? cidx[1][b] : 0, K = dim > 2 ? cidx[2][c] : 0;
+          long cd = lattice_dof(mc, rank, n2d, I, J, K, Lf[3]);
+          cl.pf.push_back(i);
+          cl.pc.push_back(cd);
+          cl.pw.push_back(cw[0][a] * (dim > 1 ? cw[1][b] : 1.0) * (dim > 2 ? cw[2][c] : 1.0));
+        }
+  }
+}
+
+// homogeneous distribute: images take their master's value, Dirichlet rows zero
+static void homogeneous_distribute(const Constraints& C, std::vector<double>& v) {
+  for (size_t i = 0; i < v.size(); ++i) {
+    if (!C.constrained[i]) continue;
+    double s = 0.0;
+    for (auto& e : C.entries[i]) s += e.second * v[e.first];
+    v[i] = s;
+  }
+}
+
+// condensation of a restricted vector: images add into masters, constrained rows zero
+static void condense(const Constraints& C, std::vector<double>& v) {
+  for (size_t i = 0; i < v.size(); ++i) {
+    if (!C.constrained[i]) continue;
+    for (auto& e : C.entries[i]) v[e.first] += e.second * v[i];
+  }
+  for (size_t i = 0; i < v.size(); ++i) if (C.constrained[i]) v[i] = 0.0;
+}
+
+static void vcycle(Block& Bfine, int l) {
+  OLevel& L = Bfine.levels[l];
+  Problem& P = *L.P;
+  const Block& LB = *std::find_if(P.blocks.begin(), P.blocks.end(), [&](const Block& x) { return x.id == Bfine.id; });
+  if (l == 0) { chebyshev(L, LB, true); return; }
+  chebyshev(L, LB, true);
+  lhs_op(P, LB, L.x.data(), L.r.data(), false);
+  for (size_t i = 0; i < L.r.size(); ++i) L.r[i] = L.b[i] - L.r[i];
+  OLevel& C = Bfine.levels[l - 1];
+  std::fill(C.b.begin(), C.b.end(), 0.0);
+  for (size_t q = 0; q < C.pf.size(); ++q) C.b[C.pc[q]] += C.pw[q] * L.r[C.pf[q]];
+  condense(C.P->fields[LB.fields[0]].cons, C.b);
+  vcycle(Bfine, l - 1);
+  std::fill(L.t.begin(), L.t.end(), 0.0);
+  for (size_t q = 0; q < C.pf.size(); ++q) L.t[C.pf[q]] += C.pw[q] * C.x[C.pc[q]];
+  homogeneous_distribute(P.fields[LB.fields[0]].cons, L.t);
+  for (size_t i = 0; i < L.x.size(); ++i) L.x[i] += L.t[i];
+  chebyshev(L, LB, false);
+}
+
+static void init_linear(Problem& P, Block& B) {
+  const int f = B.fields[0];
+  const int R = P.refine;
+  int depth = B.lin.precond == 2 ? std::max(1, B.lin.mg_depth) : 1;
+  depth = std::min(depth, R + 1);
+  B.levels.assign(depth, OLevel());
+  for (int l = 0; l < depth; ++l) {
+    OLevel& L = B.levels[l];
+    if (l == depth - 1) {
+      L.P = &P;
+    } else {
+      const int r = R - depth + 1 + l;
+      double lo[3], sz[3];
+      int per[3];
+      for (int d = 0; d < 3; ++d) { lo[d] = P.m.lo[d]; sz[d] = P.m.len[d]; per[d] = P.m.periodic[d]; }
+      Problem* C = make_problem(P.m.dim, P.m.k, P.subdiv, lo, sz, r, per);
+      for (auto& F : P.fields) {
+        Field G;
+        G.rank = F.rank;
+        std::memcpy(G.dir_on, F.dir_on, sizeof(G.dir_on));
+        for (int c = 0; c < 3; ++c) for (int b = 0; b < 6; ++b) G.dir_val[c][b] = 0.0;  // homogeneous
+        C->fields.push_back(G);
+      }
+      C->blocks = P.blocks;
+      for (auto& Bc : C->blocks) { Bc.levels.clear(); Bc.lin_init = false; }
+      C->model = P.model;
+      C->params = P.params;
+      C->dt = P.dt;
+      C->nthreads = P.nthreads;
+      finalize_fields(*C);
+      L.P = C;
+      L.owned = true;
+    }
+    const size_t n = L.P->fields[f].cur.size();
+    for (auto* v : {&L.x, &L.b, &L.r, &L.u, &L.Ax, &L.t}) v->assign(n, 0.0);
+  }
+  for (int l = 0; l + 1 < depth; ++l) build_prolongation(B.levels[l], B.levels[l + 1], f);
+  B.x_hom.assign(P.fields[f].cur.size(), 0.0);
+  B.lin_init = true;
+}
+
+static double normalization(const Problem& P, const LinParams& p) {
+  double v = 1.0;
+  if (p.tol_type == 1 || p.tol_type == 3) {
+    double vol = 1.0;
+    for (int d = 0; d < P.m.dim; ++d) vol *= P.m.len[d];
+    v *= std::sqrt(vol);
+  }
+  return v;  // one field: sqrt(n_fields) = 1
+}
+
+// LinearSolver::solve_impl (linear_solver.h:305-345)
+static int linear_solve(Problem& P, Block& B) {
+  if (!B.lin_init) init_linear(P, B);
+  const int f = B.fields[0];
+  Field& F = P.fields[f];
+  const size_t n = F.cur.size();
+  // level diagonals (recomputed every solve) and eigenvalue estimates (first use)
+  if (B.lin.precond != 0)
+    for (auto& L : B.levels) {
+      const Block& LB = *std::find_if(L.P->blocks.begin(), L.P->blocks.end(), [&](const Block& x) { return x.id == B.id; });
+      compute_inv_diag(*L.P, LB, L.inv_diag);
+      if (!L.eig_done) {
+        Block tmp = LB;
+        tmp.lin = B.lin;
+        estimate_eig(L, tmp);
+      }
+    }
+  // rhs = S compute_rhs
+  std::vector<double> rhs(n, 0.0), g(n, 0.0), Ag(n), r(n), z(n), p(n), q(n);
+  {
+    std::vector<const double*> s{nullptr};
+    std::vector<double*> d{rhs.data()};
+    std::vector<const Constraints*> c{&F.cons};
+    cell_loop(P, B, false, s, d, c, callback_for(P.model));
+    if (scaled(B.lin)) for (size_t i = 0; i < n; ++i) rhs[i] *= P.invm_sqrt[F.rank][i];
+  }
+  distribute(F.cons, g.data());  // inhomogeneous values
+  lhs_op(P, B, g.data(), Ag.data(), true);
+  for (size_t i = 0; i < n; ++i) rhs[i] -= Ag[i];
+  // CG (deal.II SolverCG) from the previous homogeneous solution
+  std::vector<double>& x = B.x_hom;
+  const double tol = B.lin.tol * normalization(P, B.lin);
+  auto precond = [&](const std::vector<double>& rr, std::vector<double>& zz) {
+    if (B.lin.precond == 0) { zz = rr; return; }
+    OLevel& Lf = B.levels.back();
+    Lf.b = rr;
+    if (B.lin.precond == 1) chebyshev(Lf, B, true);
+    else vcycle(B, (int)B.levels.size() - 1);
+    zz = Lf.x;
+  };
+  lhs_op(P, B, x.data(), q.data(), false);
+  for (size_t i = 0; i < n; ++i) r[i] = rhs[i] - q[i];
+  double res = std::sqrt(dotp(r, r));
+  int it = 0;
+  bool conv = res < tol;
+  if (!conv) {
+    precond(r, z);
+    p = z;
+    double rz = dotp(r, z);
+    while (it < B.lin.max_its) {
+      lhs_op(P, B, p.data(), q.data(), false);
+      double alpha = rz / dotp(p, q);
+      for (size_t i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+      ++it;
+      res = std::sqrt(dotp(r, r));
+      if (res < tol) { conv = true; break; }
+      precond(r, z);
+      double rzn = dotp(r, z);
+      double beta = rzn / rz;
+      rz = rzn;
+      for (size_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    }
+  }
+  B.last_its = it;
+  B.last_res = res / normalization(P, B.lin);
+  for (size_t i = 0; i < n; ++i) F.cur[i] = x[i] + g[i];
+  distribute(F.cons, F.cur.data());
+  return conv ? 0 : 4;
+}
+
+Problem* make_problem(int dim, int degree, const int* subdiv, const double* lower, const double* size, int refine,
+                      const int* periodic) {
+  auto* P = new Problem();
+  Mesh& m = P->m;
+  m.dim = dim; m.k = degree; m.n = degree + 1;
+  m.nloc = 1; for (int d = 0; d < dim; ++d) m.nloc *= m.n;
+  int sd[3] = {1, 1, 1};
+  for (int d = 0; d < dim; ++d) { sd[d] = subdiv[d]; m.lo[d] = lower[d]; m.len[d] = size[d]; m.periodic[d] = periodic[d]; }
+  for (int d = 0; d < 3; ++d) P->subdiv[d] = sd[d];
+  P->refine = refine;
+  build_cells(m, sd, refine);
+  for (int d = 0; d < 3; ++d) {
+    m.h[d] = d < dim ? m.len[d] / m.nc[d] : 1.0;
+    m.nnode[d] = d < dim ? m.k * m.nc[d] + 1 : 1;
+  }
+  m.gl = make_gl(m.n);
+  distribute_dofs(m, 0);
+  distribute_dofs(m, 1);
+  compute_invm(*P);
+  return P;
+}
+
+// state vectors and constraints of every field; the number of old ages a field keeps is
+// the oldest age any block depends on
+void finalize_fields(Problem& P) {
+  for (size_t f = 0; f < P.fields.size(); ++f) {
+    Field& F = P.fields[f];
+    const long nd = P.m.dh[F.rank].ndofs;
+    int n_old = 0;
+    for (auto& B : P.blocks)
+      for (int a = AGE_OLD1; a <= AGE_OLD4; ++a)
+        if (B.dep_rhs[f][a] || B.dep_lhs[f][a]) n_old = std::max(n_old, a);
+    F.n_old = n_old;
+    F.cur.assign(nd, 0.0);
+    for (int a = 0; a < 4; ++a) F.old[a].assign(a < n_old ? nd : 0, 0.0);
+    make_field_constraints(P, (int)f);
+  }
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -869,22 +1395,7 @@ extern "C" {
 void* orc_create(int dim, int degree, const int* subdiv, const double* lower, const double* size,
                  int refine, const int* periodic) {
   if (dim < 1 || dim > 3 || degree < 1 || degree > 6) return nullptr;
-  auto* P = new Problem();
-  Mesh& m = P->m;
-  m.dim = dim; m.k = degree; m.n = degree + 1;
-  m.nloc = 1; for (int d = 0; d < dim; ++d) m.nloc *= m.n;
-  int sd[3] = {1, 1, 1};
-  for (int d = 0; d < dim; ++d) { sd[d] = subdiv[d]; m.lo[d] = lower[d]; m.len[d] = size[d]; m.periodic[d] = periodic[d]; }
-  build_cells(m, sd, refine);
-  for (int d = 0; d < 3; ++d) {
-    m.h[d] = d < dim ? m.len[d] / m.nc[d] : 1.0;
-    m.nnode[d] = d < dim ? m.k * m.nc[d] + 1 : 1;
-  }
-  m.gl = make_gl(m.n);
-  distribute_dofs(m, 0);
-  distribute_dofs(m, 1);
-  compute_invm(*P);
-  return P;
+  return make_problem(dim, degree, subdiv, lower, size, refine, periodic);
 }
 
 void orc_destroy(void* h) { delete (Problem*)h; }
@@ -955,19 +1466,7 @@ int orc_finalize(void* h, int model, const double* params, int nparams, double d
   P->params.assign(params, params + nparams);
   P->dt = dt;
   if (!callback_for(model)) return -1;
-  // number of old ages needed per field = max old age referenced by any block
-  for (size_t f = 0; f < P->fields.size(); ++f) {
-    Field& F = P->fields[f];
-    const long nd = P->m.dh[F.rank].ndofs;
-    int n_old = 0;
-    for (auto& B : P->blocks)
-      for (int a = AGE_OLD1; a <= AGE_OLD4; ++a)
-        if (B.dep_rhs[f][a] || B.dep_lhs[f][a]) n_old = std::max(n_old, a);
-    F.n_old = n_old;
-    F.cur.assign(nd, 0.0);
-    for (int a = 0; a < 4; ++a) F.old[a].assign(a < n_old ? nd : 0, 0.0);
-    make_field_constraints(*P, (int)f);
-  }
+  finalize_fields(*P);
   return 0;
 }
 
@@ -1026,7 +1525,8 @@ int orc_run(void* h, unsigned n_increments, int output_every) {
         // SolverBase::set_initial_condition (solver_base.h:178-229) no constraints are
         // distributed on it at increment 0
       } else {
-        explicit_solve(*P, B);
+        if (B.solve_type == 2) linear_solve(*P, B);
+        else explicit_solve(*P, B);
       }
       if (P->increment == 0) {
         for (int f : B.fields) {
@@ -1079,6 +1579,32 @@ int orc_apply(void* h, int b, int which, const double* src, double* dst, int sca
     off += nd;
   }
   return 0;
+}
+
+// Linear solver parameters of block b: p = {tol_type, tol, max_its, precond, mg_depth,
+// degree, smoothing range, eig_its}
+int orc_set_linear_params(void* h, int b, const double* p) {
+  auto* P = (Problem*)h;
+  LinParams& L = P->blocks[b].lin;
+  L.tol_type = (int)p[0]; L.tol = p[1]; L.max_its = (int)p[2]; L.precond = (int)p[3];
+  L.mg_depth = (int)p[4]; L.degree = (int)p[5]; L.range = p[6]; L.eig_its = (int)p[7];
+  return 0;
+}
+
+int orc_linear_solve(void* h, int b, int* its, double* res) {
+  auto* P = (Problem*)h;
+  int rc = linear_solve(*P, P->blocks[b]);
+  if (its) *its = P->blocks[b].last_its;
+  if (res) *res = P->blocks[b].last_res;
+  return rc;
+}
+
+// matrix diagonal of block b's LHS (scaled, zero entries one), deal.II order
+void orc_diagonal(void* h, int b, double* out) {
+  auto* P = (Problem*)h;
+  std::vector<double> inv;
+  compute_inv_diag(*P, P->blocks[b], inv);
+  for (size_t i = 0; i < inv.size(); ++i) out[i] = 1.0 / inv[i];
 }
 
 }  // extern "C"

@@ -70,6 +70,9 @@ def load() -> C.CDLL:
         lib.orc_explicit_block.argtypes = [C.c_void_p, C.c_int]
         lib.orc_run.argtypes = [C.c_void_p, C.c_uint, C.c_int]
         lib.orc_apply.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp, C.c_int]
+        lib.orc_set_linear_params.argtypes = [C.c_void_p, C.c_int, dp]
+        lib.orc_linear_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), dp]
+        lib.orc_diagonal.argtypes = [C.c_void_p, C.c_int, dp]
         _lib = lib
     return _lib
 
@@ -202,6 +205,26 @@ class Oracle:
 
     def run(self, n_increments: int, output_every: int = 0) -> int:
         return int(self.lib.orc_run(self.h, n_increments, output_every))
+
+    def set_linear_params(self, b: int, tolerance_type=0, tolerance=1e-10, max_iterations=100, preconditioner=0,
+                          mg_depth=1, smoother_degree=5, smoothing_range=15.0, eig_cg_iterations=10, **_):
+        p = np.array([tolerance_type, tolerance, max_iterations, preconditioner, mg_depth, smoother_degree,
+                      smoothing_range, eig_cg_iterations], dtype=np.float64)
+        self.lib.orc_set_linear_params(self.h, b, _dp(p))
+
+    def linear_solve(self, b: int):
+        its, res = C.c_int(), C.c_double()
+        rc = self.lib.orc_linear_solve(self.h, b, C.byref(its), C.byref(res))
+        return rc, its.value, res.value
+
+    def diagonal(self, b: int) -> np.ndarray:
+        f = self.wl.blocks[b].field_indices[0]
+        p = self.dealii_to_lattice(self._rank(f))
+        d = np.zeros(p.size)
+        self.lib.orc_diagonal(self.h, b, _dp(d))
+        out = np.zeros(p.size)
+        out[p] = d
+        return out
 
     def apply(self, b: int, which: int, src: np.ndarray | None, scale: int = 0) -> np.ndarray:
         blk = self.wl.blocks[b]

@@ -35,6 +35,7 @@ EXPORTED = [
     "ppf_set_time", "ppf_get_time", "ppf_set_use_graph", "ppf_state_device_ptr", "ppf_synchronize",
     "ppf_set_stream", "ppf_kernel_timing", "ppf_kernel_stats", "ppf_kernel_stats_reset",
     "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc",
+    "ppf_default_linear_params", "ppf_set_linear_params", "ppf_linear_solve", "ppf_lhs_diagonal",
 ]
 
 
@@ -58,6 +59,14 @@ class BlockDesc(C.Structure):
         ("field_indices", C.c_int * PPF_MAX_FIELDS),
         ("dep_rhs", (C.c_ubyte * PPF_NAGE) * PPF_MAX_FIELDS),
         ("dep_lhs", (C.c_ubyte * PPF_NAGE) * PPF_MAX_FIELDS),
+    ]
+
+
+class LinearParams(C.Structure):
+    _fields_ = [
+        ("tolerance_type", C.c_int), ("tolerance", C.c_double), ("max_iterations", C.c_int),
+        ("preconditioner", C.c_int), ("mg_depth", C.c_int), ("smoother_degree", C.c_int),
+        ("smoothing_range", C.c_double), ("eig_cg_iterations", C.c_int), ("mixed_precision", C.c_int),
     ]
 
 
@@ -115,6 +124,10 @@ def load() -> C.CDLL:
     lib.ppf_device_fp64_peak.argtypes = [dp]
     lib.ppf_allen_cahn_step_noalloc.argtypes = [P(MeshDesc), C.c_double, C.c_double, C.c_double, C.c_void_p,
                                                 C.c_void_p, C.c_void_p]
+    lib.ppf_default_linear_params.argtypes = [P(LinearParams)]
+    lib.ppf_set_linear_params.argtypes = [H, C.c_int, P(LinearParams)]
+    lib.ppf_linear_solve.argtypes = [H, C.c_int, P(C.c_int), dp]
+    lib.ppf_lhs_diagonal.argtypes = [H, C.c_int, dp]
     _lib = lib
     return lib
 

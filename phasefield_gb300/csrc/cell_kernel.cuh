@@ -4,7 +4,8 @@
 // Restates the per-cell work of MFOperator::compute_local_operator
 // (src/solvers/mf_operator.cc:34-80) with FieldContainer::reinit_and_eval /
 // integrate_and_distribute (include/prismspf/core/field_container.h:794-882) as one GPU
-// kernel:
+// kernel, plus the diagonal probe of MFOperator::compute_local_field_diagonal
+// (src/solvers/mf_operator.cc:147-218):
 //   * DoF vectors are stored in lattice order (x fastest) with periodic images kept, so the
 //     nodes of cell (cx,cy,cz) are a dense (k+1)^dim box of the lattice: the gather needs no
 //     index map. Constraint maps are int32 arrays over the same index space:
@@ -16,9 +17,13 @@
 //     gradients are 1-D contractions (FieldContainer::deriv);
 //   * integration is the transposed contraction over the pre-weighted submitted terms;
 //   * distribute_local_to_global: rows constrained to a master add into the master,
-//     Dirichlet rows are dropped; contributions of neighbouring cells meet through FP64
-//     atomicAdd into a zeroed accumulator (the finalize kernel applies invM and the
-//     constraints).
+//     Dirichlet rows are dropped; contributions of neighbouring cells meet through
+//     atomicAdd into a zeroed accumulator (the finalize kernels apply invM and constraints).
+//   * MODE_DIAG replaces the SRC dependency of each block field by unit probes on one cell
+//     node at a time (identity in every component, as the reference submits
+//     identity<Rank>()) and keeps the integrated entry at the probed node.
+// `number` is the arithmetic type (double for the drop-in, float for mixed-precision
+// multigrid smoothing).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -31,15 +36,19 @@ using prismspf::FieldContainer;
 using prismspf::SimulationTimer;
 namespace pg = prismspf::gpu;
 
+enum CellMode { MODE_RHS = 0, MODE_LHS = 1, MODE_DIAG = 2 };
+
 struct SlotDesc {
-  const double* ptr;  // component-major vector (ncomp * N)
+  const void* ptr;    // component-major vector (ncomp * N) of the kernel's number type
   const int* cmap;    // constraint map, used when constrained_read
   int ncomp;
   int constrained_read;  // homogeneous constrained read (FEEvaluation::read_dof_values)
+  int is_src;            // the SRC dependency of a block field (probed in MODE_DIAG)
+  int out_index;         // block output the SRC slot belongs to (MODE_DIAG)
 };
 
 struct OutDesc {
-  double* acc;       // accumulator (ncomp * N), zeroed before the launch
+  void* acc;         // accumulator (ncomp * N), zeroed before the launch
   const int* cmap;   // destination constraint map (condensation)
   int ncomp;
 };
@@ -55,7 +64,7 @@ struct CellLaunch {
   OutDesc outs[pg::MAX_OUTS];
   int nrows_in;      // sum of slot components
   int nrows_out;     // sum over outputs of ncomp * (1 + dim)
-  const void* tables;  // device copy of CellTables<dim,degree>
+  const void* tables;  // device copy of CellTables<dim,degree,number>
   SimulationTimer timer;
   unsigned int block_id;
   int* err;
@@ -69,23 +78,44 @@ struct CellShape {
   static constexpr int threads = cpb * nq;
 };
 
-template <int dim, int degree>
+template <int dim, int degree, typename number>
 __host__ __device__ inline size_t cell_smem_bytes(int nrows_in, int nrows_out) {
   using S = CellShape<dim, degree>;
-  size_t tab = (sizeof(pg::CellTables<dim, degree>) + 15) / 16 * 16;
-  return tab + sizeof(double) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
+  size_t tab = (sizeof(pg::CellTables<dim, degree, number>) + 15) / 16 * 16;
+  return tab + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
 }
 
-template <class PDE, int dim, int degree, bool LHS>
+template <int dim, int degree, typename number>
+__device__ __forceinline__ number integrate_row(const pg::CellTables<dim, degree, number>* tab, const number* outs,
+                                                int rv, bool has_v, bool has_g, int t, int lc, int q, int qa, int qb,
+                                                int qc) {
+  using S = CellShape<dim, degree>;
+  constexpr int n = S::n, nq = S::nq;
+  number r = has_v ? outs[rv * S::threads + t] : number(0);
+  if (has_g) {
+#pragma unroll
+    for (int d = 0; d < dim; ++d) {
+      const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+      const int id = d == 0 ? qa : (d == 1 ? qb : qc);
+      const number* g = outs + (rv + 1 + d) * S::threads + lc * nq + (q - id * sd);
+      const number* Dt = tab->Dt[id];
+#pragma unroll
+      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j * sd], r);
+    }
+  }
+  return r;
+}
+
+template <class PDE, int dim, int degree, int MODE, typename number>
 __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
     cell_kernel(const CellLaunch P, const PDE pde) {
   using S = CellShape<dim, degree>;
-  using Tab = pg::CellTables<dim, degree>;
+  using Tab = pg::CellTables<dim, degree, number>;
   constexpr int n = S::n, nq = S::nq, cpb = S::cpb, k = degree;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Tab* tab = reinterpret_cast<Tab*>(smem_raw);
-  double* vals = reinterpret_cast<double*>(smem_raw + (sizeof(Tab) + 15) / 16 * 16);
-  double* outs = vals + P.nrows_in * S::threads;
+  number* vals = reinterpret_cast<number*>(smem_raw + (sizeof(Tab) + 15) / 16 * 16);
+  number* outs = vals + P.nrows_in * S::threads;
   __shared__ int sflags;
 
   // stage the tables once per resident block
@@ -115,86 +145,142 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
       if (dim > 2) cz = (int)(cell / ((long long)P.nc[0] * P.nc[1]));
       node = ((long long)(k * cz + qc) * P.nn[1] + (k * cy + qb)) * P.nn[0] + (k * cx + qa);
     }
-    __syncthreads();  // tables staged; previous tile's integrate finished with vals/outs/sflags
-    if (t == 0) sflags = 0;
+    __syncthreads();  // tables staged; previous tile finished with vals/outs/sflags
 
-    // gather (read_dof_values_plain, or read_dof_values for constrained src)
+    // gather (read_dof_values_plain, or read_dof_values for constrained src); in MODE_DIAG
+    // the SRC rows are written by the probe loop below
     {
       int row = 0;
 #pragma unroll
       for (int s = 0; s < pg::MAX_SLOTS; ++s) {
         if (s < P.nslots) {
           const SlotDesc& sd = P.slots[s];
-          for (int c = 0; c < sd.ncomp; ++c) {
-            double v = 0.0;
-            if (active) {
-              const long long idx = node + c * P.N;
-              if (sd.constrained_read) {
-                const int m = sd.cmap[idx];
-                v = m >= 0 ? __ldg(sd.ptr + m) : 0.0;
-              } else {
-                v = __ldg(sd.ptr + idx);
+          if (!(MODE == MODE_DIAG && sd.is_src)) {
+            const number* ptr = static_cast<const number*>(sd.ptr);
+            for (int c = 0; c < sd.ncomp; ++c) {
+              number v = number(0);
+              if (active) {
+                const long long idx = node + c * P.N;
+                if (sd.constrained_read) {
+                  const int m = sd.cmap[idx];
+                  v = m >= 0 ? __ldg(ptr + m) : number(0);
+                } else {
+                  v = __ldg(ptr + idx);
+                }
               }
+              vals[(row + c) * S::threads + t] = v;
             }
-            vals[(row + c) * S::threads + t] = v;
           }
           row += sd.ncomp;
         }
       }
-      for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = 0.0;
     }
-    __syncthreads();
 
-    // user callback at this quadrature point
-    pg::CellCtx<dim, degree> ctx;
-    ctx.tab = tab;
-    ctx.vals = vals;
-    ctx.outs = outs;
-    ctx.stride = S::threads;
-    ctx.lc = lc;
-    ctx.q = q;
-    ctx.cell[0] = cx;
-    ctx.cell[1] = cy;
-    ctx.cell[2] = cz;
-    ctx.err = P.err;
-    ctx.submitted = 0;
-    if (active) {
-      FieldContainer<dim, degree, double> fc(ctx);
-      if constexpr (LHS) pde.compute_lhs(fc, P.timer, P.block_id);
-      else pde.compute_rhs(fc, P.timer, P.block_id);
-      if (ctx.submitted) atomicOr(&sflags, ctx.submitted);
-    }
-    __syncthreads();
-    const int flags = sflags;
+    if constexpr (MODE != MODE_DIAG) {
+      if (t == 0) sflags = 0;
+      for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = number(0);
+      __syncthreads();
 
-    // integrate + condensed scatter
-    if (active) {
+      pg::CellCtx<dim, degree, number> ctx;
+      ctx.tab = tab;
+      ctx.vals = vals;
+      ctx.outs = outs;
+      ctx.stride = S::threads;
+      ctx.lc = lc;
+      ctx.q = q;
+      ctx.cell[0] = cx;
+      ctx.cell[1] = cy;
+      ctx.cell[2] = cz;
+      ctx.err = P.err;
+      ctx.submitted = 0;
+      if (active) {
+        FieldContainer<dim, degree, number> fc(ctx);
+        if constexpr (MODE == MODE_LHS) pde.compute_lhs(fc, P.timer, P.block_id);
+        else pde.compute_rhs(fc, P.timer, P.block_id);
+        if (ctx.submitted) atomicOr(&sflags, ctx.submitted);
+      }
+      __syncthreads();
+      const int flags = sflags;
+
+      if (active) {
 #pragma unroll
-      for (int o = 0; o < pg::MAX_OUTS; ++o) {
-        if (o < P.nout) {
-          const OutDesc& od = P.outs[o];
-          const bool has_v = flags & (1 << (2 * o));
-          const bool has_g = flags & (2 << (2 * o));
-          const int row0 = tab->out_row0[o];
-          for (int c = 0; c < od.ncomp; ++c) {
-            const int rv = row0 + c * (1 + dim);
-            double r = has_v ? outs[rv * S::threads + t] : 0.0;
-            if (has_g) {
-#pragma unroll
-              for (int d = 0; d < dim; ++d) {
-                const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
-                const int id = d == 0 ? qa : (d == 1 ? qb : qc);
-                const double* g = outs + (rv + 1 + d) * S::threads + lc * nq + (q - id * sd);
-                const double* Dt = tab->Dt[id];
-#pragma unroll
-                for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j * sd], r);
+        for (int o = 0; o < pg::MAX_OUTS; ++o) {
+          if (o < P.nout) {
+            const OutDesc& od = P.outs[o];
+            const bool has_v = flags & (1 << (2 * o));
+            const bool has_g = flags & (2 << (2 * o));
+            const int row0 = tab->out_row0[o];
+            for (int c = 0; c < od.ncomp; ++c) {
+              const number r = integrate_row<dim, degree, number>(tab, outs, row0 + c * (1 + dim), has_v, has_g, t,
+                                                                  lc, q, qa, qb, qc);
+              if (has_v || has_g) {
+                const long long idx = node + c * P.N;
+                const int target = od.cmap ? od.cmap[idx] : (int)idx;
+                if (target >= 0) atomicAdd(static_cast<number*>(od.acc) + target, r);
               }
             }
-            if (has_v || has_g) {
-              const long long idx = node + c * P.N;
-              const int target = od.cmap ? od.cmap[idx] : (int)idx;
-              if (target >= 0) atomicAdd(od.acc + target, r);
-            }
+          }
+        }
+      }
+    } else {
+      // diagonal by unit probes: for each SRC slot (one per block field) and each cell node i
+#pragma unroll 1
+      for (int s = 0; s < P.nslots; ++s) {
+        const SlotDesc& sd = P.slots[s];
+        if (!sd.is_src) continue;
+        int row = 0;
+        for (int s2 = 0; s2 < s; ++s2) row += P.slots[s2].ncomp;
+        const int o = sd.out_index;
+        const OutDesc& od = P.outs[o];
+        const int row0 = tab->out_row0[o];
+        number mine[3] = {number(0), number(0), number(0)};
+#pragma unroll 1
+        for (int i = 0; i < nq; ++i) {
+          // submit zero to every SRC slot, identity at node i of this one
+          int rr = 0;
+          for (int s2 = 0; s2 < P.nslots; ++s2) {
+            if (P.slots[s2].is_src)
+              for (int c = 0; c < P.slots[s2].ncomp; ++c)
+                vals[(rr + c) * S::threads + t] = (s2 == s && q == i) ? number(1) : number(0);
+            rr += P.slots[s2].ncomp;
+          }
+          if (t == 0) sflags = 0;
+          for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = number(0);
+          __syncthreads();
+          pg::CellCtx<dim, degree, number> ctx;
+          ctx.tab = tab;
+          ctx.vals = vals;
+          ctx.outs = outs;
+          ctx.stride = S::threads;
+          ctx.lc = lc;
+          ctx.q = q;
+          ctx.cell[0] = cx;
+          ctx.cell[1] = cy;
+          ctx.cell[2] = cz;
+          ctx.err = P.err;
+          ctx.submitted = 0;
+          if (active) {
+            FieldContainer<dim, degree, number> fc(ctx);
+            pde.compute_lhs(fc, P.timer, P.block_id);
+            if (ctx.submitted) atomicOr(&sflags, ctx.submitted);
+          }
+          __syncthreads();
+          const int flags = sflags;
+          if (active && q == i) {
+            const bool has_v = flags & (1 << (2 * o));
+            const bool has_g = flags & (2 << (2 * o));
+            for (int c = 0; c < sd.ncomp; ++c)
+              mine[c] = integrate_row<dim, degree, number>(tab, outs, row0 + c * (1 + dim), has_v, has_g, t, lc, q,
+                                                           qa, qb, qc);
+          }
+          __syncthreads();
+          (void)row;
+        }
+        if (active) {
+          for (int c = 0; c < sd.ncomp; ++c) {
+            const long long idx = node + c * P.N;
+            const int target = od.cmap ? od.cmap[idx] : (int)idx;
+            if (target >= 0) atomicAdd(static_cast<number*>(od.acc) + target, mine[c]);
           }
         }
       }

@@ -1,0 +1,164 @@
+// Internal definition of the engine handle shared by the runtime translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ppf_gb300.h"
+#include "runtime.h"
+
+namespace ppf {
+
+struct GLRule {
+  int n;
+  double x[pg::MAX_N], w[pg::MAX_N], D[pg::MAX_N][pg::MAX_N];
+};
+GLRule gauss_lobatto(int n);
+
+struct FieldState {
+  int rank = 0, ncomp = 1;
+  long long len = 0;
+  int n_old = 0;
+  double* cur = nullptr;
+  double* old[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* acc = nullptr;
+  int* cmap = nullptr;
+  double* dvals = nullptr;
+  std::vector<int> h_cmap;
+  std::vector<double> h_dvals;
+  bool constrained = false;
+  ppf_field_desc desc;
+};
+
+struct BlockPlan {
+  int nslots = 0;
+  int slot_field[pg::MAX_SLOTS];
+  int slot_age[pg::MAX_SLOTS];
+  int nrows_in = 0, nrows_out = 0;
+  void* d_tables = nullptr;
+  bool valid = false;
+};
+
+// One mesh of a multigrid hierarchy for a single-field linear block (the finest level is the
+// problem mesh). Vectors are allocated in the level's working precision.
+struct MGLevel {
+  int refine = 0;
+  int nc[3] = {1, 1, 1}, nn[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  long long N = 0, ncells = 0, len = 0;
+  int precision = 0;            // 0 FP64, 1 FP32
+  int* cmap = nullptr;          // homogeneous level constraints
+  std::vector<int> h_cmap;
+  bool constrained = false;
+  void* invm_sqrt = nullptr;    // per node, level precision
+  void* inv_diag = nullptr;     // len, level precision
+  void* tables = nullptr;       // CellTables for the LHS (level precision)
+  void* acc = nullptr;          // accumulator
+  void* x = nullptr;            // level solution
+  void* b = nullptr;            // level defect (right-hand side)
+  void* r = nullptr;            // residual / work
+  void* w0 = nullptr;           // work vectors
+  void* w1 = nullptr;
+  double lambda_max = 0.0;      // Chebyshev interval
+  double lambda_min = 0.0;
+  bool eig_done = false;
+  // separable transfer to the next finer level: per axis CSR of the 1-D prolongation
+  // (fine index -> coarse entries) and of its transpose (coarse index -> fine entries)
+  int* p_ptr[3] = {nullptr, nullptr, nullptr};
+  int* p_col[3] = {nullptr, nullptr, nullptr};
+  void* p_val[3] = {nullptr, nullptr, nullptr};
+  int* r_ptr[3] = {nullptr, nullptr, nullptr};
+  int* r_col[3] = {nullptr, nullptr, nullptr};
+  void* r_val[3] = {nullptr, nullptr, nullptr};
+  void* t0 = nullptr;           // transfer work buffers (fine-sized)
+  void* t1 = nullptr;
+  void* cvt = nullptr;          // precision-conversion buffer (coarsest level of a mixed hierarchy)
+};
+
+struct LinearState {
+  ppf_linear_params params;
+  bool params_set = false;
+  bool initialized = false;
+  std::vector<MGLevel> levels;  // coarse .. fine
+  double* rhs = nullptr;        // FP64 fine vectors
+  double* g = nullptr;          // inhomogeneous values
+  double* x_hom = nullptr;      // homogeneous solution (next initial guess)
+  double* r = nullptr;
+  double* p = nullptr;
+  double* q = nullptr;
+  double* z = nullptr;
+  double* inv_diag = nullptr;   // fine FP64 inverse diagonal (Chebyshev preconditioner)
+  double* partial = nullptr;    // dot-product partial sums
+  double cheb_lmax = 0.0, cheb_lmin = 0.0;
+  bool cheb_eig_done = false;
+  int last_iterations = 0;
+  double last_residual = 0.0;
+  double last_rhs_norm = 0.0;
+};
+
+struct BlockState {
+  ppf_block_desc desc;
+  BlockPlan plan[2];  // rhs, lhs
+  LinearState lin;
+};
+
+}  // namespace ppf
+
+struct ppf_handle_s {
+  ppf_mesh_desc mesh;
+  int dim = 2, k = 1, n = 2;
+  int nc[3] = {1, 1, 1}, nn[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  long long N = 0, ncells = 0;
+  std::vector<ppf::FieldState> fields;
+  std::vector<ppf::BlockState> blocks;
+  const ppf::ModelOps* model = nullptr;
+  std::vector<unsigned char> model_obj;
+  std::vector<unsigned char> model_obj_f32;  // FP32 object (operator sets with an FP32 LHS)
+  std::vector<double> constants;
+  double* d_invm = nullptr;
+  double* d_invm_sqrt = nullptr;
+  std::vector<double> h_invm;
+  int* d_err = nullptr;
+  cudaStream_t stream = nullptr;      // stream all work is queued on
+  cudaStream_t own_stream = nullptr;  // the handle's own stream
+  prismspf::SimulationTimer timer;
+  double dt = 0.0;
+  std::string err;
+  bool use_graph = true;
+  double* d_scratch_src = nullptr;  // ppf_apply host-path staging
+  double* d_scratch_dst = nullptr;
+  long long scratch_len = 0;
+  // kernel timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  long long cell_launches = 0;
+  long long all_launches = 0;
+};
+
+namespace ppf {
+
+inline int fail(ppf_handle h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define PPF_CUDA(h, call)                                                                            \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+unsigned grid_for(long long n);
+int check_err(ppf_handle h);
+double* state_ptr(ppf_handle h, int f, int age);
+// records a kernel launch for the statistics; brackets cell launches with events when timing
+int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L, const void* obj, size_t smem);
+int launch_cell(ppf_handle h, int b, int which, const double* const* src);
+int linear_solve(ppf_handle h, int b);
+void free_linear(LinearState& L);
+
+}  // namespace ppf

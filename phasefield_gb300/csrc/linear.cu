@@ -1,0 +1,1025 @@
+// Linear solves of a single-field Linear block: CG preconditioned by nothing, by Chebyshev on
+// the fine operator, or by a geometric-multigrid V-cycle (LinearSolver + MGContext,
+// include/prismspf/solvers/linear_solver.h:47-553).
+//
+//   * operator: the LHS cell kernel (MODE_LHS) on each level, src read with the level's
+//     homogeneous constraints, output zero on constrained rows, scaled by invM^1/2 unless the
+//     tolerance type is AbsoluteResidual (MFOperator::compute_operator, mf_operator.cc:17-32);
+//   * diagonal: unit probes (MODE_DIAG), same scaling, zero entries set to one, inverted
+//     (MFOperator::compute_diagonal + eval_matrix_diagonal, mf_operator.cc:82-255);
+//   * Chebyshev smoother of the first kind on [lambda_max/range, lambda_max] with
+//     lambda_max = 1.2 x the largest eigenvalue of the Lanczos matrix of eig_cg_iterations
+//     CG steps (Jacobi-preconditioned) on the pattern (i mod 11) minus its mean;
+//   * transfers: the Gauss-Lobatto nodal interpolation from a level to the next finer one,
+//     applied axis by axis (prolongation) and its transpose (restriction); images of
+//     periodic nodes are condensed onto their masters and constrained rows zeroed;
+//   * V-cycle: pre-smooth from zero (vmult), residual, restrict, recurse, prolongate-add,
+//     post-smooth (step); the coarsest level applies the smoother (MGCoarseGridApplySmoother);
+//   * mixed precision: all levels but the coarsest in FP32 (smoother, level operators,
+//     transfers); the coarsest level, the outer CG and its residuals and inner products FP64;
+//   * solve: LinearSolver::solve_impl (linear_solver.h:305-345): rhs = S b_rhs - S A g with
+//     g the Dirichlet values (plain read), CG from the previous homogeneous solution,
+//     x = x_hom + g, constraints distributed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "handle.h"
+
+namespace ppf {
+
+// ------------------------------------------------------------------------------------------
+// vector kernels
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void axpby_kernel(long long n, double a, const T* __restrict__ x, double b, T* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = T(a * double(x[i]) + b * double(y[i]));
+}
+
+template <typename Tin, typename Tout>
+__global__ void convert_kernel(long long n, const Tin* __restrict__ x, Tout* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = Tout(x[i]);
+}
+
+template <typename T>
+__global__ void mul_kernel(long long n, const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ y) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = a[i] * b[i];
+}
+
+// per-block partial sums of x.y in FP64 (deterministic two-stage reduction)
+template <typename T>
+__global__ void dot_partial_kernel(long long n, const T* __restrict__ x, const T* __restrict__ y, double* partial) {
+  __shared__ double s[256];
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += double(x[i]) * double(y[i]);
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
+__global__ void dot_final_kernel(int nb, double* partial) {
+  __shared__ double s[256];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partial[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[nb] = s[0];
+}
+
+// dst = scale (.) acc on free rows, zero on constrained rows (per node scale, component blocks)
+template <typename T>
+__global__ void level_finalize_kernel(T* __restrict__ dst, const T* __restrict__ acc, const T* __restrict__ scale,
+                                      const int* __restrict__ cmap, long long N) {
+  const long long base = blockIdx.y * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const long long gi = base + i;
+    const bool free_row = !cmap || cmap[gi] == (int)gi;
+    dst[gi] = free_row ? (scale ? acc[gi] * scale[i] : acc[gi]) : T(0);
+  }
+}
+
+// inverse diagonal: d = scale (.) acc, zero entries -> 1, inverted
+template <typename T>
+__global__ void inv_diag_kernel(T* __restrict__ inv, const T* __restrict__ acc, const T* __restrict__ scale, long long N) {
+  const long long base = blockIdx.y * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const long long gi = base + i;
+    T d = scale ? acc[gi] * scale[i] : acc[gi];
+    if (d == T(0)) d = T(1);
+    inv[gi] = T(1) / d;
+  }
+}
+
+// periodic images add into their master, then images and Dirichlet rows are zeroed
+template <typename T>
+__global__ void condense_add_kernel(long long len, T* v, const int* __restrict__ cmap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const int m = cmap[i];
+    if (m >= 0 && m != (int)i) atomicAdd(v + m, v[i]);
+  }
+}
+template <typename T>
+__global__ void zero_constrained_kernel(long long len, T* v, const int* __restrict__ cmap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    if (cmap[i] != (int)i) v[i] = T(0);
+}
+// images take their master's value (AffineConstraints::distribute with homogeneous rows)
+template <typename T>
+__global__ void copy_masters_kernel(long long len, T* v, const int* __restrict__ cmap) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x) {
+    const int m = cmap[i];
+    if (m != (int)i) v[i] = m >= 0 ? v[m] : T(0);
+  }
+}
+
+// one 1-D sparse operator along `axis`: out(i) = sum_k val[k] in(i with axis index col[k])
+template <typename T>
+__global__ void axis_csr_kernel(const T* __restrict__ in, T* __restrict__ out, int o0, int o1, int o2, int axis,
+                                int in_axis_len, const int* __restrict__ ptr, const int* __restrict__ col,
+                                const T* __restrict__ val) {
+  const long long total = (long long)o0 * o1 * o2;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int i0 = (int)(idx % o0);
+    const int i1 = (int)((idx / o0) % o1);
+    const int i2 = (int)(idx / ((long long)o0 * o1));
+    const int row = axis == 0 ? i0 : (axis == 1 ? i1 : i2);
+    const int d0 = axis == 0 ? in_axis_len : o0;
+    const int d1 = axis == 1 ? in_axis_len : o1;
+    T s = T(0);
+    for (int k = ptr[row]; k < ptr[row + 1]; ++k) {
+      const int c = col[k];
+      const long long j = axis == 0 ? ((long long)i2 * d1 + i1) * d0 + c
+                        : axis == 1 ? ((long long)i2 * d1 + c) * d0 + i0
+                                    : ((long long)c * d1 + i1) * d0 + i0;
+      s += val[k] * in[j];
+    }
+    out[idx] = s;
+  }
+}
+
+// Chebyshev update: u = c1 u + c2 P (b - Ax); x += u
+template <typename T>
+__global__ void cheb_update_kernel(long long n, T* __restrict__ x, T* __restrict__ u, const T* __restrict__ b,
+                                   const T* __restrict__ Ax, const T* __restrict__ pinv, double c1, double c2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T r = Ax ? b[i] - Ax[i] : b[i];
+    const T ui = T(c1) * u[i] + T(c2) * pinv[i] * r;
+    u[i] = ui;
+    x[i] += ui;
+  }
+}
+
+// CG kernels (FP64)
+__global__ void cg_update_xr_kernel(long long n, double alpha, const double* __restrict__ p,
+                                    const double* __restrict__ q, double* __restrict__ x, double* __restrict__ r) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// helpers
+// ------------------------------------------------------------------------------------------
+static size_t esize(int precision) { return precision ? sizeof(float) : sizeof(double); }
+
+template <typename F>
+static void by_precision(int precision, F&& f) {
+  if (precision) f(float(0));
+  else f(double(0));
+}
+
+static int dot(ppf_handle h, LinearState& L, int precision, long long n, const void* x, const void* y, double* out) {
+  const unsigned nb = std::min<long long>(1024, (n + 255) / 256) > 0 ? (unsigned)std::min<long long>(1024, (n + 255) / 256) : 1;
+  if (precision)
+    dot_partial_kernel<float><<<nb, 256, 0, h->stream>>>(n, (const float*)x, (const float*)y, L.partial);
+  else
+    dot_partial_kernel<double><<<nb, 256, 0, h->stream>>>(n, (const double*)x, (const double*)y, L.partial);
+  dot_final_kernel<<<1, 256, 0, h->stream>>>((int)nb, L.partial);
+  h->all_launches += 2;
+  PPF_CUDA(h, cudaMemcpyAsync(out, L.partial + nb, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return PPF_OK;
+}
+
+static void axpby(ppf_handle h, int precision, long long n, double a, const void* x, double b, void* y) {
+  if (precision) axpby_kernel<float><<<grid_for(n), 256, 0, h->stream>>>(n, a, (const float*)x, b, (float*)y);
+  else axpby_kernel<double><<<grid_for(n), 256, 0, h->stream>>>(n, a, (const double*)x, b, (double*)y);
+  h->all_launches++;
+}
+
+static void convert(ppf_handle h, int pin, int pout, long long n, const void* x, void* y) {
+  if (pin == pout) {
+    cudaMemcpyAsync(y, x, n * esize(pin), cudaMemcpyDeviceToDevice, h->stream);
+    return;
+  }
+  if (pin == 0) convert_kernel<double, float><<<grid_for(n), 256, 0, h->stream>>>(n, (const double*)x, (float*)y);
+  else convert_kernel<float, double><<<grid_for(n), 256, 0, h->stream>>>(n, (const float*)x, (double*)y);
+  h->all_launches++;
+}
+
+// lumped mass on a lattice of nc cells per axis (periodic images condensed), inverted sqrt
+static std::vector<double> level_invm_sqrt(ppf_handle h, const int* nc, const int* nn, const double* hh) {
+  const int dim = h->dim, n = h->n, k = h->k;
+  const GLRule g = gauss_lobatto(n);
+  long long N = 1;
+  for (int d = 0; d < dim; ++d) N *= nn[d];
+  // separable: the lumped mass of a node is the product of 1-D lumped masses
+  std::vector<std::vector<double>> m1(dim);
+  for (int d = 0; d < dim; ++d) {
+    m1[d].assign(nn[d], 0.0);
+    for (int c = 0; c < nc[d]; ++c)
+      for (int a = 0; a < n; ++a) m1[d][k * c + a] += g.w[a] * hh[d];
+    if (h->mesh.periodic[d]) {
+      m1[d][0] += m1[d][nn[d] - 1];
+      m1[d][nn[d] - 1] = 0.0;
+    }
+  }
+  std::vector<double> out(N);
+  for (long long i = 0; i < N; ++i) {
+    long long r = i;
+    double m = 1.0;
+    for (int d = 0; d < dim; ++d) {
+      m *= m1[d][r % nn[d]];
+      r /= nn[d];
+    }
+    out[i] = m == 0.0 ? 0.0 : std::sqrt(1.0 / m);
+  }
+  return out;
+}
+
+static bool on_face(const int* nn, long long node, int bid, int dim) {
+  const int d = bid / 2;
+  if (d >= dim) return false;
+  long long c[3] = {node % nn[0], (node / nn[0]) % nn[1], node / ((long long)nn[0] * nn[1])};
+  return (bid % 2 == 0) ? c[d] == 0 : c[d] == nn[d] - 1;
+}
+
+static std::vector<int> level_cmap(ppf_handle h, const FieldState& F, const int* nn) {
+  const int dim = h->dim;
+  long long N = 1;
+  for (int d = 0; d < dim; ++d) N *= nn[d];
+  std::vector<int> cm(F.ncomp * N);
+  for (int c = 0; c < F.ncomp; ++c)
+    for (long long i = 0; i < N; ++i) {
+      long long I = i % nn[0], J = (i / nn[0]) % nn[1], K = i / ((long long)nn[0] * nn[1]);
+      if (h->mesh.periodic[0] && I == nn[0] - 1) I = 0;
+      if (dim > 1 && h->mesh.periodic[1] && J == nn[1] - 1) J = 0;
+      if (dim > 2 && h->mesh.periodic[2] && K == nn[2] - 1) K = 0;
+      cm[c * N + i] = (int)(c * N + (K * nn[1] + J) * nn[0] + I);
+    }
+  for (int c = 0; c < F.ncomp; ++c)
+    for (int b = 0; b < 2 * dim; ++b) {
+      if (!F.desc.dirichlet[c][b]) continue;
+      for (long long i = 0; i < N; ++i) {
+        const long long gi = c * N + i;
+        if (on_face(nn, i, b, dim) && cm[gi] == (int)gi) cm[gi] = -1;
+      }
+    }
+  for (long long gi = 0; gi < (long long)cm.size(); ++gi) {
+    const int m = cm[gi];
+    if (m >= 0 && m != (int)gi && cm[m] < 0) cm[gi] = -1;
+  }
+  return cm;
+}
+
+// 1-D prolongation from a coarse axis with ncc cells to the fine axis with 2 ncc cells
+static void prolongation_1d(const GLRule& g, int k, int ncc, std::vector<int>& ptr, std::vector<int>& col,
+                            std::vector<double>& val) {
+  const int n = k + 1;
+  const int nf = k * 2 * ncc + 1;
+  ptr.assign(nf + 1, 0);
+  col.clear();
+  val.clear();
+  for (int I = 0; I < nf; ++I) {
+    const int cf = std::min(I / k, 2 * ncc - 1);
+    const double xf = g.x[I - k * cf];
+    const int cc = cf / 2;
+    const double xc = ((cf % 2) + xf) * 0.5;
+    for (int j = 0; j < n; ++j) {
+      double L = 1.0;
+      for (int m = 0; m < n; ++m)
+        if (m != j) L *= (xc - g.x[m]) / (g.x[j] - g.x[m]);
+      if (std::fabs(L) > 1e-14) {
+        col.push_back(k * cc + j);
+        val.push_back(L);
+      }
+    }
+    ptr[I + 1] = (int)col.size();
+  }
+}
+
+static void transpose_csr(int nrows, int ncols, const std::vector<int>& ptr, const std::vector<int>& col,
+                          const std::vector<double>& val, std::vector<int>& tptr, std::vector<int>& tcol,
+                          std::vector<double>& tval) {
+  tptr.assign(ncols + 1, 0);
+  for (int c : col) tptr[c + 1]++;
+  for (int i = 0; i < ncols; ++i) tptr[i + 1] += tptr[i];
+  tcol.assign(col.size(), 0);
+  tval.assign(col.size(), 0.0);
+  std::vector<int> pos(tptr.begin(), tptr.end() - 1);
+  for (int r = 0; r < nrows; ++r)
+    for (int q = ptr[r]; q < ptr[r + 1]; ++q) {
+      const int p = pos[col[q]]++;
+      tcol[p] = r;
+      tval[p] = val[q];
+    }
+}
+
+template <typename T>
+static int upload_vec(ppf_handle h, void** dst, const std::vector<T>& v) {
+  PPF_CUDA(h, cudaMalloc(dst, sizeof(T) * std::max<size_t>(1, v.size())));
+  PPF_CUDA(h, cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return PPF_OK;
+}
+
+static int upload_real(ppf_handle h, void** dst, const std::vector<double>& v, int precision) {
+  if (!precision) return upload_vec<double>(h, dst, v);
+  std::vector<float> f(v.begin(), v.end());
+  return upload_vec<float>(h, dst, f);
+}
+
+// ------------------------------------------------------------------------------------------
+// level operators
+// ------------------------------------------------------------------------------------------
+static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode, const void* src, bool plain_read) {
+  const int f = B.desc.field_indices[0];
+  FieldState& F = h->fields[f];
+  CellLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  for (int d = 0; d < 3; ++d) {
+    L.nc[d] = lv.nc[d];
+    L.nn[d] = lv.nn[d];
+  }
+  L.N = lv.N;
+  L.ncells = lv.ncells;
+  const BlockPlan& P = B.plan[1];
+  L.nslots = P.nslots;
+  for (int s = 0; s < P.nslots; ++s) {
+    SlotDesc& sd = L.slots[s];
+    sd.ncomp = h->fields[P.slot_field[s]].ncomp;
+    if (P.slot_age[s] == 5) {
+      sd.ptr = src;
+      sd.is_src = 1;
+      sd.out_index = 0;
+      sd.constrained_read = plain_read ? 0 : (lv.constrained ? 1 : 0);
+      sd.cmap = lv.cmap;
+    } else {
+      // other dependencies exist on the problem lattice only (FP64 single-level solves)
+      sd.ptr = state_ptr(h, P.slot_field[s], P.slot_age[s]);
+    }
+  }
+  L.nout = 1;
+  L.outs[0].acc = lv.acc;
+  L.outs[0].cmap = lv.constrained ? lv.cmap : nullptr;
+  L.outs[0].ncomp = F.ncomp;
+  L.nrows_in = P.nrows_in;
+  L.nrows_out = P.nrows_out;
+  L.tables = lv.tables;
+  L.timer = h->timer;
+  L.block_id = (unsigned)B.desc.id;
+  L.err = h->d_err;
+  const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
+  const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
+  PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));
+  return timed_cell_launch(h, lv.precision, mode, L, obj, smem);
+}
+
+static bool scaled(const LinearState& L) { return L.params.tolerance_type != 0; }
+
+// dst = S A src on level lv (S = invM^1/2 or identity)
+static int level_apply(ppf_handle h, BlockState& B, MGLevel& lv, const void* src, void* dst, bool plain_read = false) {
+  int rc = level_cell_launch(h, B, lv, MODE_LHS, src, plain_read);
+  if (rc) return rc;
+  dim3 grid(grid_for(lv.N), h->fields[B.desc.field_indices[0]].ncomp);
+  const int* cm = lv.constrained ? lv.cmap : nullptr;
+  const bool sc = scaled(B.lin);
+  if (lv.precision)
+    level_finalize_kernel<float><<<grid, 256, 0, h->stream>>>((float*)dst, (const float*)lv.acc,
+                                                              sc ? (const float*)lv.invm_sqrt : nullptr, cm, lv.N);
+  else
+    level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>((double*)dst, (const double*)lv.acc,
+                                                               sc ? (const double*)lv.invm_sqrt : nullptr, cm, lv.N);
+  h->all_launches++;
+  PPF_CUDA(h, cudaGetLastError());
+  return PPF_OK;
+}
+
+static int level_diagonal(ppf_handle h, BlockState& B, MGLevel& lv) {
+  int rc = level_cell_launch(h, B, lv, MODE_DIAG, lv.x, false);
+  if (rc) return rc;
+  dim3 grid(grid_for(lv.N), h->fields[B.desc.field_indices[0]].ncomp);
+  const bool sc = scaled(B.lin);
+  if (lv.precision)
+    inv_diag_kernel<float><<<grid, 256, 0, h->stream>>>((float*)lv.inv_diag, (const float*)lv.acc,
+                                                        sc ? (const float*)lv.invm_sqrt : nullptr, lv.N);
+  else
+    inv_diag_kernel<double><<<grid, 256, 0, h->stream>>>((double*)lv.inv_diag, (const double*)lv.acc,
+                                                         sc ? (const double*)lv.invm_sqrt : nullptr, lv.N);
+  h->all_launches++;
+  PPF_CUDA(h, cudaGetLastError());
+  return PPF_OK;
+}
+
+// largest eigenvalue of the symmetric tridiagonal (diag a, off-diagonal b) by bisection
+static double tridiag_max_eig(const std::vector<double>& a, const std::vector<double>& b) {
+  const int m = (int)a.size();
+  if (m == 0) return 1.0;
+  double lo = a[0], hi = a[0];
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? std::fabs(b[i - 1]) : 0.0) + (i + 1 < m ? std::fabs(b[i]) : 0.0);
+    lo = std::min(lo, a[i] - r);
+    hi = std::max(hi, a[i] + r);
+  }
+  auto count_below = [&](double x) {  // Sturm count of eigenvalues < x
+    int cnt = 0;
+    double q = a[0] - x;
+    if (q < 0) cnt++;
+    for (int i = 1; i < m; ++i) {
+      const double qq = q == 0.0 ? 1e-300 : q;
+      q = a[i] - x - b[i - 1] * b[i - 1] / qq;
+      if (q < 0) cnt++;
+    }
+    return cnt;
+  };
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (count_below(mid) >= m) hi = mid;
+    else lo = mid;
+    if (hi - lo <= 1e-14 * std::max(1.0, std::fabs(hi))) break;
+  }
+  return hi;
+}
+
+// Lanczos estimate of the largest eigenvalue of P A (P = inverse diagonal) on level lv:
+// eig_cg_iterations CG steps on A x = pattern from x = 0 (uses lv.x, lv.b, lv.r, lv.w0, lv.w1)
+template <typename T>
+static int estimate_eigenvalues(ppf_handle h, BlockState& B, MGLevel& lv) {
+  LinearState& L = B.lin;
+  const int prec = lv.precision;
+  std::vector<T> pat(lv.len);
+  std::vector<int>& cm = lv.h_cmap;
+  double mean = 0.0;
+  long long nfree = 0;
+  for (long long i = 0; i < lv.len; ++i)
+    if (cm[i] == (int)i) {
+      mean += double(i % 11);
+      nfree++;
+    }
+  mean /= std::max<long long>(1, nfree);
+  for (long long i = 0; i < lv.len; ++i) pat[i] = cm[i] == (int)i ? T(double(i % 11) - mean) : T(0);
+  PPF_CUDA(h, cudaMemcpyAsync(lv.b, pat.data(), sizeof(T) * lv.len, cudaMemcpyHostToDevice, h->stream));
+  T* x = (T*)lv.x;
+  T* r = (T*)lv.r;
+  T* z = (T*)lv.w0;
+  T* p = (T*)lv.w1;
+  PPF_CUDA(h, cudaMemsetAsync(x, 0, sizeof(T) * lv.len, h->stream));
+  PPF_CUDA(h, cudaMemcpyAsync(r, lv.b, sizeof(T) * lv.len, cudaMemcpyDeviceToDevice, h->stream));
+  const long long n = lv.len;
+  mul_kernel<T><<<grid_for(n), 256, 0, h->stream>>>(n, (const T*)lv.inv_diag, r, z);
+  PPF_CUDA(h, cudaMemcpyAsync(p, z, sizeof(T) * n, cudaMemcpyDeviceToDevice, h->stream));
+  double rz;
+  int rc = dot(h, L, prec, n, r, z, &rz);
+  if (rc) return rc;
+  double r0;
+  rc = dot(h, L, prec, n, r, r, &r0);
+  if (rc) return rc;
+  std::vector<double> alphas, betas;
+  for (int it = 0; it < L.params.eig_cg_iterations; ++it) {
+    rc = level_apply(h, B, lv, p, lv.b);  // b reused as q = A p (pattern no longer needed)
+    if (rc) return rc;
+    double pq;
+    rc = dot(h, L, prec, n, p, lv.b, &pq);
+    if (rc) return rc;
+    if (pq <= 0.0 || !std::isfinite(pq)) break;
+    const double alpha = rz / pq;
+    axpby(h, prec, n, alpha, p, 1.0, x);
+    axpby(h, prec, n, -alpha, lv.b, 1.0, r);
+    alphas.push_back(alpha);
+    double rr;
+    rc = dot(h, L, prec, n, r, r, &rr);
+    if (rc) return rc;
+    if (std::sqrt(rr) < 1e-10 * std::sqrt(r0)) break;
+    mul_kernel<T><<<grid_for(n), 256, 0, h->stream>>>(n, (const T*)lv.inv_diag, r, z);
+    double rz_new;
+    rc = dot(h, L, prec, n, r, z, &rz_new);
+    if (rc) return rc;
+    const double beta = rz_new / rz;
+    rz = rz_new;
+    betas.push_back(beta);
+    axpby(h, prec, n, 1.0, z, beta, p);
+  }
+  // Lanczos matrix of the CG coefficients
+  const int m = (int)alphas.size();
+  std::vector<double> a(m), b(m > 0 ? m - 1 : 0);
+  for (int i = 0; i < m; ++i) {
+    a[i] = 1.0 / alphas[i] + (i > 0 ? betas[i - 1] / alphas[i - 1] : 0.0);
+    if (i + 1 < m) b[i] = std::sqrt(std::max(0.0, betas[i])) / alphas[i];
+  }
+  const double est = tridiag_max_eig(a, b);
+  lv.lambda_max = 1.2 * est;
+  lv.lambda_min = lv.lambda_max / L.params.smoothing_range;
+  lv.eig_done = true;
+  return PPF_OK;
+}
+
+// Chebyshev smoother on level lv: x <- x + p(P A)(P (b - A x)); zero_start: x := 0 first
+template <typename T>
+static int chebyshev(ppf_handle h, BlockState& B, MGLevel& lv, bool zero_start) {
+  const double theta = 0.5 * (lv.lambda_max + lv.lambda_min);
+  const double delta = 0.5 * (lv.lambda_max - lv.lambda_min);
+  const double sigma = theta / delta;
+  const long long n = lv.len;
+  T* x = (T*)lv.x;
+  T* u = (T*)lv.w0;
+  T* Ax = (T*)lv.r;
+  if (zero_start) PPF_CUDA(h, cudaMemsetAsync(x, 0, sizeof(T) * n, h->stream));
+  PPF_CUDA(h, cudaMemsetAsync(u, 0, sizeof(T) * n, h->stream));
+  double rho_prev = 1.0 / sigma;
+  for (int k = 0; k < B.lin.params.smoother_degree; ++k) {
+    const T* ax = nullptr;
+    if (!(zero_start && k == 0)) {
+      int rc = level_apply(h, B, lv, x, Ax);
+      if (rc) return rc;
+      ax = Ax;
+    }
+    double c1, c2;
+    if (k == 0) {
+      c1 = 0.0;
+      c2 = 1.0 / theta;
+    } else {
+      const double rho = 1.0 / (2.0 * sigma - rho_prev);
+      c1 = rho * rho_prev;
+      c2 = 2.0 * rho / delta;
+      rho_prev = rho;
+    }
+    cheb_update_kernel<T><<<grid_for(n), 256, 0, h->stream>>>(n, x, u, (const T*)lv.b, ax, (const T*)lv.inv_diag, c1, c2);
+    h->all_launches++;
+  }
+  PPF_CUDA(h, cudaGetLastError());
+  return PPF_OK;
+}
+
+static int smooth(ppf_handle h, BlockState& B, MGLevel& lv, bool zero_start) {
+  if (lv.precision) return chebyshev<float>(h, B, lv, zero_start);
+  return chebyshev<double>(h, B, lv, zero_start);
+}
+
+// separable transfer between level c (coarse) and c+1 (fine), in precision `prec`
+template <typename T>
+static void transfer(ppf_handle h, MGLevel& cl, MGLevel& fl, const T* in, T* out, bool prolongate, int ncomp) {
+  const int dim = h->dim;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    const T* src = in + comp * (prolongate ? cl.N : fl.N);
+    T* dst = out + comp * (prolongate ? fl.N : cl.N);
+    int cur[3] = {1, 1, 1};
+    for (int d = 0; d < 3; ++d) cur[d] = prolongate ? cl.nn[d] : fl.nn[d];
+    const T* a = src;
+    for (int d = 0; d < dim; ++d) {
+      int nxt[3] = {cur[0], cur[1], cur[2]};
+      nxt[d] = prolongate ? fl.nn[d] : cl.nn[d];
+      T* b = (d == dim - 1) ? dst : (T*)((d % 2 == 0) ? fl.t0 : fl.t1);
+      const int* ptr = prolongate ? cl.p_ptr[d] : cl.r_ptr[d];
+      const int* col = prolongate ? cl.p_col[d] : cl.r_col[d];
+      const T* val = (const T*)(prolongate ? cl.p_val[d] : cl.r_val[d]);
+      const long long total = (long long)nxt[0] * nxt[1] * nxt[2];
+      axis_csr_kernel<T><<<grid_for(total), 256, 0, h->stream>>>(a, b, nxt[0], nxt[1], nxt[2], d, cur[d], ptr, col, val);
+      h->all_launches++;
+      a = b;
+      cur[d] = nxt[d];
+    }
+  }
+}
+
+// V-cycle on level l: lv.b holds the defect, lv.x receives the correction
+static int vcycle(ppf_handle h, BlockState& B, int l) {
+  auto& lvs = B.lin.levels;
+  MGLevel& lv = lvs[l];
+  const int ncomp = h->fields[B.desc.field_indices[0]].ncomp;
+  if (l == 0) return smooth(h, B, lv, true);  // coarse: the smoother as coarse solver
+  int rc = smooth(h, B, lv, true);
+  if (rc) return rc;
+  // residual t = b - A x into lv.r
+  rc = level_apply(h, B, lv, lv.x, lv.r);
+  if (rc) return rc;
+  axpby(h, lv.precision, lv.len, 1.0, lv.b, -1.0, lv.r);
+  MGLevel& cl = lvs[l - 1];
+  // restrict in the fine precision; the coarse level may hold another precision
+  void* cb = (cl.precision == lv.precision) ? cl.b : cl.cvt;
+  if (lv.precision) transfer<float>(h, cl, lv, (const float*)lv.r, (float*)cb, false, ncomp);
+  else transfer<double>(h, cl, lv, (const double*)lv.r, (double*)cb, false, ncomp);
+  if (cl.constrained) {
+    if (lv.precision) {
+      condense_add_kernel<float><<<grid_for(cl.len), 256, 0, h->stream>>>(cl.len, (float*)cb, cl.cmap);
+      zero_constrained_kernel<float><<<grid_for(cl.len), 256, 0, h->stream>>>(cl.len, (float*)cb, cl.cmap);
+    } else {
+      condense_add_kernel<double><<<grid_for(cl.len), 256, 0, h->stream>>>(cl.len, (double*)cb, cl.cmap);
+      zero_constrained_kernel<double><<<grid_for(cl.len), 256, 0, h->stream>>>(cl.len, (double*)cb, cl.cmap);
+    }
+    h->all_launches += 2;
+  }
+  if (cb != cl.b) convert(h, lv.precision, cl.precision, cl.len, cb, cl.b);
+  rc = vcycle(h, B, l - 1);
+  if (rc) return rc;
+  // prolongate-add the coarse correction
+  const void* cx = cl.x;
+  if (cl.precision != lv.precision) {
+    convert(h, cl.precision, lv.precision, cl.len, cl.x, cl.cvt);
+    cx = cl.cvt;
+  }
+  if (lv.precision) transfer<float>(h, cl, lv, (const float*)cx, (float*)lv.r, true, ncomp);
+  else transfer<double>(h, cl, lv, (const double*)cx, (double*)lv.r, true, ncomp);
+  if (lv.constrained) {
+    if (lv.precision) copy_masters_kernel<float><<<grid_for(lv.len), 256, 0, h->stream>>>(lv.len, (float*)lv.r, lv.cmap);
+    else copy_masters_kernel<double><<<grid_for(lv.len), 256, 0, h->stream>>>(lv.len, (double*)lv.r, lv.cmap);
+    h->all_launches++;
+  }
+  axpby(h, lv.precision, lv.len, 1.0, lv.r, 1.0, lv.x);
+  return smooth(h, B, lv, false);
+}
+
+// ------------------------------------------------------------------------------------------
+// set-up
+// ------------------------------------------------------------------------------------------
+static int alloc_real(ppf_handle h, void** p, long long n, int precision) {
+  PPF_CUDA(h, cudaMalloc(p, std::max<long long>(1, n) * esize(precision)));
+  PPF_CUDA(h, cudaMemset(*p, 0, std::max<long long>(1, n) * esize(precision)));
+  return PPF_OK;
+}
+
+static int init_linear(ppf_handle h, int b) {
+  BlockState& B = h->blocks[b];
+  LinearState& L = B.lin;
+  if (!L.params_set) {
+    ppf_default_linear_params(&L.params);
+    L.params_set = true;
+  }
+  if (B.desc.n_fields != 1) return fail(h, PPF_ERR_UNSUPPORTED, "linear blocks with more than one field");
+  if (!B.plan[1].valid) return fail(h, PPF_ERR_ARG, "linear block has no LHS dependencies or no compiled LHS");
+  for (int s = 0; s < B.plan[1].nslots; ++s)
+    if (B.plan[1].slot_age[s] != 5 && L.params.preconditioner == 2)
+      return fail(h, PPF_ERR_UNSUPPORTED, "GMG: the LHS may only depend on src in this build");
+  const int f = B.desc.field_indices[0];
+  FieldState& F = h->fields[f];
+  const long long len = F.len;
+  PPF_CUDA(h, cudaMalloc(&L.rhs, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.g, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.x_hom, sizeof(double) * len));
+  PPF_CUDA(h, cudaMemset(L.x_hom, 0, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.r, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.p, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.q, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.z, sizeof(double) * len));
+  PPF_CUDA(h, cudaMalloc(&L.partial, sizeof(double) * 1100));
+  // levels: coarsest refinement R - depth + 1 .. R (depth 1 = the fine level only)
+  const int R = h->mesh.global_refinement;
+  int depth = L.params.preconditioner == 2 ? std::max(1, L.params.mg_depth) : 1;
+  depth = std::min(depth, R + 1);
+  L.levels.resize(depth);
+  const GLRule g = gauss_lobatto(h->n);
+  for (int l = 0; l < depth; ++l) {
+    MGLevel& lv = L.levels[l];
+    lv.refine = R - depth + 1 + l;
+    lv.N = 1;
+    lv.ncells = 1;
+    for (int d = 0; d < 3; ++d) {
+      if (d < h->dim) {
+        lv.nc[d] = h->mesh.subdivisions[d] << lv.refine;
+        lv.nn[d] = h->k * lv.nc[d] + 1;
+        lv.h[d] = h->mesh.size[d] / lv.nc[d];
+      } else {
+        lv.nc[d] = lv.nn[d] = 1;
+        lv.h[d] = 1.0;
+      }
+      lv.N *= lv.nn[d];
+      lv.ncells *= lv.nc[d];
+    }
+    lv.len = F.ncomp * lv.N;
+    const bool is_fine = l == depth - 1;
+    lv.precision = (L.params.preconditioner == 2 && L.params.mixed_precision && l > 0) ? 1 : 0;
+    lv.h_cmap = level_cmap(h, F, lv.nn);
+    lv.constrained = false;
+    for (long long i = 0; i < lv.len; ++i)
+      if (lv.h_cmap[i] != (int)i) lv.constrained = true;
+    int rc = upload_vec<int>(h, (void**)&lv.cmap, lv.h_cmap);
+    if (rc) return rc;
+    rc = upload_real(h, &lv.invm_sqrt, level_invm_sqrt(h, lv.nc, lv.nn, lv.h), lv.precision);
+    if (rc) return rc;
+    // LHS tables of this level (the block's LHS dependency slots)
+    signed char slot_of[pg::MAX_FIELDS][pg::NAGE];
+    signed char slot_comp0[pg::MAX_SLOTS] = {};
+    signed char out_of[pg::MAX_FIELDS];
+    signed char out_row0[pg::MAX_OUTS] = {};
+    std::memset(slot_of, -1, sizeof(slot_of));
+    std::memset(out_of, -1, sizeof(out_of));
+    int row = 0;
+    for (int s = 0; s < B.plan[1].nslots; ++s) {
+      slot_of[B.plan[1].slot_field[s]][B.plan[1].slot_age[s]] = (signed char)s;
+      slot_comp0[s] = (signed char)row;
+      row += h->fields[B.plan[1].slot_field[s]].ncomp;
+    }
+    out_of[f] = 0;
+    double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
+    auto tab = build_cell_tables(h->dim, h->k, lv.precision, lo, lv.h, slot_of, slot_comp0, out_of, out_row0);
+    PPF_CUDA(h, cudaMalloc(&lv.tables, tab.size()));
+    PPF_CUDA(h, cudaMemcpy(lv.tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+    for (void** p : {&lv.inv_diag, &lv.acc, &lv.x, &lv.b, &lv.r, &lv.w0, &lv.w1}) {
+      rc = alloc_real(h, p, lv.len, lv.precision);
+      if (rc) return rc;
+    }
+    (void)is_fine;
+  }
+  // transfers between consecutive levels (stored on the coarse level; work buffers on the fine)
+  for (int l = 0; l + 1 < depth; ++l) {
+    MGLevel& cl = L.levels[l];
+    MGLevel& fl = L.levels[l + 1];
+    const int tp = fl.precision;  // transfers run in the fine level's precision
+    for (int d = 0; d < h->dim; ++d) {
+      std::vector<int> ptr, col, tptr, tcol;
+      std::vector<double> val, tval;
+      prolongation_1d(g, h->k, cl.nc[d], ptr, col, val);
+      transpose_csr(fl.nn[d], cl.nn[d], ptr, col, val, tptr, tcol, tval);
+      int rc = upload_vec<int>(h, (void**)&cl.p_ptr[d], ptr);
+      if (!rc) rc = upload_vec<int>(h, (void**)&cl.p_col[d], col);
+      if (!rc) rc = upload_real(h, &cl.p_val[d], val, tp);
+      if (!rc) rc = upload_vec<int>(h, (void**)&cl.r_ptr[d], tptr);
+      if (!rc) rc = upload_vec<int>(h, (void**)&cl.r_col[d], tcol);
+      if (!rc) rc = upload_real(h, &cl.r_val[d], tval, tp);
+      if (rc) return rc;
+    }
+    int rc = alloc_real(h, &fl.t0, fl.N, tp);
+    if (!rc) rc = alloc_real(h, &fl.t1, fl.N, tp);
+    if (rc) return rc;
+    if (cl.precision != tp) {  // conversion buffer of coarse size in the transfer precision
+      rc = alloc_real(h, &cl.cvt, cl.len, tp);
+      if (rc) return rc;
+    }
+  }
+  PPF_CUDA(h, cudaDeviceSynchronize());
+  L.initialized = true;
+  return PPF_OK;
+}
+
+static double normalization(ppf_handle h, const LinearState& L) {
+  double v = 1.0;
+  const int t = L.params.tolerance_type;
+  if (t == 1 || t == 3) {
+    double vol = 1.0;
+    for (int d = 0; d < h->dim; ++d) vol *= h->mesh.size[d];
+    v *= std::sqrt(vol);
+  }
+  if (t == 1 || t == 2) v *= 1.0;  // sqrt(number of fields) with one field
+  return v;
+}
+
+// preconditioner application z = M^-1 r (FP64 fine vectors)
+static int precondition(ppf_handle h, BlockState& B, const double* r, double* z) {
+  LinearState& L = B.lin;
+  const long long n = h->fields[B.desc.field_indices[0]].len;
+  if (L.params.preconditioner == 0) {
+    PPF_CUDA(h, cudaMemcpyAsync(z, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    return PPF_OK;
+  }
+  MGLevel& fine = L.levels.back();
+  // the fine level's defect/solution vectors carry the V-cycle (or the Chebyshev smoother)
+  convert(h, 0, fine.precision, n, r, fine.b);
+  int rc = L.params.preconditioner == 1 ? smooth(h, B, fine, true) : vcycle(h, B, (int)L.levels.size() - 1);
+  if (rc) return rc;
+  convert(h, fine.precision, 0, n, fine.x, z);
+  return PPF_OK;
+}
+
+int linear_solve(ppf_handle h, int b) {
+  BlockState& B = h->blocks[b];
+  LinearState& L = B.lin;
+  if (!L.initialized) {
+    int rc = init_linear(h, b);
+    if (rc) return rc;
+  }
+  const int f = B.desc.field_indices[0];
+  FieldState& F = h->fields[f];
+  const long long n = F.len;
+  // FP64 outer operator on the problem lattice (the handle's FP64 LHS plan), also when the
+  // fine multigrid level runs in FP32
+  auto outer_apply = [&](const double* src, double* dst, bool plain) -> int {
+    const double* srcs[PPF_MAX_FIELDS] = {src};
+    PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * n, h->stream));
+    CellLaunch Lc;
+    std::memset(&Lc, 0, sizeof(Lc));
+    for (int d = 0; d < 3; ++d) {
+      Lc.nc[d] = h->nc[d];
+      Lc.nn[d] = h->nn[d];
+    }
+    Lc.N = h->N;
+    Lc.ncells = h->ncells;
+    const BlockPlan& P = B.plan[1];
+    Lc.nslots = P.nslots;
+    for (int s = 0; s < P.nslots; ++s) {
+      SlotDesc& sd = Lc.slots[s];
+      const int sf = P.slot_field[s];
+      sd.ncomp = h->fields[sf].ncomp;
+      if (P.slot_age[s] == 5) {
+        sd.ptr = srcs[0];
+        sd.constrained_read = plain ? 0 : (F.constrained ? 1 : 0);
+        sd.cmap = F.cmap;
+        sd.is_src = 1;
+      } else {
+        sd.ptr = state_ptr(h, sf, P.slot_age[s]);
+      }
+    }
+    Lc.nout = 1;
+    Lc.outs[0].acc = F.acc;
+    Lc.outs[0].cmap = F.constrained ? F.cmap : nullptr;
+    Lc.outs[0].ncomp = F.ncomp;
+    Lc.nrows_in = P.nrows_in;
+    Lc.nrows_out = P.nrows_out;
+    Lc.tables = P.d_tables;
+    Lc.timer = h->timer;
+    Lc.block_id = (unsigned)B.desc.id;
+    Lc.err = h->d_err;
+    const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
+    int rc = timed_cell_launch(h, 0, MODE_LHS, Lc, h->model_obj.data(), smem);
+    if (rc) return rc;
+    dim3 grid(grid_for(h->N), F.ncomp);
+    level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>(dst, F.acc, scaled(L) ? h->d_invm_sqrt : nullptr,
+                                                               F.constrained ? F.cmap : nullptr, h->N);
+    h->all_launches++;
+    PPF_CUDA(h, cudaGetLastError());
+    return PPF_OK;
+  };
+  // diagonals of every level (recomputed for each solve, as the reference does)
+  if (L.params.preconditioner != 0) {
+    for (auto& lv : L.levels) {
+      int rc = level_diagonal(h, B, lv);
+      if (rc) return rc;
+      if (!lv.eig_done) {
+        rc = lv.precision ? estimate_eigenvalues<float>(h, B, lv) : estimate_eigenvalues<double>(h, B, lv);
+        if (rc) return rc;
+      }
+    }
+  }
+  // rhs = S * compute_rhs
+  {
+    PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * n, h->stream));
+    if (B.plan[0].valid && B.plan[0].nslots >= 0) {
+      int rc = launch_cell(h, b, 0, nullptr);
+      if (rc) return rc;
+    }
+    dim3 grid(grid_for(h->N), F.ncomp);
+    level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>(L.rhs, F.acc, scaled(L) ? h->d_invm_sqrt : nullptr,
+                                                               F.constrained ? F.cmap : nullptr, h->N);
+    h->all_launches++;
+  }
+  // inhomogeneous Dirichlet values g and rhs -= S A_plain g
+  PPF_CUDA(h, cudaMemsetAsync(L.g, 0, sizeof(double) * n, h->stream));
+  bool has_inhom = false;
+  for (double v : F.h_dvals) has_inhom |= v != 0.0;
+  if (has_inhom) {
+    std::vector<double> gh(n, 0.0);
+    for (long long i = 0; i < n; ++i)
+      if (F.h_cmap[i] < 0) gh[i] = F.h_dvals[-1 - F.h_cmap[i]];
+    PPF_CUDA(h, cudaMemcpyAsync(L.g, gh.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+    int rc = outer_apply(L.g, L.q, true);
+    if (rc) return rc;
+    axpby(h, 0, n, -1.0, L.q, 1.0, L.rhs);
+  }
+  // CG on S A x = rhs from the previous homogeneous solution (SolverCG)
+  double* x = L.x_hom;
+  const double tol = L.params.tolerance * normalization(h, L);
+  int rc = outer_apply(x, L.q, false);
+  if (rc) return rc;
+  PPF_CUDA(h, cudaMemcpyAsync(L.r, L.rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  axpby(h, 0, n, -1.0, L.q, 1.0, L.r);
+  double rr;
+  rc = dot(h, L, 0, n, L.r, L.r, &rr);
+  if (rc) return rc;
+  double res = std::sqrt(rr);
+  int it = 0;
+  bool converged = res < tol;
+  if (!converged) {
+    rc = precondition(h, B, L.r, L.z);
+    if (rc) return rc;
+    PPF_CUDA(h, cudaMemcpyAsync(L.p, L.z, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    double rz;
+    rc = dot(h, L, 0, n, L.r, L.z, &rz);
+    if (rc) return rc;
+    while (it < L.params.max_iterations) {
+      rc = outer_apply(L.p, L.q, false);
+      if (rc) return rc;
+      double pq;
+      rc = dot(h, L, 0, n, L.p, L.q, &pq);
+      if (rc) return rc;
+      const double alpha = rz / pq;
+      cg_update_xr_kernel<<<grid_for(n), 256, 0, h->stream>>>(n, alpha, L.p, L.q, x, L.r);
+      h->all_launches++;
+      ++it;
+      rc = dot(h, L, 0, n, L.r, L.r, &rr);
+      if (rc) return rc;
+      res = std::sqrt(rr);
+      if (!std::isfinite(res)) return fail(h, PPF_ERR_NAN, "non-finite residual in the linear solve");
+      if (res < tol) {
+        converged = true;
+        break;
+      }
+      rc = precondition(h, B, L.r, L.z);
+      if (rc) return rc;
+      double rz_new;
+      rc = dot(h, L, 0, n, L.r, L.z, &rz_new);
+      if (rc) return rc;
+      const double beta = rz_new / rz;
+      rz = rz_new;
+      axpby(h, 0, n, 1.0, L.z, beta, L.p);
+    }
+  }
+  L.last_iterations = it;
+  L.last_residual = res / normalization(h, L);
+  double bb;
+  rc = dot(h, L, 0, n, L.rhs, L.rhs, &bb);
+  if (rc) return rc;
+  L.last_rhs_norm = std::sqrt(bb);
+  // solution = x_hom + g, then constraints
+  PPF_CUDA(h, cudaMemcpyAsync(F.cur, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  axpby(h, 0, n, 1.0, L.g, 1.0, F.cur);
+  rc = ppf_apply_constraints(h, f);
+  if (rc) return rc;
+  rc = check_err(h);
+  if (rc) return rc;
+  if (!converged) return fail(h, PPF_ERR_NOCONV, "linear solver did not converge before max iterations");
+  return PPF_OK;
+}
+
+void free_linear(LinearState& L) {
+  for (double* p : {L.rhs, L.g, L.x_hom, L.r, L.p, L.q, L.z, L.inv_diag, L.partial}) cudaFree(p);
+  for (auto& lv : L.levels) {
+    cudaFree(lv.cmap);
+    for (void* p : {lv.invm_sqrt, lv.inv_diag, lv.tables, lv.acc, lv.x, lv.b, lv.r, lv.w0, lv.w1, lv.t0, lv.t1, lv.cvt})
+      cudaFree(p);
+    for (int d = 0; d < 3; ++d) {
+      cudaFree(lv.p_ptr[d]);
+      cudaFree(lv.p_col[d]);
+      cudaFree(lv.p_val[d]);
+      cudaFree(lv.r_ptr[d]);
+      cudaFree(lv.r_col[d]);
+      cudaFree(lv.r_val[d]);
+    }
+  }
+  L.levels.clear();
+  L.initialized = false;
+}
+
+}  // namespace ppf
+
+using namespace ppf;
+
+extern "C" {
+
+int ppf_default_linear_params(ppf_linear_params* p) {
+  if (!p) return PPF_ERR_ARG;
+  p->tolerance_type = 0;
+  p->tolerance = 1e-10;
+  p->max_iterations = 100;
+  p->preconditioner = 0;
+  p->mg_depth = 1;
+  p->smoother_degree = 5;
+  p->smoothing_range = 15.0;
+  p->eig_cg_iterations = 10;
+  p->mixed_precision = 0;
+  return PPF_OK;
+}
+
+int ppf_set_linear_params(ppf_handle h, int b, const ppf_linear_params* p) {
+  if (!h || !p || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  if (p->preconditioner < 0 || p->preconditioner > 2 || p->smoother_degree < 1 || p->mg_depth < 1 ||
+      p->max_iterations < 1 || p->eig_cg_iterations < 1 || p->smoothing_range <= 1.0)
+    return fail(h, PPF_ERR_ARG, "invalid linear solver parameters");
+  LinearState& L = h->blocks[b].lin;
+  if (L.initialized) return fail(h, PPF_ERR_ARG, "linear parameters are fixed after the first solve");
+  L.params = *p;
+  L.params_set = true;
+  return PPF_OK;
+}
+
+int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual) {
+  if (!h || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  if (h->blocks[b].desc.solve_type != PPF_LINEAR) return fail(h, PPF_ERR_ARG, "block is not Linear");
+  const int rc = linear_solve(h, b);
+  if (iterations) *iterations = h->blocks[b].lin.last_iterations;
+  if (residual) *residual = h->blocks[b].lin.last_residual;
+  return rc;
+}
+
+int ppf_lhs_diagonal(ppf_handle h, int b, double* out) {
+  if (!h || !out || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  BlockState& B = h->blocks[b];
+  if (!B.lin.initialized) {
+    int rc = init_linear(h, b);
+    if (rc) return rc;
+  }
+  MGLevel& fine = B.lin.levels.back();
+  if (fine.precision) return fail(h, PPF_ERR_ARG, "diagonal export needs an FP64 fine level");
+  int rc = level_diagonal(h, B, fine);
+  if (rc) return rc;
+  std::vector<double> inv(fine.len);
+  PPF_CUDA(h, cudaMemcpyAsync(inv.data(), fine.inv_diag, sizeof(double) * fine.len, cudaMemcpyDeviceToHost, h->stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (long long i = 0; i < fine.len; ++i) out[i] = 1.0 / inv[i];
+  return check_err(h);
+}
+
+}  // extern "C"

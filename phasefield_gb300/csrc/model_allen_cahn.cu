@@ -6,7 +6,12 @@
 namespace ppf {
 namespace {
 
-size_t make_object(int dim, int degree, const double* c, int nc, void* out, size_t cap, std::string* err) {
+size_t make_object(int dim, int degree, int precision, const double* c, int nc, void* out, size_t cap,
+                   std::string* err) {
+  if (precision != 0) {
+    *err = "allen_cahn: only the FP64 operator is compiled";
+    return 0;
+  }
   if (nc < 2) {
     *err = "allen_cahn expects Model constants (m_well, kappa)";
     return 0;
@@ -19,8 +24,7 @@ size_t make_object(int dim, int degree, const double* c, int nc, void* out, size
   return sizeof(o);
 }
 
-const ModelOps ops = {"allen_cahn", false, make_object, dispatch_launch<AllenCahn, false>,
-                      dispatch_occupancy<AllenCahn, false>};
+const ModelOps ops = {"allen_cahn", false, make_object, dispatch_launch<AllenCahn, false>};
 struct Reg {
   Reg() { register_model(&ops); }
 } reg;

@@ -6,7 +6,12 @@
 namespace ppf {
 namespace {
 
-size_t make_object(int dim, int degree, const double* c, int nc, void* out, size_t cap, std::string* err) {
+size_t make_object(int dim, int degree, int precision, const double* c, int nc, void* out, size_t cap,
+                   std::string* err) {
+  if (precision != 0) {
+    *err = "cahn_hilliard: only the FP64 operator is compiled";
+    return 0;
+  }
   if (nc < 3) {
     *err = "cahn_hilliard expects Model constants (McV, KcV, WcV)";
     return 0;
@@ -19,8 +24,7 @@ size_t make_object(int dim, int degree, const double* c, int nc, void* out, size
   return sizeof(o);
 }
 
-const ModelOps ops = {"cahn_hilliard", false, make_object, dispatch_launch<CahnHilliard, false>,
-                      dispatch_occupancy<CahnHilliard, false>};
+const ModelOps ops = {"cahn_hilliard", false, make_object, dispatch_launch<CahnHilliard, false>};
 struct Reg {
   Reg() { register_model(&ops); }
 } reg;

@@ -6,7 +6,12 @@
 namespace ppf {
 namespace {
 
-size_t make_object(int dim, int degree, const double* c, int nc, void* out, size_t cap, std::string* err) {
+size_t make_object(int dim, int degree, int precision, const double* c, int nc, void* out, size_t cap,
+                   std::string* err) {
+  if (precision != 0) {
+    *err = "coupled_acch: only the FP64 operator is compiled";
+    return 0;
+  }
   if (nc < 3) {
     *err = "coupled_acch expects Model constants (Mc, Mn, Kn)";
     return 0;
@@ -19,8 +24,7 @@ size_t make_object(int dim, int degree, const double* c, int nc, void* out, size
   return sizeof(o);
 }
 
-const ModelOps ops = {"coupled_acch", false, make_object, dispatch_launch<CoupledACCH, false>,
-                      dispatch_occupancy<CoupledACCH, false>};
+const ModelOps ops = {"coupled_acch", false, make_object, dispatch_launch<CoupledACCH, false>};
 struct Reg {
   Reg() { register_model(&ops); }
 } reg;

@@ -1,5 +1,5 @@
-// Instantiation and dispatch of cell_kernel<PDE, dim, degree, lhs> for one operator set.
-// Each built-in model's translation unit includes this with its own template.
+// Instantiation and dispatch of cell_kernel<PDE, dim, degree, mode, number> for one operator
+// set. Each built-in model's translation unit includes this with its own template.
 #pragma once
 
 #include <cstring>
@@ -9,11 +9,11 @@
 
 namespace ppf {
 
-template <template <unsigned int, unsigned int, typename> class M, int dim, int degree, bool lhs>
+template <template <unsigned int, unsigned int, typename> class M, int dim, int degree, int mode, typename number>
 cudaError_t launch_one(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
-  using PDE = M<dim, degree, double>;
+  using PDE = M<dim, degree, number>;
   using S = CellShape<dim, degree>;
-  auto kern = cell_kernel<PDE, dim, degree, lhs>;
+  auto kern = cell_kernel<PDE, dim, degree, mode, number>;
   static size_t attr_smem = 0;
   static int occ = 0;
   static int sms = 0;
@@ -39,16 +39,20 @@ cudaError_t launch_one(const CellLaunch& P, const void* obj, size_t smem, cudaSt
   return cudaGetLastError();
 }
 
+// precision: 0 = FP64, 1 = FP32 (LHS modes only, for mixed-precision smoothing)
 template <template <unsigned int, unsigned int, typename> class M, bool with_lhs>
-cudaError_t dispatch_launch(int dim, int degree, bool lhs, const CellLaunch& P, const void* obj, size_t smem,
-                            cudaStream_t s) {
-#define PPF_CASE(D, K)                                                       \
-  if (dim == D && degree == K) {                                             \
-    if constexpr (with_lhs) {                                                \
-      if (lhs) return launch_one<M, D, K, true>(P, obj, smem, s);            \
-    }                                                                        \
-    if (!lhs) return launch_one<M, D, K, false>(P, obj, smem, s);            \
-    return cudaErrorInvalidValue;                                            \
+cudaError_t dispatch_launch(int dim, int degree, int mode, int precision, const CellLaunch& P, const void* obj,
+                            size_t smem, cudaStream_t s) {
+#define PPF_CASE(D, K)                                                                   \
+  if (dim == D && degree == K) {                                                         \
+    if constexpr (with_lhs) {                                                            \
+      if (precision == 0 && mode == MODE_LHS) return launch_one<M, D, K, MODE_LHS, double>(P, obj, smem, s);   \
+      if (precision == 0 && mode == MODE_DIAG) return launch_one<M, D, K, MODE_DIAG, double>(P, obj, smem, s); \
+      if (precision == 1 && mode == MODE_LHS) return launch_one<M, D, K, MODE_LHS, float>(P, obj, smem, s);    \
+      if (precision == 1 && mode == MODE_DIAG) return launch_one<M, D, K, MODE_DIAG, float>(P, obj, smem, s);  \
+    }                                                                                    \
+    if (precision == 0 && mode == MODE_RHS) return launch_one<M, D, K, MODE_RHS, double>(P, obj, smem, s);     \
+    return cudaErrorInvalidValue;                                                        \
   }
   PPF_CASE(2, 1)
   PPF_CASE(2, 2)
@@ -60,37 +64,6 @@ cudaError_t dispatch_launch(int dim, int degree, bool lhs, const CellLaunch& P, 
   PPF_CASE(3, 4)
 #undef PPF_CASE
   return cudaErrorInvalidValue;
-}
-
-template <template <unsigned int, unsigned int, typename> class M, int dim, int degree, bool lhs>
-int occupancy_one(size_t smem) {
-  using S = CellShape<dim, degree>;
-  auto kern = cell_kernel<M<dim, degree, double>, dim, degree, lhs>;
-  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
-  return occ;
-}
-
-template <template <unsigned int, unsigned int, typename> class M, bool with_lhs>
-int dispatch_occupancy(int dim, int degree, bool lhs, size_t smem) {
-#define PPF_CASE(D, K)                                                   \
-  if (dim == D && degree == K) {                                         \
-    if constexpr (with_lhs) {                                            \
-      if (lhs) return occupancy_one<M, D, K, true>(smem);                \
-    }                                                                    \
-    return occupancy_one<M, D, K, false>(smem);                          \
-  }
-  PPF_CASE(2, 1)
-  PPF_CASE(2, 2)
-  PPF_CASE(2, 3)
-  PPF_CASE(2, 4)
-  PPF_CASE(3, 1)
-  PPF_CASE(3, 2)
-  PPF_CASE(3, 3)
-  PPF_CASE(3, 4)
-#undef PPF_CASE
-  return 0;
 }
 
 }  // namespace ppf

@@ -254,8 +254,8 @@ extern "C" int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_w
   L.timer = prismspf::SimulationTimer(dt, 0.0);
   L.block_id = 1;
   L.err = d_err;
-  const size_t smem = cell_smem(dim, degree, L.nrows_in, L.nrows_out);
-  if (model->launch(dim, degree, false, L, &pde, smem, s) != cudaSuccess)
+  const size_t smem = cell_smem(dim, degree, 0, L.nrows_in, L.nrows_out);
+  if (model->launch(dim, degree, MODE_RHS, 0, L, &pde, smem, s) != cudaSuccess)
     return noalloc_fail(PPF_ERR_CUDA, "cell kernel launch failed");
 
   LumpedMass1D lm{};

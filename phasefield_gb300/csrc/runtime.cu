@@ -23,8 +23,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ppf_gb300.h"
-#include "runtime.h"
+#include "handle.h"
 
 namespace ppf {
 
@@ -46,10 +45,6 @@ const ModelOps* find_model(const char* name) {
 // Gauss-Lobatto rule on [0,1]: nodes are the endpoints and the roots of P'_{n-1}; the
 // derivative matrix is built from barycentric weights.
 // ------------------------------------------------------------------------------------------
-struct GLRule {
-  int n;
-  double x[pg::MAX_N], w[pg::MAX_N], D[pg::MAX_N][pg::MAX_N];
-};
 
 static void legendre_pd(int N, double t, double& p, double& dp, double& d2p) {
   // P_N and its first two derivatives at t in (-1,1) by the three-term recurrence
@@ -65,7 +60,7 @@ static void legendre_pd(int N, double t, double& p, double& dp, double& d2p) {
   d2p = (2.0 * t * dp - N * (N + 1.0) * p) / (1.0 - t * t);
 }
 
-static GLRule gauss_lobatto(int n) {
+GLRule gauss_lobatto(int n) {
   GLRule r{};
   r.n = n;
   const int N = n - 1;
@@ -170,6 +165,39 @@ static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
   return out;
 }
 
+// the same tables rounded to FP32 (mixed-precision level operators)
+template <int dim, int degree>
+static std::vector<unsigned char> tables_impl_f32(const double* lo, const double* h,
+                                                  const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
+                                                  const signed char* slot_comp0, const signed char* out_of,
+                                                  const signed char* out_row0) {
+  using T64 = pg::CellTables<dim, degree, double>;
+  using T32 = pg::CellTables<dim, degree, float>;
+  auto b = tables_impl<dim, degree>(lo, h, slot_of, slot_comp0, out_of, out_row0);
+  const T64& a = *reinterpret_cast<const T64*>(b.data());
+  T32 t;
+  std::memset(&t, 0, sizeof(t));
+  auto cvt = [](const double* s, float* d, size_t n) {
+    for (size_t i = 0; i < n; ++i) d[i] = float(s[i]);
+  };
+  cvt(&a.Dh[0][0][0], &t.Dh[0][0][0], sizeof(a.Dh) / sizeof(double));
+  cvt(&a.D2h[0][0][0], &t.D2h[0][0][0], sizeof(a.D2h) / sizeof(double));
+  cvt(&a.Dt[0][0], &t.Dt[0][0], sizeof(a.Dt) / sizeof(double));
+  cvt(a.jxw, t.jxw, sizeof(a.jxw) / sizeof(double));
+  cvt(&a.jxw_ih[0][0], &t.jxw_ih[0][0], sizeof(a.jxw_ih) / sizeof(double));
+  cvt(a.lo, t.lo, 3);
+  cvt(a.h, t.h, 3);
+  cvt(a.gl_x, t.gl_x, sizeof(a.gl_x) / sizeof(double));
+  t.vol = float(a.vol);
+  std::memcpy(t.slot_of, a.slot_of, sizeof(t.slot_of));
+  std::memcpy(t.slot_comp0, a.slot_comp0, sizeof(t.slot_comp0));
+  std::memcpy(t.out_of, a.out_of, sizeof(t.out_of));
+  std::memcpy(t.out_row0, a.out_row0, sizeof(t.out_row0));
+  std::vector<unsigned char> out(sizeof(T32));
+  std::memcpy(out.data(), &t, sizeof(T32));
+  return out;
+}
+
 #define PPF_DD_SWITCH(F, ...)                                  \
   switch (dim * 10 + degree) {                                 \
     case 21: return F<2, 1>(__VA_ARGS__);                       \
@@ -183,10 +211,14 @@ static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
     default: break;                                            \
   }
 
-std::vector<unsigned char> build_cell_tables(int dim, int degree, const double* lo, const double* h,
+std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
                                              const signed char* out_row0) {
+  if (precision == 1) {
+    PPF_DD_SWITCH(tables_impl_f32, lo, h, slot_of, slot_comp0, out_of, out_row0)
+    return {};
+  }
   PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0)
   return {};
 }
@@ -198,9 +230,11 @@ int cell_threads(int dim, int degree) {
   return 0;
 }
 template <int dim, int degree>
-static size_t smem_impl(int a, int b) { return cell_smem_bytes<dim, degree>(a, b); }
-size_t cell_smem(int dim, int degree, int nrows_in, int nrows_out) {
-  PPF_DD_SWITCH(smem_impl, nrows_in, nrows_out)
+static size_t smem_impl(int precision, int a, int b) {
+  return precision ? cell_smem_bytes<dim, degree, float>(a, b) : cell_smem_bytes<dim, degree, double>(a, b);
+}
+size_t cell_smem(int dim, int degree, int precision, int nrows_in, int nrows_out) {
+  PPF_DD_SWITCH(smem_impl, precision, nrows_in, nrows_out)
   return 0;
 }
 
@@ -252,83 +286,6 @@ __global__ void distribute_kernel(double* __restrict__ u, const int* __restrict_
     u[i] = cm >= 0 ? u[cm] : dvals[-1 - cm];
   }
 }
-
-// ------------------------------------------------------------------------------------------
-// handle
-// ------------------------------------------------------------------------------------------
-struct FieldState {
-  int rank = 0, ncomp = 1;
-  long long len = 0;
-  int n_old = 0;
-  double* cur = nullptr;
-  double* old[4] = {nullptr, nullptr, nullptr, nullptr};
-  double* acc = nullptr;
-  int* cmap = nullptr;  // nullptr when the field has no constraints
-  double* dvals = nullptr;
-  std::vector<int> h_cmap;
-  std::vector<double> h_dvals;
-  bool constrained = false;
-};
-
-struct BlockPlan {
-  int nslots = 0;
-  int slot_field[pg::MAX_SLOTS];
-  int slot_age[pg::MAX_SLOTS];
-  int nrows_in = 0, nrows_out = 0;
-  void* d_tables = nullptr;
-  bool valid = false;
-};
-
-struct BlockState {
-  ppf_block_desc desc;
-  BlockPlan plan[2];  // rhs, lhs
-};
-
-}  // namespace ppf
-
-struct ppf_handle_s {
-  ppf_mesh_desc mesh;
-  int dim = 2, k = 1, n = 2;
-  int nc[3] = {1, 1, 1}, nn[3] = {1, 1, 1};
-  double h[3] = {1, 1, 1};
-  long long N = 0, ncells = 0;
-  std::vector<ppf::FieldState> fields;
-  std::vector<ppf::BlockState> blocks;
-  const ppf::ModelOps* model = nullptr;
-  std::vector<unsigned char> model_obj;
-  double* d_invm = nullptr;
-  double* d_invm_sqrt = nullptr;
-  std::vector<double> h_invm;
-  int* d_err = nullptr;
-  cudaStream_t stream = nullptr;      // stream all work is queued on
-  cudaStream_t own_stream = nullptr;  // the handle's own stream
-  prismspf::SimulationTimer timer;
-  double dt = 0.0;
-  std::string err;
-  bool use_graph = true;
-  double* d_scratch_src = nullptr;  // ppf_apply host-path staging
-  double* d_scratch_dst = nullptr;
-  long long scratch_len = 0;
-  // kernel timing
-  bool timing = false;
-  std::vector<cudaEvent_t> ev_pool;
-  size_t ev_used = 0;
-  long long cell_launches = 0;
-  long long all_launches = 0;
-};
-
-namespace ppf {
-
-static int fail(ppf_handle h, int code, const std::string& msg) {
-  if (h) h->err = msg;
-  return code;
-}
-
-#define PPF_CUDA(h, call)                                                                    \
-  do {                                                                                       \
-    cudaError_t e_ = (call);                                                                 \
-    if (e_ != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
-  } while (0)
 
 // lattice node index of periodic master (images folded onto the lower face)
 static long long periodic_master(const ppf_handle h, long long node) {
@@ -542,7 +499,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   }
   if (P.nrows_in + P.nrows_out > 127) return fail(h, PPF_ERR_UNSUPPORTED, "block too large");
   double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
-  auto tab = build_cell_tables(h->dim, h->k, lo, h->h, slot_of, slot_comp0, out_of, out_row0);
+  auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0);
   if (tab.empty()) return fail(h, PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
@@ -550,7 +507,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   return PPF_OK;
 }
 
-static double* state_ptr(ppf_handle h, int f, int age) {
+double* state_ptr(ppf_handle h, int f, int age) {
   FieldState& F = h->fields[f];
   if (age == 0) return F.cur;
   if (age >= 1 && age <= 4) return F.old[age - 1];
@@ -559,7 +516,7 @@ static double* state_ptr(ppf_handle h, int f, int age) {
 
 // Launches the cell kernel of block b (which: 0 rhs, 1 lhs) accumulating into each block
 // field's acc. `src` supplies the SRC dependency per block field (may be null).
-static int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
+int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
   BlockState& B = h->blocks[b];
   BlockPlan& P = B.plan[which];
   if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
@@ -605,7 +562,11 @@ static int launch_cell(ppf_handle h, int b, int which, const double* const* src)
   L.timer = h->timer;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
-  const size_t smem = cell_smem(h->dim, h->k, P.nrows_in, P.nrows_out);
+  const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
+  return timed_cell_launch(h, 0, which == 1 ? MODE_LHS : MODE_RHS, L, h->model_obj.data(), smem);
+}
+
+int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L, const void* obj, size_t smem) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (h->timing) {
     while (h->ev_pool.size() < h->ev_used + 2) {
@@ -617,7 +578,7 @@ static int launch_cell(ppf_handle h, int b, int which, const double* const* src)
     e1 = h->ev_pool[h->ev_used++];
     PPF_CUDA(h, cudaEventRecord(e0, h->stream));
   }
-  cudaError_t e = h->model->launch(h->dim, h->k, which == 1, L, h->model_obj.data(), smem, h->stream);
+  cudaError_t e = h->model->launch(h->dim, h->k, mode, precision, L, obj, smem, h->stream);
   if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("cell kernel launch: ") + cudaGetErrorString(e));
   if (h->timing) PPF_CUDA(h, cudaEventRecord(e1, h->stream));
   h->cell_launches++;
@@ -625,7 +586,7 @@ static int launch_cell(ppf_handle h, int b, int which, const double* const* src)
   return PPF_OK;
 }
 
-static unsigned grid_for(long long n) {
+unsigned grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 152 * 16) g = 152 * 16;
   if (g < 1) g = 1;
@@ -651,7 +612,7 @@ static int explicit_solve(ppf_handle h, int b) {
   return PPF_OK;
 }
 
-static int check_err(ppf_handle h) {
+int check_err(ppf_handle h) {
   int e = 0;
   PPF_CUDA(h, cudaMemcpyAsync(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   PPF_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -689,8 +650,11 @@ static int solve_increment(ppf_handle h, int output_every) {
       if (rc) return rc;
     } else if (d.solve_type == PPF_CONSTANT) {
       // constant fields keep their values
+    } else if (d.solve_type == PPF_LINEAR) {
+      int rc = linear_solve(h, (int)b);
+      if (rc && rc != PPF_ERR_NOCONV) return rc;  // non-convergence is logged, not fatal
     } else {
-      return fail(h, PPF_ERR_UNSUPPORTED, "linear/Newton blocks are driven through the solver entry points");
+      return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks are not implemented in this build");
     }
     if (inc == 0) {
       for (int i = 0; i < d.n_fields; ++i) {
@@ -752,13 +716,20 @@ static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, 
   h->timer = prismspf::SimulationTimer(dt, 0.0);
   h->model_obj.resize(8192);
   std::string merr;
-  const size_t osz = h->model->make_object(h->dim, h->k, constants, n_constants, h->model_obj.data(),
+  const size_t osz = h->model->make_object(h->dim, h->k, 0, constants, n_constants, h->model_obj.data(),
                                            h->model_obj.size(), &merr);
   if (!osz) {
     cerr = merr;
     return PPF_ERR_ARG;
   }
   h->model_obj.resize(osz);
+  h->constants.assign(constants, constants + n_constants);
+  if (h->model->has_lhs) {
+    h->model_obj_f32.resize(8192);
+    const size_t o32 = h->model->make_object(h->dim, h->k, 1, constants, n_constants, h->model_obj_f32.data(),
+                                             h->model_obj_f32.size(), &merr);
+    h->model_obj_f32.resize(o32);
+  }
   if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
     cerr = "no CUDA device available";
     return PPF_ERR_CUDA;
@@ -771,6 +742,7 @@ static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, 
   for (int f = 0; f < n_fields; ++f) {
     FieldState& F = h->fields[f];
     F.rank = fields[f].rank;
+    F.desc = fields[f];
     F.ncomp = F.rank == 0 ? 1 : h->dim;
     F.len = F.ncomp * h->N;
     build_constraints(h.get(), F, fields[f]);
@@ -858,8 +830,10 @@ void ppf_destroy(ppf_handle h) {
     cudaFree(F.cmap);
     cudaFree(F.dvals);
   }
-  for (auto& B : h->blocks)
+  for (auto& B : h->blocks) {
     for (auto& P : B.plan) cudaFree(P.d_tables);
+    free_linear(B.lin);
+  }
   cudaFree(h->d_invm);
   cudaFree(h->d_invm_sqrt);
   cudaFree(h->d_err);

@@ -11,17 +11,17 @@
 namespace ppf {
 
 // A compiled PDE operator set (one user CustomPDE): how to build its device object from the
-// Model constants and how to launch its cell kernel for a (dim, degree, rhs|lhs).
+// Model constants and how to launch its cell kernel for a (dim, degree, mode, precision).
 struct ModelOps {
   const char* name;
   bool has_lhs;
-  // fills `out` (capacity `cap` bytes) with the device object; returns its size, 0 on error
-  size_t (*make_object)(int dim, int degree, const double* c, int nc, void* out, size_t cap, std::string* err);
-  // launches cell_kernel<PDE,dim,degree,lhs>; grid = number of thread blocks
-  cudaError_t (*launch)(int dim, int degree, bool lhs, const CellLaunch& P, const void* obj, size_t smem,
-                        cudaStream_t s);
-  // max resident blocks per SM for the kernel at this smem size
-  int (*occupancy)(int dim, int degree, bool lhs, size_t smem);
+  // fills `out` (capacity `cap` bytes) with the device object in the given precision
+  // (0 FP64, 1 FP32); returns its size, 0 on error
+  size_t (*make_object)(int dim, int degree, int precision, const double* c, int nc, void* out, size_t cap,
+                        std::string* err);
+  // launches cell_kernel<PDE, dim, degree, mode, number>
+  cudaError_t (*launch)(int dim, int degree, int mode, int precision, const CellLaunch& P, const void* obj,
+                        size_t smem, cudaStream_t s);
 };
 
 const ModelOps* find_model(const char* name);
@@ -29,9 +29,9 @@ void register_model(const ModelOps* ops);
 
 // threads per block of the cell kernel for (dim, degree)
 int cell_threads(int dim, int degree);
-size_t cell_smem(int dim, int degree, int nrows_in, int nrows_out);
-// builds CellTables<dim,degree> bytes
-std::vector<unsigned char> build_cell_tables(int dim, int degree, const double* lo, const double* h,
+size_t cell_smem(int dim, int degree, int precision, int nrows_in, int nrows_out);
+// builds CellTables<dim,degree,number> bytes (precision 0 FP64, 1 FP32)
+std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
                                              const signed char* out_row0);

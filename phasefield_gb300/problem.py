@@ -229,6 +229,29 @@ class Problem:
         self._check(self.lib.ppf_apply(self.h, b, which, sp, capi.dptr(dst), scale))
         return dst
 
+    # --- linear solves --------------------------------------------------------------------
+    def set_linear_params(self, b: int, **kw):
+        """LinearSolverParameters of Linear block b (keys of ppf_linear_params)."""
+        p = capi.LinearParams()
+        self.lib.ppf_default_linear_params(C.byref(p))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        self._check(self.lib.ppf_set_linear_params(self.h, b, C.byref(p)))
+
+    def linear_solve(self, b: int, allow_noconv: bool = False) -> tuple[int, float]:
+        its, res = C.c_int(), C.c_double()
+        rc = self.lib.ppf_linear_solve(self.h, b, C.byref(its), C.byref(res))
+        if rc == capi.PPF_ERR_NOCONV and allow_noconv:
+            return its.value, res.value
+        self._check(rc)
+        return its.value, res.value
+
+    def lhs_diagonal(self, b: int) -> np.ndarray:
+        f = self.blocks[b].field_indices[0]
+        out = np.empty(self.field_length(f), dtype=np.float64)
+        self._check(self.lib.ppf_lhs_diagonal(self.h, b, capi.dptr(out)))
+        return out
+
     def set_time(self, increment: int, time: float):
         self._check(self.lib.ppf_set_time(self.h, increment, time))
 

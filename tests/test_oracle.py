@@ -158,3 +158,33 @@ def test_elasticity_patch_uniform_eigenstrain():
     rhs = o.apply(0, 0, None)
     assert np.max(np.abs(Au + rhs)) < 1e-12 * np.max(np.abs(Au))
     assert np.max(np.abs(Au)) > 1e-3
+
+
+@pytest.mark.parametrize("preconditioner,depth", [(1, 1), (2, 2), (2, 3)])
+def test_preconditioned_solves_agree_with_plain_cg(preconditioner, depth):
+    wl = W.eshelby_3d(refine=2, degree=2, size=8.0, n_incl=3)
+    base = dict(tolerance_type=1, tolerance=1e-11, max_iterations=3000, smoother_degree=4)
+    o0 = po.Oracle(wl)
+    o0.set_linear_params(0, preconditioner=0, **base)
+    rc0, its0, _ = o0.linear_solve(0)
+    o1 = po.Oracle(wl)
+    o1.set_linear_params(0, preconditioner=preconditioner, mg_depth=depth, **base)
+    rc1, its1, res1 = o1.linear_solve(0)
+    assert rc0 == 0 and rc1 == 0
+    assert res1 < 1e-11
+    assert its1 < its0
+    u0, u1 = o0.get(0), o1.get(0)
+    assert np.linalg.norm(u1 - u0) < 1e-8 * np.linalg.norm(u0)
+
+
+def test_gmg_iterations_fall_with_depth_symmetric_scaling():
+    wl = W.eshelby_3d(refine=3, degree=1, size=16.0, n_incl=5)
+    its = []
+    for depth in (1, 2, 3):
+        o = po.Oracle(wl)
+        o.set_linear_params(0, tolerance_type=0, tolerance=1e-9, max_iterations=800, preconditioner=2, mg_depth=depth,
+                            smoother_degree=4)
+        rc, it, _ = o.linear_solve(0)
+        assert rc == 0
+        its.append(it)
+    assert its[0] > its[1] > its[2]
