@@ -226,6 +226,56 @@ def gmg_cg_measure(refine=6, depth=7):
     return out
 
 
+def ensemble_measure(steps=30):
+    """Aggregate DoF-updates/s of the 256-instance Allen-Cahn ensemble (cells per side
+    32..256, Q1/Q2, per-instance m_well/kappa, grain ICs), one persistent launch per step
+    under a captured graph after the autotuner's choice, against the same instances run one
+    simulation per launch sequence (a handle each, ppf_run)."""
+    import torch
+    from phasefield_gb300 import ensemble as E
+    from phasefield_gb300 import workloads as W
+    meshes, mw, ka, ics = E.allen_cahn_ensemble(n_instances=256)
+    dofs = sum(len(ic) for ic in ics)
+    dt = 0.01
+    ens = E.Ensemble(meshes, mw, ka, dt)
+    for i, ic in enumerate(ics):
+        ens.upload(i, ic)
+    tune_ms, shape, grid = ens.autotune(steps=3)
+    ens.run(3)
+    ens.synchronize()
+    t0 = time.perf_counter()
+    ens.run(steps)
+    ens.synchronize()
+    batched_s = time.perf_counter() - t0
+    ens.close()
+    # one simulation per launch sequence
+    probs = []
+    for i, m in enumerate(meshes):
+        wl = W.allen_cahn_2d(degree=m.degree, refine=m.global_refinement, m_well=mw[i], kappa=ka[i], dt=dt,
+                             subdivisions=m.subdivisions[:2])
+        wl.initial = {0: ics[i]}
+        p = wl.make_problem()
+        p.solve(1)
+        probs.append(p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        for p in probs:
+            p.lib.ppf_run(p.h, 2 + k, 0)
+    torch.cuda.synchronize()
+    single_s = time.perf_counter() - t0
+    for p in probs:
+        p.close()
+    return {"workload": "256 Allen-Cahn instances, [0,100]^2, cells per side U{32..256}, Q1/Q2, "
+                        "m_well U[0.5,2], kappa U[1,4], 12 seeded grains each, dt 0.01",
+            "dofs_total": dofs, "steps": steps,
+            "batched_dof_updates_per_s": dofs * steps / batched_s,
+            "single_dof_updates_per_s": dofs * steps / single_s,
+            "speedup_batched_vs_single": single_s / batched_s,
+            "autotune": {"ms_per_step": tune_ms, "shape": shape, "grid_multiplier": grid},
+            "launches_per_step_batched": 1}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -321,7 +371,8 @@ def run_ours(args):
         flops_per_launch = cell_flops_per_step() * ncells / 2
         fp64_achieved = flops_per_launch / avg_launch_s / 1e12
         cpu = cpu_baseline_sample()
-        gmg = gmg_cg_measure() if not args.skip_gmg else None
+        gmg = gmg_cg_measure() if not args.skip_extras else None
+        ens = ensemble_measure() if not args.skip_extras else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -335,7 +386,7 @@ def run_ours(args):
                 "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
                                   "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
                                   "flops_per_launch": flops_per_launch, "peak_source": "measured in this run"},
-                "cpu_baseline": cpu, "gmg_cg": gmg}
+                "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens}
         print(json.dumps(line), flush=True)
     p.close()
     if ws > 1:
@@ -349,7 +400,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--skip-gmg", action="store_true", help="omit the GMG-CG measurement")
+    ap.add_argument("--skip-extras", action="store_true", help="omit the GMG-CG and ensemble measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

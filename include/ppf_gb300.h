@@ -177,6 +177,30 @@ int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual);
  * (MFOperator::compute_diagonal, mf_operator.cc:82-101); lattice order, host output. */
 int ppf_lhs_diagonal(ppf_handle h, int b, double* out);
 
+/* ---- Ensembles --------------------------------------------------------------------------
+ * Many independent explicit Allen-Cahn simulations (block 1 of
+ * applications/allen_cahn/explicit/custom_pde.h:72-87) of uneven mesh size (2-D, natural
+ * boundaries), degree 1 or 2 and parameters (m_well, kappa per instance), advanced together
+ * by ONE kernel launch per time step; steps are replayed from a captured CUDA graph. No
+ * counterpart in the reference, which runs one simulation per process. */
+typedef struct ppf_ensemble_s* ppf_ensemble;
+
+int ppf_ensemble_create(int n_instances, const ppf_mesh_desc* meshes, const double* m_well, const double* kappa,
+                        double dt, ppf_ensemble* out);
+void ppf_ensemble_destroy(ppf_ensemble e);
+const char* ppf_ensemble_last_error(ppf_ensemble e);
+long long ppf_ensemble_instance_length(ppf_ensemble e, int instance);
+/* field of one instance in lattice order */
+int ppf_ensemble_upload(ppf_ensemble e, int instance, const double* host);
+int ppf_ensemble_download(ppf_ensemble e, int instance, double* host);
+/* advance every instance by n_steps explicit steps (one launch per step) */
+int ppf_ensemble_run(ppf_ensemble e, int n_steps, int use_graph);
+/* times the candidate tile shapes and grid sizes on `steps` steps of this ensemble, keeps the
+ * fastest and restores the state; outputs the best time per step and the choice */
+int ppf_ensemble_autotune(ppf_ensemble e, int steps, double* best_ms, int* best_shape, int* best_grid);
+int ppf_ensemble_synchronize(ppf_ensemble e);
+int ppf_ensemble_set_stream(ppf_ensemble e, void* stream);
+
 /* Capture the explicit increment loop in a CUDA graph (on by default for ppf_run). */
 int ppf_set_use_graph(ppf_handle h, int on);
 

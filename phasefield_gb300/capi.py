@@ -36,6 +36,10 @@ EXPORTED = [
     "ppf_set_stream", "ppf_kernel_timing", "ppf_kernel_stats", "ppf_kernel_stats_reset",
     "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc",
     "ppf_default_linear_params", "ppf_set_linear_params", "ppf_linear_solve", "ppf_lhs_diagonal",
+    # ensembles (bound in phasefield_gb300/ensemble.py)
+    "ppf_ensemble_create", "ppf_ensemble_destroy", "ppf_ensemble_last_error", "ppf_ensemble_instance_length",
+    "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_run", "ppf_ensemble_autotune",
+    "ppf_ensemble_synchronize", "ppf_ensemble_set_stream",
 ]
 
 

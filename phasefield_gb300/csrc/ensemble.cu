@@ -1,0 +1,545 @@
+// Batched ensemble of independent explicit Allen-Cahn simulations (block 1 of
+// applications/allen_cahn/explicit) of uneven mesh size, degree (Q1/Q2) and parameters,
+// advanced by ONE kernel launch per time step, the step loop captured in a CUDA graph.
+//
+// GB300 design:
+//   * no grid-wide barrier: the state of each instance is kept as its un-normalised
+//     accumulator; a step reads the accumulator of step k, forms n = invM (.) acc on the fly
+//     in the gather (the same product the single-simulation finalize kernel computes), and
+//     scatters the cell integrals of step k+1 into a second accumulator, while it zeroes a
+//     third one (read one step earlier, so no block of this launch touches it). The three
+//     accumulators rotate; a launch depends only on the previous launch having finished.
+//   * one persistent launch for every instance and both degrees: a global list of cell tiles
+//     (instance, first cell) is walked grid-stride; a tile of a Q1 instance runs the Q1 body,
+//     of a Q2 instance the Q2 body (block-uniform branch), with the instance's own mesh
+//     spacing and parameters (m_well, kappa) staged per tile.
+//   * tile shapes (cells per tile for Q1 and for Q2) and the grid size are chosen by a
+//     project-written autotuner that times candidate shapes on the ensemble itself.
+// Natural boundary conditions (the ensemble workload has no constraints).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ppf_gb300.h"
+#include "handle.h"
+#include "models.cuh"
+
+namespace ppf {
+namespace {
+
+struct EnsInstance {
+  int degree;
+  int nc[2];
+  int nn[2];
+  long long N;
+  long long off;  // offset of the instance's vectors in the packed arrays
+  double h[2];
+  double m_well, kappa;
+};
+
+struct EnsTables {  // per degree, staged per tile
+  double Dh[2][3][3];
+  double Dt[3][3];
+  double jxw[9];
+  double jxw_ih[2][9];
+};
+
+struct EnsLaunch {
+  const EnsInstance* inst;
+  const int* tile_inst;         // instance of each tile
+  const long long* tile_cell0;  // first cell of each tile
+  long long ntiles;
+  const double* invm;
+  const double* acc_in;
+  double* acc_out;
+  double* acc_zero;
+  long long total_len;
+  double dt;
+  double gl_w[2][3];   // GL weights per degree (index degree-1)
+  double gl_D[2][3][3];
+};
+
+template <int degree, int CPB>
+__device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cell0, double* smem) {
+  constexpr int n = degree + 1, nq = n * n;
+  using Tab = pg::CellTables<2, degree, double>;
+  Tab* tab = reinterpret_cast<Tab*>(smem);
+  double* vals = smem + (sizeof(Tab) + 7) / 8;
+  double* outs = vals + CPB * nq;
+  const int t = threadIdx.x;
+  // stage the instance's tables (mesh spacing differs per instance)
+  if (t < nq) {
+    const int a = t % n, b = t / n;
+    const double detJ = I.h[0] * I.h[1];
+    const double w = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][b];
+    tab->jxw[t] = w;
+    tab->jxw_ih[0][t] = w / I.h[0];
+    tab->jxw_ih[1][t] = w / I.h[1];
+  }
+  if (t < n * n) {
+    const int i = t / n, j = t % n;
+    tab->Dh[0][i][j] = P.gl_D[degree - 1][i][j] / I.h[0];
+    tab->Dh[1][i][j] = P.gl_D[degree - 1][i][j] / I.h[1];
+    tab->Dt[i][j] = P.gl_D[degree - 1][j][i];
+  }
+  if (t < 8) {
+    reinterpret_cast<signed char*>(tab->out_of)[t] = (t == 0) ? 0 : -1;
+    for (int a = 0; a < pg::NAGE; ++a) tab->slot_of[t][a] = (t == 0 && a == 1) ? 0 : -1;
+  }
+  if (t == 0) {
+    tab->slot_comp0[0] = 0;
+    tab->out_row0[0] = 0;
+    tab->vol = I.h[0] * I.h[1];
+    for (int d = 0; d < 3; ++d) {
+      tab->lo[d] = 0.0;
+      tab->h[d] = d < 2 ? I.h[d] : 1.0;
+    }
+    for (int a = 0; a < n; ++a) tab->gl_x[a] = 0.0;
+  }
+  const int lc = t / nq, q = t - lc * nq;
+  const bool in_tile = lc < CPB;
+  const long long cell = cell0 + lc;
+  const long long ncells = (long long)I.nc[0] * I.nc[1];
+  const bool active = in_tile && cell < ncells;
+  const int qa = q % n, qb = q / n;
+  long long node = 0;
+  int cx = 0, cy = 0;
+  if (active) {
+    cx = (int)(cell % I.nc[0]);
+    cy = (int)(cell / I.nc[0]);
+    node = (long long)(degree * cy + qb) * I.nn[0] + (degree * cx + qa);
+    // gather: n = invM (.) acc of the previous step
+    vals[lc * nq + q] = P.invm[I.off + node] * P.acc_in[I.off + node];
+  }
+  if (in_tile)
+    for (int r = 0; r < 3; ++r) outs[r * CPB * nq + lc * nq + q] = 0.0;
+  __syncthreads();
+  pg::CellCtx<2, degree, double> ctx;
+  ctx.tab = tab;
+  ctx.vals = vals;
+  ctx.outs = outs;
+  ctx.stride = CPB * nq;
+  ctx.lc = lc;
+  ctx.q = q;
+  ctx.cell[0] = cx;
+  ctx.cell[1] = cy;
+  ctx.cell[2] = 0;
+  ctx.err = nullptr;
+  ctx.submitted = 0;
+  if (active) {
+    AllenCahn<2, degree, double> pde{I.m_well, I.kappa};
+    FieldContainer<2, degree, double> fc(ctx);
+    pde.compute_rhs(fc, SimulationTimer(P.dt, 0.0), 1u);
+  }
+  __syncthreads();
+  if (active) {
+    double r = outs[lc * nq + q];
+    {
+      const double* g = outs + 1 * CPB * nq + lc * nq + (q - qa);
+      const double* Dt = tab->Dt[qa];
+#pragma unroll
+      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j], r);
+    }
+    {
+      const double* g = outs + 2 * CPB * nq + lc * nq + (q - qb * n);
+      const double* Dt = tab->Dt[qb];
+#pragma unroll
+      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j * n], r);
+    }
+    atomicAdd(P.acc_out + I.off + node, r);
+  }
+  __syncthreads();
+}
+
+template <int CPB1, int CPB2, int THREADS>
+__global__ void __launch_bounds__(THREADS) ensemble_step_kernel(const EnsLaunch P) {
+  extern __shared__ __align__(16) double ens_smem[];
+  // zero the third accumulator (read one step earlier, untouched by this launch)
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P.total_len;
+       i += (long long)gridDim.x * blockDim.x)
+    P.acc_zero[i] = 0.0;
+  for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
+    const EnsInstance I = P.inst[P.tile_inst[tile]];
+    const long long cell0 = P.tile_cell0[tile];
+    if (I.degree == 1) ens_tile<1, CPB1>(P, I, cell0, ens_smem);
+    else ens_tile<2, CPB2>(P, I, cell0, ens_smem);
+  }
+}
+
+template <int CPB1, int CPB2>
+size_t ens_smem_bytes() {
+  const size_t t1 = (sizeof(pg::CellTables<2, 1, double>) + 7) / 8 * 8 + 8 * 4 * CPB1 * 4;
+  const size_t t2 = (sizeof(pg::CellTables<2, 2, double>) + 7) / 8 * 8 + 8 * 4 * CPB2 * 9;
+  return std::max(t1, t2) + 64;
+}
+
+// extraction of the field values: n = invM (.) acc
+__global__ void ensemble_extract_kernel(double* out, const double* invm, const double* acc, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = invm[i] * acc[i];
+}
+
+// tile-shape candidates: cells per tile for Q1 and for Q2, threads per block
+struct Shape {
+  int cpb1, cpb2, threads;
+};
+constexpr Shape SHAPES[] = {{64, 28, 256}, {32, 14, 128}, {16, 7, 64}};
+constexpr int NSHAPES = 3;
+
+typedef void (*EnsKernel)(const EnsLaunch);
+EnsKernel kernel_for(int s) {
+  switch (s) {
+    case 0: return ensemble_step_kernel<64, 28, 256>;
+    case 1: return ensemble_step_kernel<32, 14, 128>;
+    default: return ensemble_step_kernel<16, 7, 64>;
+  }
+}
+size_t smem_for(int s) {
+  switch (s) {
+    case 0: return ens_smem_bytes<64, 28>();
+    case 1: return ens_smem_bytes<32, 14>();
+    default: return ens_smem_bytes<16, 7>();
+  }
+}
+
+}  // namespace
+}  // namespace ppf
+
+struct ppf_ensemble_s {
+  int n = 0;
+  std::vector<ppf::EnsInstance> h_inst;
+  ppf::EnsInstance* d_inst = nullptr;
+  long long total = 0;
+  double* invm = nullptr;
+  double* acc[3] = {nullptr, nullptr, nullptr};
+  double* scratch = nullptr;
+  int* tile_inst = nullptr;
+  long long* tile_cell0 = nullptr;
+  long long ntiles = 0;
+  int shape = 0;
+  int grid_mult = 4;
+  int sms = 0;
+  double dt = 0.0;
+  long long step = 0;  // accumulator rotation counter
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_shape = -1, graph_grid = -1;
+  long long graph_phase = -1;
+  std::string err;
+  double gl_w[2][3];
+  double gl_D[2][3][3];
+};
+
+namespace ppf {
+namespace {
+
+int efail(ppf_ensemble e, int code, const std::string& m) {
+  if (e) e->err = m;
+  return code;
+}
+
+#define ENS_CUDA(e, call)                                                                            \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return efail(e, PPF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// tile list for the current shape
+int build_tiles(ppf_ensemble e) {
+  const Shape sh = SHAPES[e->shape];
+  std::vector<int> ti;
+  std::vector<long long> tc;
+  for (int i = 0; i < e->n; ++i) {
+    const EnsInstance& I = e->h_inst[i];
+    const long long nc = (long long)I.nc[0] * I.nc[1];
+    const int cpb = I.degree == 1 ? sh.cpb1 : sh.cpb2;
+    for (long long c = 0; c < nc; c += cpb) {
+      ti.push_back(i);
+      tc.push_back(c);
+    }
+  }
+  // interleave instances so consecutive tiles (and thus the blocks of one wave) mix
+  // instances of both degrees
+  std::vector<size_t> order(ti.size());
+  for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+    const long long ra = tc[a] / (e->h_inst[ti[a]].degree == 1 ? sh.cpb1 : sh.cpb2);
+    const long long rb = tc[b] / (e->h_inst[ti[b]].degree == 1 ? sh.cpb1 : sh.cpb2);
+    return ra < rb;
+  });
+  std::vector<int> ti2(ti.size());
+  std::vector<long long> tc2(tc.size());
+  for (size_t k = 0; k < order.size(); ++k) {
+    ti2[k] = ti[order[k]];
+    tc2[k] = tc[order[k]];
+  }
+  if (e->graph) {  // the captured steps point at the previous tile list
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  cudaFree(e->tile_inst);
+  cudaFree(e->tile_cell0);
+  e->ntiles = (long long)ti2.size();
+  ENS_CUDA(e, cudaMalloc(&e->tile_inst, sizeof(int) * e->ntiles));
+  ENS_CUDA(e, cudaMalloc(&e->tile_cell0, sizeof(long long) * e->ntiles));
+  ENS_CUDA(e, cudaMemcpy(e->tile_inst, ti2.data(), sizeof(int) * e->ntiles, cudaMemcpyHostToDevice));
+  ENS_CUDA(e, cudaMemcpy(e->tile_cell0, tc2.data(), sizeof(long long) * e->ntiles, cudaMemcpyHostToDevice));
+  return PPF_OK;
+}
+
+EnsLaunch make_launch(ppf_ensemble e, long long step) {
+  EnsLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.inst = e->d_inst;
+  L.tile_inst = e->tile_inst;
+  L.tile_cell0 = e->tile_cell0;
+  L.ntiles = e->ntiles;
+  L.invm = e->invm;
+  L.acc_in = e->acc[step % 3];
+  L.acc_out = e->acc[(step + 1) % 3];
+  L.acc_zero = e->acc[(step + 2) % 3];
+  L.total_len = e->total;
+  L.dt = e->dt;
+  std::memcpy(L.gl_w, e->gl_w, sizeof(L.gl_w));
+  std::memcpy(L.gl_D, e->gl_D, sizeof(L.gl_D));
+  return L;
+}
+
+int launch_step(ppf_ensemble e, long long step, cudaStream_t s) {
+  EnsKernel k = kernel_for(e->shape);
+  const size_t smem = smem_for(e->shape);
+  long long grid = (long long)e->sms * e->grid_mult;
+  grid = std::max<long long>(1, std::min(grid, e->ntiles));
+  k<<<(unsigned)grid, SHAPES[e->shape].threads, smem, s>>>(make_launch(e, step));
+  return cudaGetLastError() == cudaSuccess ? PPF_OK : efail(e, PPF_ERR_CUDA, "ensemble step launch failed");
+}
+
+}  // namespace
+}  // namespace ppf
+
+using namespace ppf;
+
+extern "C" {
+
+int ppf_ensemble_create(int n_instances, const ppf_mesh_desc* meshes, const double* m_well, const double* kappa,
+                        double dt, ppf_ensemble* out) {
+  if (!out || n_instances < 1 || !meshes || !m_well || !kappa) return PPF_ERR_ARG;
+  *out = nullptr;
+  auto* e = new ppf_ensemble_s();
+  e->n = n_instances;
+  e->dt = dt;
+  for (int deg = 1; deg <= 2; ++deg) {
+    GLRule g = gauss_lobatto(deg + 1);
+    for (int i = 0; i <= deg; ++i) {
+      e->gl_w[deg - 1][i] = g.w[i];
+      for (int j = 0; j <= deg; ++j) e->gl_D[deg - 1][i][j] = g.D[i][j];
+    }
+  }
+  long long off = 0;
+  std::vector<double> invm;
+  for (int i = 0; i < n_instances; ++i) {
+    const ppf_mesh_desc& m = meshes[i];
+    if (m.dim != 2 || m.degree < 1 || m.degree > 2 || m.periodic[0] || m.periodic[1]) {
+      delete e;
+      return PPF_ERR_UNSUPPORTED;
+    }
+    EnsInstance I{};
+    I.degree = m.degree;
+    for (int d = 0; d < 2; ++d) {
+      I.nc[d] = m.subdivisions[d] << m.global_refinement;
+      I.nn[d] = m.degree * I.nc[d] + 1;
+      I.h[d] = m.size[d] / I.nc[d];
+    }
+    I.N = (long long)I.nn[0] * I.nn[1];
+    I.off = off;
+    I.m_well = m_well[i];
+    I.kappa = kappa[i];
+    off += I.N;
+    e->h_inst.push_back(I);
+    // lumped mass of the instance (natural boundaries)
+    std::vector<double> m1[2];
+    for (int d = 0; d < 2; ++d) {
+      m1[d].assign(I.nn[d], 0.0);
+      for (int c = 0; c < I.nc[d]; ++c)
+        for (int a = 0; a <= I.degree; ++a) m1[d][I.degree * c + a] += e->gl_w[I.degree - 1][a] * I.h[d];
+    }
+    for (int J = 0; J < I.nn[1]; ++J)
+      for (int K = 0; K < I.nn[0]; ++K) invm.push_back(1.0 / (m1[0][K] * m1[1][J]));
+  }
+  e->total = off;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, dev);
+  auto bail = [&](int code) {
+    ppf_ensemble_destroy(e);
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(PPF_ERR_CUDA);
+  e->stream = e->own_stream;
+  if (cudaMalloc(&e->d_inst, sizeof(EnsInstance) * n_instances) != cudaSuccess) return bail(PPF_ERR_CUDA);
+  cudaMemcpy(e->d_inst, e->h_inst.data(), sizeof(EnsInstance) * n_instances, cudaMemcpyHostToDevice);
+  if (cudaMalloc(&e->invm, sizeof(double) * off) != cudaSuccess) return bail(PPF_ERR_CUDA);
+  cudaMemcpy(e->invm, invm.data(), sizeof(double) * off, cudaMemcpyHostToDevice);
+  for (int k = 0; k < 3; ++k) {
+    if (cudaMalloc(&e->acc[k], sizeof(double) * off) != cudaSuccess) return bail(PPF_ERR_CUDA);
+    cudaMemset(e->acc[k], 0, sizeof(double) * off);
+  }
+  if (cudaMalloc(&e->scratch, sizeof(double) * off) != cudaSuccess) return bail(PPF_ERR_CUDA);
+  for (int s = 0; s < NSHAPES; ++s)
+    cudaFuncSetAttribute(kernel_for(s), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_for(s));
+  if (build_tiles(e)) return bail(PPF_ERR_CUDA);
+  *out = e;
+  return PPF_OK;
+}
+
+void ppf_ensemble_destroy(ppf_ensemble e) {
+  if (!e) return;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  cudaFree(e->d_inst);
+  cudaFree(e->invm);
+  for (int k = 0; k < 3; ++k) cudaFree(e->acc[k]);
+  cudaFree(e->scratch);
+  cudaFree(e->tile_inst);
+  cudaFree(e->tile_cell0);
+  if (e->own_stream) cudaStreamDestroy(e->own_stream);
+  delete e;
+}
+
+const char* ppf_ensemble_last_error(ppf_ensemble e) { return e ? e->err.c_str() : "null ensemble"; }
+
+long long ppf_ensemble_instance_length(ppf_ensemble e, int i) {
+  if (!e || i < 0 || i >= e->n) return -1;
+  return e->h_inst[i].N;
+}
+
+// upload instance i's field (lattice order): the accumulator holds mass (.) n
+int ppf_ensemble_upload(ppf_ensemble e, int i, const double* host) {
+  if (!e || !host || i < 0 || i >= e->n) return PPF_ERR_ARG;
+  const EnsInstance& I = e->h_inst[i];
+  std::vector<double> im(I.N), acc(I.N);
+  ENS_CUDA(e, cudaMemcpy(im.data(), e->invm + I.off, sizeof(double) * I.N, cudaMemcpyDeviceToHost));
+  for (long long k = 0; k < I.N; ++k) acc[k] = host[k] / im[k];
+  ENS_CUDA(e, cudaMemcpy(e->acc[e->step % 3] + I.off, acc.data(), sizeof(double) * I.N, cudaMemcpyHostToDevice));
+  return PPF_OK;
+}
+
+int ppf_ensemble_download(ppf_ensemble e, int i, double* host) {
+  if (!e || !host || i < 0 || i >= e->n) return PPF_ERR_ARG;
+  const EnsInstance& I = e->h_inst[i];
+  ensemble_extract_kernel<<<grid_for(I.N), 256, 0, e->stream>>>(e->scratch + I.off, e->invm + I.off,
+                                                                  e->acc[e->step % 3] + I.off, I.N);
+  ENS_CUDA(e, cudaGetLastError());
+  ENS_CUDA(e, cudaMemcpyAsync(host, e->scratch + I.off, sizeof(double) * I.N, cudaMemcpyDeviceToHost, e->stream));
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  return PPF_OK;
+}
+
+// advance every instance by n_steps explicit steps: one launch per step; with use_graph the
+// steps are replayed from a captured graph of three steps (one accumulator rotation)
+int ppf_ensemble_run(ppf_ensemble e, int n_steps, int use_graph) {
+  if (!e || n_steps < 0) return PPF_ERR_ARG;
+  int done = 0;
+  if (use_graph) {
+    const long long phase = e->step % 3;
+    if (!e->graph || e->graph_shape != e->shape || e->graph_grid != e->grid_mult || e->graph_phase != phase) {
+      if (e->graph) cudaGraphExecDestroy(e->graph);
+      e->graph = nullptr;
+      cudaGraph_t g;
+      ENS_CUDA(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < 3; ++k) launch_step(e, e->step + k, e->stream);
+      ENS_CUDA(e, cudaStreamEndCapture(e->stream, &g));
+      ENS_CUDA(e, cudaGraphInstantiate(&e->graph, g, 0));
+      cudaGraphDestroy(g);
+      e->graph_shape = e->shape;
+      e->graph_grid = e->grid_mult;
+      e->graph_phase = phase;
+    }
+    while (n_steps - done >= 3) {
+      ENS_CUDA(e, cudaGraphLaunch(e->graph, e->stream));
+      done += 3;
+      e->step += 3;  // phase unchanged
+    }
+  }
+  for (; done < n_steps; ++done) {
+    int rc = launch_step(e, e->step, e->stream);
+    if (rc) return rc;
+    e->step++;
+  }
+  return PPF_OK;
+}
+
+// autotuner: times each tile shape and grid size on `steps` steps of this ensemble (on a copy
+// of the state, which is restored) and keeps the fastest; returns its time per step in ms
+int ppf_ensemble_autotune(ppf_ensemble e, int steps, double* best_ms, int* best_shape, int* best_grid) {
+  if (!e || steps < 1) return PPF_ERR_ARG;
+  // save the state
+  std::vector<double> save(e->total);
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  ENS_CUDA(e, cudaMemcpy(save.data(), e->acc[e->step % 3], sizeof(double) * e->total, cudaMemcpyDeviceToHost));
+  const long long step0 = e->step;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best = 1e300;
+  int bs = e->shape, bg = e->grid_mult;
+  const int grids[] = {1, 2, 4, 8};
+  for (int s = 0; s < NSHAPES; ++s) {
+    e->shape = s;
+    if (build_tiles(e)) return PPF_ERR_CUDA;
+    for (int gm : grids) {
+      e->grid_mult = gm;
+      launch_step(e, e->step, e->stream);  // warm-up
+      e->step++;
+      cudaEventRecord(a, e->stream);
+      for (int k = 0; k < steps; ++k) {
+        launch_step(e, e->step, e->stream);
+        e->step++;
+      }
+      cudaEventRecord(b, e->stream);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms / steps < best) {
+        best = ms / steps;
+        bs = s;
+        bg = gm;
+      }
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e->shape = bs;
+  e->grid_mult = bg;
+  if (build_tiles(e)) return PPF_ERR_CUDA;
+  // restore the state
+  e->step = step0;
+  for (int k = 0; k < 3; ++k) ENS_CUDA(e, cudaMemset(e->acc[k], 0, sizeof(double) * e->total));
+  ENS_CUDA(e, cudaMemcpy(e->acc[e->step % 3], save.data(), sizeof(double) * e->total, cudaMemcpyHostToDevice));
+  if (best_ms) *best_ms = best;
+  if (best_shape) *best_shape = bs;
+  if (best_grid) *best_grid = bg;
+  return PPF_OK;
+}
+
+int ppf_ensemble_synchronize(ppf_ensemble e) {
+  if (!e) return PPF_ERR_ARG;
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  return PPF_OK;
+}
+
+int ppf_ensemble_set_stream(ppf_ensemble e, void* stream) {
+  if (!e) return PPF_ERR_ARG;
+  ENS_CUDA(e, cudaStreamSynchronize(e->stream));
+  if (e->graph) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  e->stream = stream ? static_cast<cudaStream_t>(stream) : e->own_stream;
+  return PPF_OK;
+}
+
+}  // extern "C"
