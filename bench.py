@@ -276,6 +276,53 @@ def ensemble_measure(steps=30):
             "launches_per_step_batched": 1}
 
 
+def adjoint_measure(steps=500, snapshots=32):
+    """Adjoint calibration workload: coupled Allen-Cahn/Cahn-Hilliard 2-D, [0,128]^2, 256^2
+    cells, Q2, dt 1e-3, 500 explicit steps; loss J = sum_i m_i (c_K - c_target)^2 with the
+    target produced by (1.5 Mc, 0.5 Kn); gradient w.r.t. (Mc, Kn, n_0) by the adjoint with 32
+    binomial checkpoint slots, checked against central differences (Mc, Kn) in the same run."""
+    from phasefield_gb300 import workloads as W
+
+    def final_c(Mc, Kn):
+        wl = W.coupled_acch_2d(Mc=Mc, Kn=Kn)
+        p = wl.make_problem()
+        p.solve(steps)
+        c = p.download(0, age=1)
+        m = 1.0 / p.invm()
+        p.close()
+        return c, m
+
+    base = W.coupled_acch_2d()
+    Mc, Mn, Kn = base.constants
+    target, mass = final_c(1.5 * Mc, 0.5 * Kn)
+    p = base.make_problem()
+    N = p.n_nodes
+    p.synchronize()
+    t0 = time.perf_counter()
+    p.adjoint_forward(0, steps, snapshots)
+    cK = p.download(0)
+    dJ = np.concatenate([2.0 * mass * (cK - target), np.zeros(N)])
+    dparams, du0, fsteps = p.adjoint_backward(dJ)
+    el = time.perf_counter() - t0
+    p.close()
+    fd = []
+    for i, (val, key) in enumerate(((Mc, "Mc"), (Kn, "Kn"))):
+        eps = 1e-5 * val
+        args_p = {"Mc": Mc, "Kn": Kn}
+        args_m = dict(args_p)
+        args_p[key] = val + eps
+        args_m[key] = val - eps
+        jp = float(np.sum(mass * (final_c(**args_p)[0] - target) ** 2))
+        jm = float(np.sum(mass * (final_c(**args_m)[0] - target) ** 2))
+        fd.append((jp - jm) / (2 * eps))
+    rel = [abs(dparams[i] - fd[i]) / abs(fd[i]) for i in range(2)]
+    return {"workload": "coupled AC/CH 2-D, [0,128]^2, 256^2 cells, FE_Q(2), dt 1e-3, 500 steps, "
+                        "target from (1.5 Mc, 0.5 Kn), loss sum m (c_K - c_t)^2",
+            "snapshots": snapshots, "forward_plus_backward_s": el, "forward_steps_taken": int(fsteps),
+            "dJ_dMc": float(dparams[0]), "dJ_dKn": float(dparams[1]), "fd_dJ_dMc": fd[0], "fd_dJ_dKn": fd[1],
+            "rel_err_vs_fd": rel, "dJ_dn0_norm": float(np.linalg.norm(du0[N:]))}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -373,6 +420,7 @@ def run_ours(args):
         cpu = cpu_baseline_sample()
         gmg = gmg_cg_measure() if not args.skip_extras else None
         ens = ensemble_measure() if not args.skip_extras else None
+        adj = adjoint_measure() if not args.skip_extras else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -386,7 +434,7 @@ def run_ours(args):
                 "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
                                   "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
                                   "flops_per_launch": flops_per_launch, "peak_source": "measured in this run"},
-                "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens}
+                "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens, "adjoint": adj}
         print(json.dumps(line), flush=True)
     p.close()
     if ws > 1:

@@ -201,6 +201,27 @@ int ppf_ensemble_autotune(ppf_ensemble e, int steps, double* best_ms, int* best_
 int ppf_ensemble_synchronize(ppf_ensemble e);
 int ppf_ensemble_set_stream(ppf_ensemble e, void* stream);
 
+/* ---- Adjoint ------------------------------------------------------------------------------
+ * Hand-written adjoint of the explicit step of a coupled_acch block (fields c, n; scalar,
+ * unconstrained), used to calibrate Mc, Kn and the initial fields. No counterpart in the
+ * reference. Vectors are the block fields concatenated (c then n), lattice order.
+ *
+ * ppf_adjoint_forward: runs n_steps explicit steps from the fields' current vectors (u_0),
+ *   keeping n_snapshots checkpoint slots (u_0 included) placed by the binomial schedule; the
+ *   fields' current vectors then hold u_K.
+ * ppf_adjoint_backward: from dJ/du_K returns dJ/d(Mc, Kn) and dJ/du_0, recomputing the
+ *   states it needs from the checkpoints; forward_steps reports the forward steps taken by the
+ *   forward and backward calls together.
+ * ppf_tangent_linear: forward-mode reference du_K = (dF^K)(du_0, dMc, dKn) along the same
+ *   trajectory (state left unchanged).
+ * ppf_checkpoint_schedule_cost: forward steps of the schedule for (n_steps, n_snapshots). */
+int ppf_adjoint_forward(ppf_handle h, int block, int n_steps, int n_snapshots);
+int ppf_adjoint_backward(ppf_handle h, const double* dJ_duK, double* dJ_dparams, double* dJ_du0,
+                         long long* forward_steps);
+int ppf_tangent_linear(ppf_handle h, int block, int n_steps, const double* du0, const double* dparams,
+                       double* duK);
+long long ppf_checkpoint_schedule_cost(int n_steps, int n_snapshots);
+
 /* Capture the explicit increment loop in a CUDA graph (on by default for ppf_run). */
 int ppf_set_use_graph(ppf_handle h, int on);
 

@@ -40,6 +40,7 @@ EXPORTED = [
     "ppf_ensemble_create", "ppf_ensemble_destroy", "ppf_ensemble_last_error", "ppf_ensemble_instance_length",
     "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_run", "ppf_ensemble_autotune",
     "ppf_ensemble_synchronize", "ppf_ensemble_set_stream",
+    "ppf_adjoint_forward", "ppf_adjoint_backward", "ppf_tangent_linear", "ppf_checkpoint_schedule_cost",
 ]
 
 
@@ -132,6 +133,11 @@ def load() -> C.CDLL:
     lib.ppf_set_linear_params.argtypes = [H, C.c_int, P(LinearParams)]
     lib.ppf_linear_solve.argtypes = [H, C.c_int, P(C.c_int), dp]
     lib.ppf_lhs_diagonal.argtypes = [H, C.c_int, dp]
+    lib.ppf_adjoint_forward.argtypes = [H, C.c_int, C.c_int, C.c_int]
+    lib.ppf_adjoint_backward.argtypes = [H, dp, dp, dp, P(C.c_longlong)]
+    lib.ppf_tangent_linear.argtypes = [H, C.c_int, C.c_int, dp, dp, dp]
+    lib.ppf_checkpoint_schedule_cost.argtypes = [C.c_int, C.c_int]
+    lib.ppf_checkpoint_schedule_cost.restype = C.c_longlong
     _lib = lib
     return lib
 

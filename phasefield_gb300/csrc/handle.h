@@ -77,6 +77,8 @@ struct MGLevel {
   void* cvt = nullptr;          // precision-conversion buffer (coarsest level of a mixed hierarchy)
 };
 
+struct AdjointState;
+
 struct LinearState {
   ppf_linear_params params;
   bool params_set = false;
@@ -131,6 +133,7 @@ struct ppf_handle_s {
   double* d_scratch_src = nullptr;  // ppf_apply host-path staging
   double* d_scratch_dst = nullptr;
   long long scratch_len = 0;
+  ppf::AdjointState* adj = nullptr;  // adjoint / tangent-linear state (created on first use)
   // kernel timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -160,5 +163,8 @@ int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L
 int launch_cell(ppf_handle h, int b, int which, const double* const* src);
 int linear_solve(ppf_handle h, int b);
 void free_linear(LinearState& L);
+int explicit_solve_entry(ppf_handle h, int b);
+struct AdjointState;
+void free_adjoint(AdjointState* A);
 
 }  // namespace ppf

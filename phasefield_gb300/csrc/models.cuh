@@ -207,4 +207,133 @@ struct CoupledACCH {
   PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
 };
 
+// ------------------------------------------------------------------------------------------
+// Hand-written linearisations of the coupled model's explicit block (block 0 above).
+//
+// Per quadrature point the block maps the inputs x = (c, grad c, n, grad n) to the submitted
+// terms y = (v_c, g_c, v_n, g_n):
+//   A = (1-h) fa'' + h fb'',  B = (fb' - fa') h'
+//   v_c = c,  g_c = -dt Mc (A grad c + B grad n)
+//   v_n = n - dt Mn (fb - fa) h',  g_n = -dt Kn Mn grad n
+// The explicit step is u+ = invM (.) R(u) with R the integrated terms. Its Jacobian is applied
+// pointwise through dy/dx:
+//   CoupledACCHTangent: dy = (dy/dx) dx + (dy/dtheta) dtheta, integrated like the forward terms
+//                       (tangent-linear step, dtheta = (dMc, dKn) from the constants);
+//   CoupledACCHAdjoint: given w = invM (.) lambda evaluated as (W, grad W) per field, submits
+//                       (dy/dx)^T w as value/gradient terms (the transposed sum-factorised
+//                       apply gives (dR/du)^T w) and w.(dy/dMc), w.(dy/dKn) as value terms of
+//                       two extra fields whose nodal sums are the parameter gradients.
+// Field indices inside these operators: inputs u = (c, n) as fields 0, 1 at age Current, the
+// direction (dx or w) as fields 0, 1 at age SRC; outputs fields 0, 1 (and 2, 3 for dMc, dKn).
+// ------------------------------------------------------------------------------------------
+template <typename number>
+struct ACCHPoint {
+  number A, B, A_c, A_n, B_c, B_n, dvn_dc, dvn_dn, gc_dMc_fac;
+  number fbfa_hn;  // (fb - fa) h'
+};
+
+template <typename number>
+PPF_HD ACCHPoint<number> acch_point(number c, number n) {
+  constexpr double a1 = -4.776, a2 = 5.1622, a3 = -2.7375, a4 = 1.3687;
+  constexpr double a0 = -1.6704, b0 = -1.5924, b1 = -5.9746, b2 = 5.0;
+  const number c2 = c * c, c3 = c2 * c, c4 = c2 * c2;
+  const number n2 = n * n, n3 = n2 * n, n4 = n2 * n2, n5 = n4 * n;
+  const number fa = a0 + a1 * c + a2 * c2 + a3 * c3 + a4 * c4;
+  const number fa_c = a1 + 2 * a2 * c + 3 * a3 * c2 + 4 * a4 * c3;
+  const number fa_cc = 2 * a2 + 6 * a3 * c + 12 * a4 * c2;
+  const number fa_ccc = 6 * a3 + 24 * a4 * c;
+  const number fb = b0 + b1 * c + b2 * c2;
+  const number fb_c = b1 + 2 * b2 * c;
+  const number fb_cc = 2 * b2;
+  const number h = 10.0 * n3 - 15.0 * n4 + 6.0 * n5;
+  const number hn = 30.0 * n2 - 60.0 * n3 + 30.0 * n4;
+  const number hnn = 60.0 * n - 180.0 * n2 + 120.0 * n3;
+  ACCHPoint<number> p;
+  p.A = (1.0 - h) * fa_cc + h * fb_cc;
+  p.B = (fb_c - fa_c) * hn;
+  p.A_c = (1.0 - h) * fa_ccc;
+  p.A_n = hn * (fb_cc - fa_cc);
+  p.B_c = (fb_cc - fa_cc) * hn;
+  p.B_n = (fb_c - fa_c) * hnn;
+  p.dvn_dc = (fb_c - fa_c) * hn;  // times -dt Mn
+  p.dvn_dn = (fb - fa) * hnn;     // times -dt Mn
+  p.fbfa_hn = (fb - fa) * hn;
+  p.gc_dMc_fac = 0.0;
+  return p;
+}
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct CoupledACCHTangent {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number Mc, Mn, Kn;
+  number dMc, dKn;  // parameter direction
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& vl, const SimulationTimer& t, unsigned int) const {
+    const number dt = t.get_timestep();
+    const number c = vl.template get_value<Scalar, Current>(0).v;
+    const number n = vl.template get_value<Scalar, Current>(1).v;
+    const ScalarGrad cx = vl.template get_gradient<Scalar, Current>(0);
+    const ScalarGrad nx = vl.template get_gradient<Scalar, Current>(1);
+    const number dc = vl.template get_value<Scalar, SRC>(0).v;
+    const number dn = vl.template get_value<Scalar, SRC>(1).v;
+    const ScalarGrad dcx = vl.template get_gradient<Scalar, SRC>(0);
+    const ScalarGrad dnx = vl.template get_gradient<Scalar, SRC>(1);
+    const ACCHPoint<number> p = acch_point<number>(c, n);
+    ScalarGrad gc, gn;
+    for (unsigned int d = 0; d < dim; ++d) {
+      const number lin = (p.A_c * cx[d].v + p.B_c * nx[d].v) * dc + (p.A_n * cx[d].v + p.B_n * nx[d].v) * dn +
+                         p.A * dcx[d].v + p.B * dnx[d].v;
+      gc[d] = -dt * Mc * lin - dt * dMc * (p.A * cx[d].v + p.B * nx[d].v);
+      gn[d] = -dt * Kn * Mn * dnx[d].v - dt * dKn * Mn * nx[d].v;
+    }
+    vl.set_value_term(0, ScalarValue(dc));
+    vl.set_gradient_term(0, gc);
+    vl.set_value_term(1, ScalarValue(dn - dt * Mn * (p.dvn_dc * dc + p.dvn_dn * dn)));
+    vl.set_gradient_term(1, gn);
+  }
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
+};
+
+template <unsigned int dim, unsigned int degree, typename number>
+struct CoupledACCHAdjoint {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number Mc, Mn, Kn;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& vl, const SimulationTimer& t, unsigned int) const {
+    const number dt = t.get_timestep();
+    const number c = vl.template get_value<Scalar, Current>(0).v;
+    const number n = vl.template get_value<Scalar, Current>(1).v;
+    const ScalarGrad cx = vl.template get_gradient<Scalar, Current>(0);
+    const ScalarGrad nx = vl.template get_gradient<Scalar, Current>(1);
+    const number Wc = vl.template get_value<Scalar, SRC>(0).v;
+    const number Wn = vl.template get_value<Scalar, SRC>(1).v;
+    const ScalarGrad Wcx = vl.template get_gradient<Scalar, SRC>(0);
+    const ScalarGrad Wnx = vl.template get_gradient<Scalar, SRC>(1);
+    const ACCHPoint<number> p = acch_point<number>(c, n);
+    // (dy/dx)^T w
+    number ac = Wc - dt * Mn * p.dvn_dc * Wn;  // value entries
+    number an = Wn - dt * Mn * p.dvn_dn * Wn;
+    ScalarGrad gc, gn;
+    number dMc = 0.0, dKn = 0.0;
+    for (unsigned int d = 0; d < dim; ++d) {
+      const number wgc = Wcx[d].v, wgn = Wnx[d].v;
+      ac += -dt * Mc * (p.A_c * cx[d].v + p.B_c * nx[d].v) * wgc;
+      an += -dt * Mc * (p.A_n * cx[d].v + p.B_n * nx[d].v) * wgc;
+      gc[d] = -dt * Mc * p.A * wgc;
+      gn[d] = -dt * Mc * p.B * wgc - dt * Kn * Mn * wgn;
+      dMc += -dt * (p.A * cx[d].v + p.B * nx[d].v) * wgc;
+      dKn += -dt * Mn * nx[d].v * wgn;
+    }
+    vl.set_value_term(0, ScalarValue(ac));
+    vl.set_gradient_term(0, gc);
+    vl.set_value_term(1, ScalarValue(an));
+    vl.set_gradient_term(1, gn);
+    vl.set_value_term(2, ScalarValue(dMc));
+    vl.set_value_term(3, ScalarValue(dKn));
+  }
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>&, const SimulationTimer&, unsigned int) const {}
+};
+
 }  // namespace ppf

@@ -593,6 +593,9 @@ unsigned grid_for(long long n) {
   return (unsigned)g;
 }
 
+static int explicit_solve(ppf_handle h, int b);
+int explicit_solve_entry(ppf_handle h, int b) { return explicit_solve(h, b); }
+
 static int explicit_solve(ppf_handle h, int b) {
   BlockState& B = h->blocks[b];
   for (int i = 0; i < B.desc.n_fields; ++i) {
@@ -834,6 +837,7 @@ void ppf_destroy(ppf_handle h) {
     for (auto& P : B.plan) cudaFree(P.d_tables);
     free_linear(B.lin);
   }
+  free_adjoint(h->adj);
   cudaFree(h->d_invm);
   cudaFree(h->d_invm_sqrt);
   cudaFree(h->d_err);

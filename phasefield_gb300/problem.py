@@ -252,6 +252,27 @@ class Problem:
         self._check(self.lib.ppf_lhs_diagonal(self.h, b, capi.dptr(out)))
         return out
 
+    # --- adjoint (coupled_acch explicit block) --------------------------------------------
+    def adjoint_forward(self, b: int, n_steps: int, n_snapshots: int):
+        self._check(self.lib.ppf_adjoint_forward(self.h, b, n_steps, n_snapshots))
+
+    def adjoint_backward(self, dJ_duK: np.ndarray):
+        """Returns (dJ/d(Mc, Kn), dJ/du_0, forward steps taken)."""
+        g = np.ascontiguousarray(dJ_duK, dtype=np.float64)
+        dp = np.zeros(2)
+        du0 = np.zeros_like(g)
+        steps = C.c_longlong()
+        self._check(self.lib.ppf_adjoint_backward(self.h, capi.dptr(g), capi.dptr(dp), capi.dptr(du0),
+                                                  C.byref(steps)))
+        return dp, du0, steps.value
+
+    def tangent_linear(self, b: int, n_steps: int, du0: np.ndarray, dparams) -> np.ndarray:
+        d0 = np.ascontiguousarray(du0, dtype=np.float64)
+        dp = np.ascontiguousarray(dparams, dtype=np.float64)
+        out = np.zeros_like(d0)
+        self._check(self.lib.ppf_tangent_linear(self.h, b, n_steps, capi.dptr(d0), capi.dptr(dp), capi.dptr(out)))
+        return out
+
     def set_time(self, increment: int, time: float):
         self._check(self.lib.ppf_set_time(self.h, increment, time))
 

@@ -151,8 +151,12 @@ def eshelby_3d(refine: int = 6, degree: int = 2, seed: int = 777, size: float = 
 
 
 def coupled_acch_2d(refine: int = 8, degree: int = 2, seed: int = 99, size: float = 128.0, n_steps: int = 500,
-                    dt: float = 1e-3, Mc: float = 1.0, Mn: float = 1.0, Kn: float = 2.0, n_precip: int = 8) -> Workload:
-    """Coupled Allen-Cahn / Cahn-Hilliard: fields c, n, f_tot, mag_grad_c (coupled app main.cc)."""
+                    dt: float = 2e-4, Mc: float = 1.0, Mn: float = 1.0, Kn: float = 2.0, n_precip: int = 8) -> Workload:
+    """Coupled Allen-Cahn / Cahn-Hilliard: fields c, n, f_tot, mag_grad_c (coupled app main.cc).
+
+    The application's free energy has f'' of about 10, so the explicit limit on the 256^2 Q2
+    mesh of [0,128]^2 is about dt = 1e-3 / Mc; dt = 2e-4 keeps the step stable for the
+    calibration targets (Mc up to 1.5)."""
     mesh = RectangularMesh(dim=2, degree=degree, size=(size, size), subdivisions=(1, 1, 1), global_refinement=refine)
     fields = [FieldAttributes("c"), FieldAttributes("n"), FieldAttributes("f_tot"), FieldAttributes("mag_grad_c")]
     exp_block = SolveBlock(id=0, solve_type=Explicit, solve_timing=Primary, field_indices=[0, 1],
