@@ -379,11 +379,8 @@ def run_ours(args):
     cell_n, all_n = C.c_longlong(), C.c_longlong()
     lib.ppf_kernel_stats(p.h, C.byref(cell_ms), C.byref(cell_n), C.byref(all_n))
     lib.ppf_kernel_timing(p.h, 0)
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    max_ms = float(t.item())
-    dof_updates = 2 * N * args.steps * ws
+    from phasefield_gb300 import replicas
+    max_ms, dof_updates = replicas.aggregate(total_ms, 2 * N * args.steps, dist if ws > 1 else None, dev)
     value = dof_updates / (max_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ----

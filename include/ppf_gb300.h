@@ -222,7 +222,10 @@ int ppf_tangent_linear(ppf_handle h, int block, int n_steps, const double* du0, 
                        double* duK);
 long long ppf_checkpoint_schedule_cost(int n_steps, int n_snapshots);
 
-/* Capture the explicit increment loop in a CUDA graph (on by default for ppf_run). */
+/* Replay the explicit increment loop of ppf_run from a CUDA graph (on by default): one graph
+ * holds as many increments as the age-rotation period, each followed by a device-side timer
+ * advance. Used from increment 2 on when every block is Explicit or Constant, no PostProcess
+ * output is requested and kernel timing is off. */
 int ppf_set_use_graph(ppf_handle h, int on);
 
 /* Device pointer of a field state (for zero-copy callers), valid until the next rotation. */

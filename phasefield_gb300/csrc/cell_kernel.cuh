@@ -66,6 +66,7 @@ struct CellLaunch {
   int nrows_out;     // sum over outputs of ncomp * (1 + dim)
   const void* tables;  // device copy of CellTables<dim,degree,number>
   SimulationTimer timer;
+  const SimulationTimer* timer_dev;  // when set (graph replays), the timer is read from here
   unsigned int block_id;
   int* err;
 };
@@ -195,8 +196,9 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
       ctx.submitted = 0;
       if (active) {
         FieldContainer<dim, degree, number> fc(ctx);
-        if constexpr (MODE == MODE_LHS) pde.compute_lhs(fc, P.timer, P.block_id);
-        else pde.compute_rhs(fc, P.timer, P.block_id);
+        const SimulationTimer timer = P.timer_dev ? *P.timer_dev : P.timer;
+        if constexpr (MODE == MODE_LHS) pde.compute_lhs(fc, timer, P.block_id);
+        else pde.compute_rhs(fc, timer, P.block_id);
         if (ctx.submitted) atomicOr(&sflags, ctx.submitted);
       }
       __syncthreads();
@@ -261,7 +263,8 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
           ctx.submitted = 0;
           if (active) {
             FieldContainer<dim, degree, number> fc(ctx);
-            pde.compute_lhs(fc, P.timer, P.block_id);
+            const SimulationTimer timer = P.timer_dev ? *P.timer_dev : P.timer;
+            pde.compute_lhs(fc, timer, P.block_id);
             if (ctx.submitted) atomicOr(&sflags, ctx.submitted);
           }
           __syncthreads();

@@ -134,6 +134,15 @@ struct ppf_handle_s {
   double* d_scratch_dst = nullptr;
   long long scratch_len = 0;
   ppf::AdjointState* adj = nullptr;  // adjoint / tangent-linear state (created on first use)
+  // CUDA graph of the explicit increment loop
+  prismspf::SimulationTimer* d_timer = nullptr;
+  cudaGraphExec_t run_graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int graph_period = 0;
+  long long graph_phase = 0;
+  long long graph_launches = 0;
+  long long rot_count = 0;
+  bool capturing = false;
   // kernel timing
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;

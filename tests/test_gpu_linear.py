@@ -79,6 +79,29 @@ def test_linear_block_runs_in_increment_loop(gpu_lib):
     assert rel_l2(p.download(0), o.get(0)) < 1e-8
 
 
+@pytest.mark.parametrize("tolerance_type", [0, 1])
+def test_inhomogeneous_dirichlet_lift_matches_oracle(gpu_lib, tolerance_type):
+    # u = 0 on x = 0 and a prescribed displacement u_x = 0.05 on x = 16 (boundary id 1):
+    # rhs -= S A_plain g (linear_solver.h:316-327), then x = x_hom + g
+    wl = small_elasticity(degree=2, refine=2)
+    wl.fields[0].dirichlet[(0, 1)] = 0.05
+    prm = dict(tolerance_type=tolerance_type, tolerance=1e-11, max_iterations=2000, preconditioner=2, mg_depth=2,
+               smoother_degree=4)
+    p = wl.make_problem()
+    p.set_linear_params(0, **prm)
+    p.linear_solve(0)
+    o = po.Oracle(wl)
+    o.set_linear_params(0, **prm)
+    rc, _, _ = o.linear_solve(0)
+    assert rc == 0
+    u, ref = p.download(0), o.get(0)
+    assert rel_l2(u, ref) < 1e-8
+    # the prescribed face carries the Dirichlet value
+    x = W.lattice_coordinates(wl.mesh)
+    face = np.isclose(x[:, 0], 16.0)
+    assert np.allclose(u[: len(x)][face], 0.05, rtol=0, atol=1e-14)
+
+
 def test_nonconvergence_reports_noconv(gpu_lib):
     wl = small_elasticity(degree=1, refine=2)
     p = wl.make_problem()

@@ -190,6 +190,24 @@ def test_coupled_two_field_block_steps(gpu_lib):
         assert rel_l2(p.download(f), o.get(f, 0)) < STEPS_TOL
 
 
+@pytest.mark.parametrize("which", ["ch", "acch"])
+def test_graph_replay_matches_plain_launches(gpu_lib, which):
+    if which == "ch":
+        wl = W.cahn_hilliard_3d(refine=2, degree=2, size=4.0, dt=1e-4)
+    else:
+        wl = W.coupled_acch_2d(refine=4, degree=2, size=32.0, dt=1e-3)
+    res = []
+    for use_graph in (0, 1):
+        p = wl.make_problem()
+        p.lib.ppf_set_use_graph(p.h, use_graph)
+        p.solve(23)
+        res.append([p.download(f, age=1) for f in (0, 1)])
+        assert p.get_time()[0] == 24
+        p.close()
+    for a, b in zip(res[0], res[1]):
+        assert rel_l2(b, a) < 1e-12
+
+
 def test_dealii_ordering_roundtrip(gpu_lib):
     wl = W.cahn_hilliard_3d(refine=1, degree=2, size=2.0)
     p = wl.make_problem()
