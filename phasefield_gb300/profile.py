@@ -1,14 +1,19 @@
-"""Runs a few increments of a named workload on cuda:0 (for profilers such as ncu).
+"""Runs a short, fixed piece of a named workload on cuda:0 (for profilers such as ncu).
 
   python -m phasefield_gb300.profile --workload cahn_hilliard_3d --refine 6 --steps 3
+  python -m phasefield_gb300.profile --workload eshelby_3d --refine 5 --mixed 1
+  python -m phasefield_gb300.profile --workload ensemble --steps 3
 
-The workloads are those of phasefield_gb300.workloads with their default parameters except
-the refinement level; the command exits non-zero if the run reports an error.
+Explicit workloads run `steps` increments; eshelby_3d runs one GMG-CG solve (mg_depth =
+refine + 1, Chebyshev degree 4, FP32 smoothing with --mixed 1); ensemble runs `steps` steps of
+the 256-instance Allen-Cahn ensemble. The command exits non-zero if a run reports an error.
 """
 from __future__ import annotations
 
 import argparse
 import sys
+
+import numpy as np
 
 from . import workloads as W
 
@@ -16,17 +21,39 @@ from . import workloads as W
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="cahn_hilliard_3d",
-                    choices=["allen_cahn_2d", "cahn_hilliard_3d", "coupled_acch_2d"])
+                    choices=["allen_cahn_2d", "cahn_hilliard_3d", "coupled_acch_2d", "eshelby_3d", "ensemble"])
     ap.add_argument("--refine", type=int, default=None)
     ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--mixed", type=int, default=0)
     args = ap.parse_args(argv)
     kw = {} if args.refine is None else {"refine": args.refine}
-    wl = getattr(W, args.workload)(**kw)
-    p = wl.make_problem()
-    p.solve(args.steps)
-    p.synchronize()
-    p.close()
-    print(f"{args.workload}: {args.steps} increments ok")
+    if args.workload == "ensemble":
+        from . import ensemble as E
+        meshes, mw, ka, ics = E.allen_cahn_ensemble(n_instances=256)
+        ens = E.Ensemble(meshes, mw, ka, 0.01)
+        for i, ic in enumerate(ics):
+            ens.upload(i, ic)
+        ens.run(args.steps, use_graph=False)
+        ens.synchronize()
+        ens.close()
+    elif args.workload == "eshelby_3d":
+        wl = W.eshelby_3d(**kw)
+        p = wl.make_problem()
+        b = p.apply(0, 0, None, scale=0)
+        p.set_linear_params(0, tolerance_type=0, tolerance=1e-10 * float(np.linalg.norm(b)), max_iterations=500,
+                            preconditioner=2, mg_depth=wl.mesh.global_refinement + 1, smoother_degree=4,
+                            mixed_precision=args.mixed)
+        its, _ = p.linear_solve(0)
+        p.close()
+        print(f"eshelby_3d: GMG-CG {its} iterations ok")
+        return 0
+    else:
+        wl = getattr(W, args.workload)(**kw)
+        p = wl.make_problem()
+        p.solve(args.steps)
+        p.synchronize()
+        p.close()
+    print(f"{args.workload}: {args.steps} steps ok")
     return 0
 
 
