@@ -98,6 +98,49 @@ int ppf_create(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fi
 void ppf_destroy(ppf_handle h);
 const char* ppf_last_error(ppf_handle h);
 
+/* A PDE operator compiled outside this library: the user's CustomPDE, instantiated by the
+ * drop-in prismspf/core/problem.h in the user's own translation unit (the callbacks of
+ * PDEOperatorBase::compute_rhs / compute_lhs, pde_operator_base.h:77-90). For every
+ * cell-kernel launch the engine calls `launch` with its launch record (`cell_launch`, a
+ * ppf::CellLaunch from prismspf/gpu/cell_kernel.cuh), the operator object bytes of the
+ * requested precision (host memory; they travel as a kernel argument), the dynamic shared
+ * memory size and the CUDA stream (a cudaStream_t). `launch` returns a cudaError_t value.
+ * mode: 0 rhs, 1 lhs, 2 lhs diagonal probe; precision: 0 FP64, 1 FP32. */
+typedef int (*ppf_cell_launch_fn)(int dim, int degree, int mode, int precision, const void* cell_launch,
+                                  const void* object, size_t smem, void* stream);
+typedef struct {
+  const char* name;
+  int has_lhs;                 /* compute_lhs is implemented (Linear blocks) */
+  const void* object;          /* FP64 operator object bytes */
+  size_t object_size;
+  const void* object_f32;      /* FP32 operator object (mixed-precision smoothing) or NULL */
+  size_t object_f32_size;
+  ppf_cell_launch_fn launch;
+  size_t cell_launch_size;     /* sizeof(ppf::CellLaunch) in the caller's build (layout check) */
+} ppf_model_desc;
+
+/* ppf_create for an operator compiled by the caller (Problem::Problem + init_system,
+ * problem.cc:229-338, with the user's PDEOperatorBase). The object bytes are copied. */
+int ppf_create_custom(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields,
+                      const ppf_block_desc* blocks, int n_blocks, const ppf_model_desc* model, double dt,
+                      ppf_handle* out);
+
+/* Per-node Dirichlet values of field f (the values set_dirichlet returns at the boundary
+ * support points, constraint_manager.cc:427-446): `values` is a lattice-order vector of the
+ * field's length; the entries at Dirichlet-constrained positions are taken, the rest ignored.
+ * Replaces the per-face constants of ppf_field_desc from this call on. */
+int ppf_set_dirichlet_values(ppf_handle h, int field, const double* values);
+
+/* Support points of cells [first_cell, first_cell + n_cells) in deal.II's active-cell order,
+ * each cell's (degree+1)^dim points in FE_Q's local DoF order (vertices, lines, faces,
+ * interior): the order VectorTools::interpolate visits them when it evaluates an initial
+ * condition (solver_base.h:178-229). `out` receives lattice node indices, n_cells*(k+1)^dim. */
+int ppf_dealii_cell_nodes(ppf_handle h, long long first_cell, long long n_cells, long long* out);
+
+/* The solution of field f as it stood at the end of the last increment's solves, before the
+ * age rotation (what SolutionOutput writes, problem.cc:505-552). */
+int ppf_download_solution(ppf_handle h, int field, double* host, int ordering);
+
 /* sizes: lattice nodes per component, vector length of field f, cell count */
 long long ppf_n_nodes(ppf_handle h);
 long long ppf_field_length(ppf_handle h, int field);

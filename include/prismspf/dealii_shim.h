@@ -86,6 +86,8 @@ struct Tensor<1, dim, T> {
   static constexpr unsigned int n_independent_components = dim;
   T values[dim];
   PPF_HD Tensor() { for (int i = 0; i < dim; ++i) values[i] = T(0.0); }
+  // from an array of components, e.g. Tensor<1, 2>({200.0, 200.0})
+  PPF_HD explicit Tensor(const T (&init)[dim]) { for (int i = 0; i < dim; ++i) values[i] = init[i]; }
   PPF_HD T& operator[](unsigned int i) { return values[i]; }
   PPF_HD const T& operator[](unsigned int i) const { return values[i]; }
   PPF_HD Tensor& operator+=(const Tensor& o) { for (int i = 0; i < dim; ++i) values[i] += o.values[i]; return *this; }
@@ -139,6 +141,9 @@ template <typename N> PPF_HD dealii::VectorizedArray<N> pow(dealii::VectorizedAr
 template <typename N> PPF_HD dealii::VectorizedArray<N> pow(dealii::VectorizedArray<N> x, dealii::VectorizedArray<N> p) { return ::pow(x.v, p.v); }
 template <typename N> PPF_HD dealii::VectorizedArray<N> min(dealii::VectorizedArray<N> a, dealii::VectorizedArray<N> b) { return a.v < b.v ? a.v : b.v; }
 template <typename N> PPF_HD dealii::VectorizedArray<N> max(dealii::VectorizedArray<N> a, dealii::VectorizedArray<N> b) { return a.v > b.v ? a.v : b.v; }
+template <typename N> PPF_HD dealii::VectorizedArray<N> atan(dealii::VectorizedArray<N> x) { return ::atan(x.v); }
+template <typename N> PPF_HD dealii::VectorizedArray<N> atan2(dealii::VectorizedArray<N> y, dealii::VectorizedArray<N> x) { return ::atan2(y.v, x.v); }
+template <typename N> PPF_HD dealii::VectorizedArray<N> erf(dealii::VectorizedArray<N> x) { return ::erf(x.v); }
 }  // namespace std
 
 namespace dealii {
@@ -221,5 +226,20 @@ struct Point : public Tensor<1, dim, T> {
   PPF_HD Point(T x, T y, T z) { this->values[0] = x; if (dim > 1) this->values[1] = y; if (dim > 2) this->values[2] = z; }
   PPF_HD T distance(const Point& o) const { return (Tensor<1, dim, T>(*this) - Tensor<1, dim, T>(o)).norm(); }
 };
+
+// ----------------------------------------------------------------------------------------
+// EvaluationFlags (the dependency flags of a solve block; host side)
+// ----------------------------------------------------------------------------------------
+namespace EvaluationFlags {
+enum EvaluationFlags { nothing = 0, values = 1, gradients = 2, hessians = 4 };
+inline constexpr EvaluationFlags operator|(EvaluationFlags a, EvaluationFlags b) {
+  return static_cast<EvaluationFlags>(static_cast<int>(a) | static_cast<int>(b));
+}
+inline constexpr EvaluationFlags operator&(EvaluationFlags a, EvaluationFlags b) {
+  return static_cast<EvaluationFlags>(static_cast<int>(a) & static_cast<int>(b));
+}
+inline EvaluationFlags& operator|=(EvaluationFlags& a, EvaluationFlags b) { return a = a | b; }
+inline EvaluationFlags& operator&=(EvaluationFlags& a, EvaluationFlags b) { return a = a & b; }
+}  // namespace EvaluationFlags
 
 }  // namespace dealii

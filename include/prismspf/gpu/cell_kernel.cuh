@@ -30,6 +30,13 @@
 
 #include <prismspf/core/field_container.h>
 
+// prismspf/core/pde_operator_base.h re-declares the callback names as macros for user
+// classes; the kernel calls them by their plain names.
+#pragma push_macro("compute_rhs")
+#pragma push_macro("compute_lhs")
+#undef compute_rhs
+#undef compute_lhs
+
 namespace ppf {
 
 using prismspf::FieldContainer;
@@ -109,7 +116,7 @@ __device__ __forceinline__ number integrate_row(const pg::CellTables<dim, degree
 
 template <class PDE, int dim, int degree, int MODE, typename number>
 __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
-    cell_kernel(const CellLaunch P, const PDE pde) {
+    cell_kernel(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde) {
   using S = CellShape<dim, degree>;
   using Tab = pg::CellTables<dim, degree, number>;
   constexpr int n = S::n, nq = S::nq, cpb = S::cpb, k = degree;
@@ -292,3 +299,6 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
 }
 
 }  // namespace ppf
+
+#pragma pop_macro("compute_lhs")
+#pragma pop_macro("compute_rhs")

@@ -1,0 +1,45 @@
+// Host-side launcher of cell_kernel<PDE, dim, degree, mode, number>: opts in to the dynamic
+// shared memory the launch needs, sizes a persistent grid of (SM count x resident blocks per
+// SM) blocks capped at the number of cell tiles, and launches on the given stream.
+//
+// Used by the library's built-in operators and by prismspf/core/problem.h for a user's
+// CustomPDE, so both sides launch the kernel the same way. `obj` points to the host bytes of
+// the operator object; they are passed to the kernel by value.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <prismspf/gpu/cell_kernel.cuh>
+
+namespace ppf {
+
+template <class PDE, int dim, int degree, int mode, typename number>
+cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
+  using S = CellShape<dim, degree>;
+  auto kern = cell_kernel<PDE, dim, degree, mode, number>;
+  static size_t attr_smem = 0;
+  static int occ = 0;
+  static int sms = 0;
+  if (smem > attr_smem) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_smem = smem;
+    occ = 0;
+  }
+  if (occ == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  const long long ntiles = (P.ncells + S::cpb - 1) / S::cpb;
+  long long grid = (long long)sms * occ;
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj));
+  return cudaGetLastError();
+}
+
+}  // namespace ppf

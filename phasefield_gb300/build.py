@@ -44,7 +44,7 @@ def _needs_rebuild() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + list((ROOT / "include").rglob("*.h")) + [Path(__file__)]
+    deps = list(CSRC.glob("*")) + list((ROOT / "include").rglob("*.h")) + list((ROOT / "include").rglob("*.cuh")) + [Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps if p.is_file())
 
 

@@ -41,6 +41,8 @@ EXPORTED = [
     "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_run", "ppf_ensemble_autotune",
     "ppf_ensemble_synchronize", "ppf_ensemble_set_stream",
     "ppf_adjoint_forward", "ppf_adjoint_backward", "ppf_tangent_linear", "ppf_checkpoint_schedule_cost",
+    # operators compiled by the caller (bound from C++ by prismspf/core/problem.h)
+    "ppf_create_custom", "ppf_set_dirichlet_values", "ppf_dealii_cell_nodes", "ppf_download_solution",
 ]
 
 

@@ -28,6 +28,7 @@ struct FieldState {
   double* dvals = nullptr;
   std::vector<int> h_cmap;
   std::vector<double> h_dvals;
+  std::vector<long long> h_drow;  // position (component-major lattice index) of Dirichlet row j
   bool constrained = false;
   ppf_field_desc desc;
 };
@@ -117,6 +118,9 @@ struct ppf_handle_s {
   std::vector<ppf::FieldState> fields;
   std::vector<ppf::BlockState> blocks;
   const ppf::ModelOps* model = nullptr;
+  ppf::ModelOps custom_ops{};              // operator compiled by the caller (ppf_create_custom)
+  std::string custom_name;
+  ppf_cell_launch_fn custom_launch = nullptr;
   std::vector<unsigned char> model_obj;
   std::vector<unsigned char> model_obj_f32;  // FP32 object (operator sets with an FP32 LHS)
   std::vector<double> constants;

@@ -990,6 +990,8 @@ int ppf_set_linear_params(ppf_handle h, int b, const ppf_linear_params* p) {
     return fail(h, PPF_ERR_ARG, "invalid linear solver parameters");
   LinearState& L = h->blocks[b].lin;
   if (L.initialized) return fail(h, PPF_ERR_ARG, "linear parameters are fixed after the first solve");
+  if (p->mixed_precision && h->model_obj_f32.empty())
+    return fail(h, PPF_ERR_UNSUPPORTED, "mixed precision needs an FP32 instance of the operator");
   L.params = *p;
   L.params_set = true;
   return PPF_OK;

@@ -5,38 +5,15 @@
 #include <cstring>
 #include <string>
 
+#include <prismspf/gpu/launch.cuh>
+
 #include "runtime.h"
 
 namespace ppf {
 
 template <template <unsigned int, unsigned int, typename> class M, int dim, int degree, int mode, typename number>
 cudaError_t launch_one(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
-  using PDE = M<dim, degree, number>;
-  using S = CellShape<dim, degree>;
-  auto kern = cell_kernel<PDE, dim, degree, mode, number>;
-  static size_t attr_smem = 0;
-  static int occ = 0;
-  static int sms = 0;
-  if (smem > attr_smem) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_smem = smem;
-    occ = 0;
-  }
-  if (occ == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
-  const long long ntiles = (P.ncells + S::cpb - 1) / S::cpb;
-  long long grid = (long long)sms * occ;
-  if (grid > ntiles) grid = ntiles;
-  if (grid < 1) grid = 1;
-  kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj));
-  return cudaGetLastError();
+  return launch_cell_kernel<M<dim, degree, number>, dim, degree, mode, number>(P, obj, smem, s);
 }
 
 // precision: 0 = FP64, 1 = FP32 (LHS modes only, for mixed-precision smoothing)

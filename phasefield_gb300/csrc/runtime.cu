@@ -309,6 +309,7 @@ static void build_constraints(ppf_handle h, FieldState& F, const ppf_field_desc&
   const long long N = h->N;
   F.h_cmap.resize(F.len);
   F.h_dvals.clear();
+  F.h_drow.clear();
   bool any = false;
   for (int c = 0; c < F.ncomp; ++c)
     for (long long i = 0; i < N; ++i) {
@@ -324,6 +325,7 @@ static void build_constraints(ppf_handle h, FieldState& F, const ppf_field_desc&
         if (!node_on_boundary(h, i, b) || F.h_cmap[gi] != (int)gi) continue;
         F.h_cmap[gi] = -1 - (int)F.h_dvals.size();
         F.h_dvals.push_back(fd.dirichlet_value[c][b]);
+        F.h_drow.push_back(gi);
         any = true;
       }
     }
@@ -367,21 +369,8 @@ static void build_invm(ppf_handle h) {
   cudaMemcpy(h->d_invm_sqrt, isq.data(), sizeof(double) * h->N, cudaMemcpyHostToDevice);
 }
 
-// deal.II distribute_dofs order as a map dealii index -> lattice index (component-major).
-// Cells: coarse cells lexicographic, fine cells of each coarse cell in Morton order with the
-// x bit lowest at every level (refine_global child order). Per cell the geometric objects
-// come in deal.II order: vertices (x + 2y + 4z), lines (2-D: x=0, x=1, y=0, y=1; 3-D: those
-// four at z=0, again at z=1, then the four z-lines at (0,0),(1,0),(0,1),(1,1)), faces
-// (x=0, x=1, y=0, y=1, z=0, z=1), interior. An object is numbered the first time a cell
-// reaches it; a vector element numbers all components of an object one after the other.
-static std::vector<long long> dealii_dof_map(const ppf_handle h, int ncomp) {
-  const int dim = h->dim, k = h->k;
-  const int r = h->mesh.global_refinement;
-  const long long N = h->N;
-  std::vector<long long> map;
-  map.reserve(N * ncomp);
-  std::vector<char> seen(N, 0);
-  // object list in cell-local lattice offsets
+// FE_Q's geometric objects of one cell in deal.II order, as cell-local lattice offsets.
+static std::vector<std::vector<std::array<int, 3>>> dealii_cell_objects(int dim, int k) {
   std::vector<std::vector<std::array<int, 3>>> objs;
   const int nv = 1 << dim;
   for (int v = 0; v < nv; ++v) objs.push_back({{(v & 1) * k, ((v >> 1) & 1) * k, ((v >> 2) & 1) * k}});
@@ -434,6 +423,15 @@ static std::vector<long long> dealii_dof_map(const ppf_handle h, int ncomp) {
         for (int a = 1; a < k; ++a) o.push_back({a, b, dim == 3 ? c : 0});
     objs.push_back(o);
   }
+  return objs;
+}
+
+// Visits the active cells in deal.II order: coarse cells lexicographic, fine cells of each
+// coarse cell in Morton order with the x bit lowest at every level (refine_global child order).
+template <class Fn>
+static void for_each_dealii_cell(const ppf_handle h, Fn&& fn) {
+  const int dim = h->dim;
+  const int r = h->mesh.global_refinement;
   const long long per_coarse = 1LL << (r * dim);
   const int sub[3] = {h->mesh.subdivisions[0], dim > 1 ? h->mesh.subdivisions[1] : 1,
                       dim > 2 ? h->mesh.subdivisions[2] : 1};
@@ -444,22 +442,37 @@ static std::vector<long long> dealii_dof_map(const ppf_handle h, int ncomp) {
           long long f[3] = {0, 0, 0};
           for (int lvl = 0; lvl < r; ++lvl)
             for (int d = 0; d < dim; ++d) f[d] |= ((m >> (lvl * dim + d)) & 1LL) << lvl;
-          const long long cx = (long long)CX * (1LL << r) + f[0];
-          const long long cy = (long long)CY * (1LL << r) + f[1];
-          const long long cz = (long long)CZ * (1LL << r) + f[2];
-          for (auto& o : objs) {
-            if (o.empty()) continue;
-            const auto& p0 = o[0];
-            const long long n0 = ((cz * k + p0[2]) * h->nn[1] + (cy * k + p0[1])) * h->nn[0] + (cx * k + p0[0]);
-            if (seen[n0]) continue;
-            for (int c = 0; c < ncomp; ++c)
-              for (auto& p : o) {
-                const long long nd = ((cz * k + p[2]) * h->nn[1] + (cy * k + p[1])) * h->nn[0] + (cx * k + p[0]);
-                seen[nd] = 1;
-                map.push_back(c * N + nd);
-              }
-          }
+          fn((long long)CX * (1LL << r) + f[0], (long long)CY * (1LL << r) + f[1], (long long)CZ * (1LL << r) + f[2]);
         }
+}
+
+// deal.II distribute_dofs order as a map dealii index -> lattice index (component-major).
+// Per cell the geometric objects come in deal.II order: vertices (x + 2y + 4z), lines (2-D:
+// x=0, x=1, y=0, y=1; 3-D: those four at z=0, again at z=1, then the four z-lines at (0,0),
+// (1,0),(0,1),(1,1)), faces (x=0, x=1, y=0, y=1, z=0, z=1), interior. An object is numbered
+// the first time a cell reaches it; a vector element numbers all components of an object one
+// after the other.
+static std::vector<long long> dealii_dof_map(const ppf_handle h, int ncomp) {
+  const int k = h->k;
+  const long long N = h->N;
+  std::vector<long long> map;
+  map.reserve(N * ncomp);
+  std::vector<char> seen(N, 0);
+  const auto objs = dealii_cell_objects(h->dim, k);
+  for_each_dealii_cell(h, [&](long long cx, long long cy, long long cz) {
+    for (auto& o : objs) {
+      if (o.empty()) continue;
+      const auto& p0 = o[0];
+      const long long n0 = ((cz * k + p0[2]) * h->nn[1] + (cy * k + p0[1])) * h->nn[0] + (cx * k + p0[0]);
+      if (seen[n0]) continue;
+      for (int c = 0; c < ncomp; ++c)
+        for (auto& p : o) {
+          const long long nd = ((cz * k + p[2]) * h->nn[1] + (cy * k + p[1])) * h->nn[0] + (cx * k + p[0]);
+          seen[nd] = 1;
+          map.push_back(c * N + nd);
+        }
+    }
+  });
   return map;
 }
 
@@ -579,7 +592,9 @@ int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L
     e1 = h->ev_pool[h->ev_used++];
     PPF_CUDA(h, cudaEventRecord(e0, h->stream));
   }
-  cudaError_t e = h->model->launch(h->dim, h->k, mode, precision, L, obj, smem, h->stream);
+  cudaError_t e = h->custom_launch
+                      ? (cudaError_t)h->custom_launch(h->dim, h->k, mode, precision, &L, obj, smem, (void*)h->stream)
+                      : h->model->launch(h->dim, h->k, mode, precision, L, obj, smem, h->stream);
   if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("cell kernel launch: ") + cudaGetErrorString(e));
   if (h->timing) PPF_CUDA(h, cudaEventRecord(e1, h->stream));
   h->cell_launches++;
@@ -687,7 +702,7 @@ extern "C" {
 
 static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields, const ppf_block_desc* blocks,
                int n_blocks, const char* model, const double* constants, int n_constants, double dt,
-               std::unique_ptr<ppf_handle_s>& h, std::string& cerr) {
+               const ppf_model_desc* custom, std::unique_ptr<ppf_handle_s>& h, std::string& cerr) {
   if (!mesh || mesh->dim < 2 || mesh->dim > 3 || mesh->degree < 1 || mesh->degree > 4) {
     cerr = "mesh: dim must be 2 or 3 and degree 1..4";
     return PPF_ERR_ARG;
@@ -714,24 +729,47 @@ static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, 
     h->N *= h->nn[d];
   }
   if (h->N * 3 >= (1LL << 31)) return PPF_ERR_UNSUPPORTED;  // int32 constraint maps
-  h->model = find_model(model);
-  if (!h->model) {
-    cerr = std::string("unknown model: ") + (model ? model : "(null)");
-    return PPF_ERR_ARG;
-  }
   h->dt = dt;
   h->timer = prismspf::SimulationTimer(dt, 0.0);
-  h->model_obj.resize(8192);
-  std::string merr;
-  const size_t osz = h->model->make_object(h->dim, h->k, 0, constants, n_constants, h->model_obj.data(),
-                                           h->model_obj.size(), &merr);
-  if (!osz) {
-    cerr = merr;
-    return PPF_ERR_ARG;
+  if (custom) {
+    if (!custom->launch || !custom->object || custom->object_size == 0) {
+      cerr = "custom operator: launch function and object bytes are required";
+      return PPF_ERR_ARG;
+    }
+    if (custom->cell_launch_size != sizeof(CellLaunch)) {
+      cerr = "custom operator: launch record layout differs from this library (rebuild against its headers)";
+      return PPF_ERR_ARG;
+    }
+    h->custom_name = custom->name ? custom->name : "custom";
+    h->custom_ops.name = h->custom_name.c_str();
+    h->custom_ops.has_lhs = custom->has_lhs != 0;
+    h->custom_launch = custom->launch;
+    h->model = &h->custom_ops;
+    const unsigned char* ob = static_cast<const unsigned char*>(custom->object);
+    h->model_obj.assign(ob, ob + custom->object_size);
+    if (custom->object_f32 && custom->object_f32_size) {
+      const unsigned char* of = static_cast<const unsigned char*>(custom->object_f32);
+      h->model_obj_f32.assign(of, of + custom->object_f32_size);
+    }
+  } else {
+    h->model = find_model(model);
+    if (!h->model) {
+      cerr = std::string("unknown model: ") + (model ? model : "(null)");
+      return PPF_ERR_ARG;
+    }
+    h->model_obj.resize(8192);
+    std::string merr;
+    const size_t osz = h->model->make_object(h->dim, h->k, 0, constants, n_constants, h->model_obj.data(),
+                                             h->model_obj.size(), &merr);
+    if (!osz) {
+      cerr = merr;
+      return PPF_ERR_ARG;
+    }
+    h->model_obj.resize(osz);
+    if (n_constants > 0) h->constants.assign(constants, constants + n_constants);
   }
-  h->model_obj.resize(osz);
-  h->constants.assign(constants, constants + n_constants);
-  if (h->model->has_lhs) {
+  if (!custom && h->model->has_lhs) {
+    std::string merr;
     h->model_obj_f32.resize(8192);
     const size_t o32 = h->model->make_object(h->dim, h->k, 1, constants, n_constants, h->model_obj_f32.data(),
                                              h->model_obj_f32.size(), &merr);
@@ -813,7 +851,25 @@ int ppf_create(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fi
   *out = nullptr;
   std::unique_ptr<ppf_handle_s> h(new ppf_handle_s());
   g_create_error.clear();
-  const int rc = create_impl(mesh, fields, n_fields, blocks, n_blocks, model, constants, n_constants, dt, h, g_create_error);
+  const int rc = create_impl(mesh, fields, n_fields, blocks, n_blocks, model, constants, n_constants, dt, nullptr, h,
+                             g_create_error);
+  if (rc != PPF_OK) {
+    if (g_create_error.empty()) g_create_error = "invalid problem description";
+    ppf_destroy(h.release());
+    return rc;
+  }
+  *out = h.release();
+  return PPF_OK;
+}
+
+int ppf_create_custom(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, int n_fields,
+                      const ppf_block_desc* blocks, int n_blocks, const ppf_model_desc* model, double dt,
+                      ppf_handle* out) {
+  if (!out || !model) return PPF_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<ppf_handle_s> h(new ppf_handle_s());
+  g_create_error.clear();
+  const int rc = create_impl(mesh, fields, n_fields, blocks, n_blocks, nullptr, nullptr, 0, dt, model, h, g_create_error);
   if (rc != PPF_OK) {
     if (g_create_error.empty()) g_create_error = "invalid problem description";
     ppf_destroy(h.release());
@@ -918,6 +974,40 @@ int ppf_download_state(ppf_handle h, int f, int age, double* host, int ordering)
   double* p = state_ptr(h, f, age);
   if (!p) return fail(h, PPF_ERR_ARG, "age not stored for this field");
   return permute_io(h, f, host, p, nullptr, ordering, false);
+}
+
+int ppf_download_solution(ppf_handle h, int f, double* host, int ordering) {
+  if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  FieldState& F = h->fields[f];
+  // the rotation at the end of an increment moved the solution into old_1
+  double* p = (F.n_old > 0 && h->rot_count > 0) ? F.old[0] : F.cur;
+  return permute_io(h, f, host, p, nullptr, ordering, false);
+}
+
+int ppf_set_dirichlet_values(ppf_handle h, int f, const double* values) {
+  if (!h || !values || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  FieldState& F = h->fields[f];
+  if (F.h_dvals.empty()) return PPF_OK;
+  for (size_t j = 0; j < F.h_dvals.size(); ++j) F.h_dvals[j] = values[F.h_drow[j]];
+  PPF_CUDA(h, cudaMemcpyAsync(F.dvals, F.h_dvals.data(), sizeof(double) * F.h_dvals.size(), cudaMemcpyHostToDevice,
+                              h->stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return PPF_OK;
+}
+
+int ppf_dealii_cell_nodes(ppf_handle h, long long first, long long count, long long* out) {
+  if (!h || !out || first < 0 || count < 0 || first + count > h->ncells) return PPF_ERR_ARG;
+  const int k = h->k;
+  const auto objs = dealii_cell_objects(h->dim, k);
+  long long cell = 0, o = 0;
+  const long long last = first + count;
+  for_each_dealii_cell(h, [&](long long cx, long long cy, long long cz) {
+    if (cell >= first && cell < last)
+      for (auto& ob : objs)
+        for (auto& p : ob) out[o++] = ((cz * k + p[2]) * h->nn[1] + (cy * k + p[1])) * h->nn[0] + (cx * k + p[0]);
+    ++cell;
+  });
+  return PPF_OK;
 }
 
 int ppf_apply_constraints(ppf_handle h, int f) {

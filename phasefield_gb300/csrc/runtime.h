@@ -6,7 +6,7 @@
 #include <string>
 #include <vector>
 
-#include "cell_kernel.cuh"
+#include <prismspf/gpu/cell_kernel.cuh>
 
 namespace ppf {
 
