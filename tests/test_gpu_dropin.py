@@ -112,8 +112,8 @@ set Model constant n_grains = 12, INT
     assert rel_l2(to_lattice(v1, wl.mesh, "n"), o.get(0, 1)) < 1e-9
     for f, name in ((1, "mg_n"), (2, "f_tot")):
         assert rel_l2(to_lattice(v1, wl.mesh, name), o.get(f, 0)) < 1e-9, name
-    norms = logged_norms(out, n)
-    assert norms["n"] == pytest.approx(np.linalg.norm(o.get(0, 1)), rel=1e-9)
+    norms = logged_norms(out, n)  # printed with the stream's default 6 significant digits
+    assert norms["n"] == pytest.approx(np.linalg.norm(o.get(0, 1)), rel=1e-5)
 
 
 def test_cahn_hilliard_application_matches_oracle(gpu_lib, tmp_path):
