@@ -2,11 +2,14 @@
 
   python -m phasefield_gb300.profile --workload cahn_hilliard_3d --refine 6 --steps 3
   python -m phasefield_gb300.profile --workload eshelby_3d --refine 5 --mixed 1
+  python -m phasefield_gb300.profile --workload eshelby_3d --refine 6 --preconditioner 1
   python -m phasefield_gb300.profile --workload ensemble --steps 3
 
-Explicit workloads run `steps` increments; eshelby_3d runs one GMG-CG solve (mg_depth =
-refine + 1, Chebyshev degree 4, FP32 smoothing with --mixed 1); ensemble runs `steps` steps of
-the 256-instance Allen-Cahn ensemble. The command exits non-zero if a run reports an error.
+Explicit workloads run `steps` increments; eshelby_3d runs one preconditioned CG solve
+(--preconditioner 2: GMG with --mg-depth levels, default refine + 1; 1: Chebyshev on the fine
+level only; Chebyshev degree 4; FP32 smoothing levels with --mixed 1); ensemble runs `steps`
+steps of the 256-instance Allen-Cahn ensemble. The command exits non-zero if a run reports an
+error.
 """
 from __future__ import annotations
 
@@ -25,6 +28,8 @@ def main(argv=None) -> int:
     ap.add_argument("--refine", type=int, default=None)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--mixed", type=int, default=0)
+    ap.add_argument("--preconditioner", type=int, default=2, choices=[0, 1, 2])
+    ap.add_argument("--mg-depth", type=int, default=None)
     args = ap.parse_args(argv)
     kw = {} if args.refine is None else {"refine": args.refine}
     if args.workload == "ensemble":
@@ -40,12 +45,13 @@ def main(argv=None) -> int:
         wl = W.eshelby_3d(**kw)
         p = wl.make_problem()
         b = p.apply(0, 0, None, scale=0)
-        p.set_linear_params(0, tolerance_type=0, tolerance=1e-10 * float(np.linalg.norm(b)), max_iterations=500,
-                            preconditioner=2, mg_depth=wl.mesh.global_refinement + 1, smoother_degree=4,
+        depth = args.mg_depth if args.mg_depth else wl.mesh.global_refinement + 1
+        p.set_linear_params(0, tolerance_type=0, tolerance=1e-10 * float(np.linalg.norm(b)), max_iterations=2000,
+                            preconditioner=args.preconditioner, mg_depth=depth, smoother_degree=4,
                             mixed_precision=args.mixed)
         its, _ = p.linear_solve(0)
         p.close()
-        print(f"eshelby_3d: GMG-CG {its} iterations ok")
+        print(f"eshelby_3d: preconditioner {args.preconditioner} CG {its} iterations ok")
         return 0
     else:
         wl = getattr(W, args.workload)(**kw)
