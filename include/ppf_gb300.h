@@ -204,6 +204,8 @@ typedef struct {
   double smoothing_range;  /* lambda_max / lambda_min of the Chebyshev interval (default 15) */
   int eig_cg_iterations;   /* CG steps of the largest-eigenvalue estimate (default 10) */
   int mixed_precision;     /* see above (default 0) */
+  int solver_type;         /* 0 cg (SolverCG), 1 bicgstab (SolverBicgstab, for non-symmetric Newton
+                              Jacobians); Linear blocks use cg */
 } ppf_linear_params;
 
 int ppf_default_linear_params(ppf_linear_params* p);
@@ -214,6 +216,19 @@ int ppf_set_linear_params(ppf_handle h, int block, const ppf_linear_params* p);
  * previous homogeneous solution, then constraints. Returns PPF_ERR_NOCONV when max_iterations
  * is reached (the solution is still written, as the reference logs and continues). */
 int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual);
+
+/* NonlinearSolverParameters of Newton block b (solve_parameters.cc:350-470): at most
+ * max_iterations Newton steps (default 100), stop when the scaled residual norm is at most
+ * tolerance * normalisation (default 1e-10), update u += step_length * change (default 1). */
+int ppf_set_newton_params(ppf_handle h, int b, int max_iterations, double tolerance, double step_length);
+
+/* NewtonSolver::solve_impl (newton_solver.h:73-156) for Newton block b over all its fields:
+ * start from old_1, then repeat { apply constraints; R = S compute_rhs; stop if ||R|| is small
+ * enough; solve S compute_lhs(change) = R with the block's linear parameters (cg or bicgstab,
+ * no preconditioner, or Chebyshev for single-field blocks), warm-started from the previous
+ * change; u += step_length * change }. Returns PPF_ERR_NOCONV after max_iterations steps (the
+ * solution is kept, as the reference warns and continues). Outputs may be NULL. */
+int ppf_newton_solve(ppf_handle h, int b, int* newton_iterations, int* linear_iterations, double* residual);
 
 /* Matrix diagonal of the LHS of block b by unit probes, scaled by invM^1/2 when the
  * tolerance type is not AbsoluteResidual, zero entries set to one

@@ -21,7 +21,8 @@
 //     problem.cc:505-552);
 //   * a non-finite solution writes the output of that increment and throws ExcNaN.
 // Not carried over: adaptive refinement (runs on the uniform mesh), nucleation, checkpoints,
-// initial conditions from files, pre/post_solve_block hooks, Newton blocks, user stop.
+// initial conditions from files, pre/post_solve_block hooks, user stop. Newton blocks run
+// with cg or bicgstab (no preconditioner, or Chebyshev for single-field blocks).
 #pragma once
 
 #include <cmath>
@@ -285,8 +286,6 @@ class Problem {
     for (size_t b = 0; b < solve_blocks.size(); ++b) {
       const SolveBlock& sb = solve_blocks[b];
       sb.validate();
-      if (sb.solve_type == SolveType::Newton)
-        throw std::invalid_argument("Newton solve blocks are not supported by this engine");
       std::memset(&bd[b], 0, sizeof(ppf_block_desc));
       bd[b].id = sb.id;
       bd[b].solve_type = (int)sb.solve_type;
@@ -304,9 +303,10 @@ class Problem {
           for (int age = 0; age < PPF_NAGE; ++age)
             (deps == &sb.dependencies_rhs ? bd[b].dep_rhs : bd[b].dep_lhs)[f][age] = detail::age_flags(d, age);
         }
-      any_linear |= sb.solve_type == SolveType::Linear;
+      any_linear |= sb.solve_type == SolveType::Linear || sb.solve_type == SolveType::Newton;
     }
-    if (any_linear && !has_lhs) throw std::invalid_argument("a Linear solve block needs compute_lhs in the operator");
+    if (any_linear && !has_lhs)
+      throw std::invalid_argument("a Linear or Newton solve block needs compute_lhs in the operator");
 
     const SimulationTimer t0(user_inputs->temporal_discretization.dt, user_inputs->temporal_discretization.initial_time);
     ppf_model_desc md{};
@@ -325,13 +325,16 @@ class Problem {
     if (user_inputs->temporal_discretization.initial_time != 0.0)
       check(ppf_set_time(handle, 0, user_inputs->temporal_discretization.initial_time), "start time");
 
-    // linear solver parameters (linear_solver.h:220-402)
+    // linear (and Newton) solver parameters (linear_solver.h:220-402, newton_solver.h:73-156)
     for (size_t b = 0; b < solve_blocks.size(); ++b) {
-      if (solve_blocks[b].solve_type != SolveType::Linear) continue;
+      const SolveType st = solve_blocks[b].solve_type;
+      if (st != SolveType::Linear && st != SolveType::Newton) continue;
       const LinearSolverParameters& L = solve_blocks[b].linear_solver_parameters;
-      if (L.solver_type != "cg") throw std::invalid_argument("only the cg linear solver is supported");
       ppf_linear_params p;
       ppf_default_linear_params(&p);
+      if (L.solver_type == "cg") p.solver_type = 0;
+      else if (L.solver_type == "bicgstab" && st == SolveType::Newton) p.solver_type = 1;
+      else throw std::invalid_argument("linear solver type " + L.solver_type + " is not supported for this block");
       p.tolerance_type = (int)L.tolerance_type;
       p.tolerance = L.tolerance;
       p.max_iterations = (int)L.max_iterations;
@@ -341,6 +344,11 @@ class Problem {
       p.smoothing_range = L.chebyshev_parameters.smoothing_range;
       p.eig_cg_iterations = (int)L.chebyshev_parameters.eig_cg_n_iterations;
       check(ppf_set_linear_params(handle, (int)b, &p), "linear solver parameters");
+      if (st == SolveType::Newton) {
+        const NonlinearSolverParameters& N = solve_blocks[b].nonlinear_solver_parameters;
+        check(ppf_set_newton_params(handle, (int)b, (int)N.max_iterations, N.tolerance_value, N.step_length),
+              "Newton solver parameters");
+      }
     }
 
     update_dirichlet(0);

@@ -366,6 +366,14 @@ struct LinParams {
   int degree = 5;
   double range = 15.0;
   int eig_its = 10;
+  int solver = 0;            // 0 cg (SolverCG), 1 bicgstab (SolverBicgstab)
+};
+
+// NonlinearSolverParameters (src/user_inputs/solve_parameters.cc:350-470)
+struct NewtonParams {
+  int max_its = 100;
+  double tol = 1e-10;
+  double step = 1.0;
 };
 
 struct OLevel {
@@ -390,6 +398,12 @@ struct Block {
   std::vector<OLevel> levels;
   int last_its = 0;
   double last_res = 0.0;
+  // Newton solves
+  NewtonParams newton;
+  std::vector<double> newton_update;  // the "change" vector, kept between solves
+  int last_newton_its = 0;
+  int last_newton_lin_its = 0;
+  double last_newton_res = 0.0;
 };
 
 struct Model;
@@ -468,6 +482,56 @@ static void cb_cahn_hilliard(const Problem& P, QData& q, int block_id, bool) {
     for (int d = 0; d < dim; ++d) q.set_grad(1, 0, d, KcV * q.g(0, AGE_CURRENT, 0, d));
   } else if (block_id == 2) {
     double c = q.v(0, AGE_CURRENT);
+    double g2 = 0;
+    for (int d = 0; d < dim; ++d) g2 += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
+    q.set_value(2, 0, c * c * c * c - 2.0 * c * c * c + c * c + 0.5 * KcV * g2);
+  }
+}
+
+// allen_cahn/implicit/custom_pde.h:70-125 (Newton block 1, post-processing block 2).
+// params: m_well, kappa. fields n(0), mg_n(1), f_tot(2)
+static void cb_allen_cahn_implicit(const Problem& P, QData& q, int block_id, bool lhs) {
+  const double m_well = P.params[0], kappa = P.params[1], dt = P.dt;
+  const int dim = q.dim;
+  if (block_id == 1 && !lhs) {
+    const double n = q.v(0, AGE_CURRENT), n_old = q.v(0, AGE_OLD1);
+    const double f_well = 4.0 * n * (n - 1.0) * (n - 0.5);
+    q.set_value(0, 0, n_old - n - dt * m_well * f_well);
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, -dt * kappa * m_well * q.g(0, AGE_CURRENT, 0, d));
+  } else if (block_id == 1 && lhs) {
+    const double n = q.v(0, AGE_CURRENT), dn = q.v(0, AGE_SRC);
+    const double df_well = 12.0 * n * (n - 1.0) + 2.0;
+    q.set_value(0, 0, dn * (1.0 + dt * m_well * df_well));
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, dt * kappa * m_well * q.g(0, AGE_SRC, 0, d));
+  } else if (block_id == 2 && !lhs) {
+    const double n = q.v(0, AGE_CURRENT);
+    double g2 = 0;
+    for (int d = 0; d < dim; ++d) g2 += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
+    q.set_value(1, 0, std::sqrt(g2));
+    q.set_value(2, 0, n * n * n * n - 2.0 * n * n * n + n * n + 0.5 * kappa * g2);
+  }
+}
+
+// cahn_hilliard/implicit/custom_pde.h:90-160 (Newton block 0 over c and mu, post-processing
+// block 2). params: McV, KcV, WcV. fields c(0), mu(1), f_tot(2)
+static void cb_cahn_hilliard_implicit(const Problem& P, QData& q, int block_id, bool lhs) {
+  const double McV = P.params[0], KcV = P.params[1], WcV = P.params[2], dt = P.dt;
+  const int dim = q.dim;
+  if (block_id == 0 && !lhs) {
+    const double c = q.v(0, AGE_CURRENT), mu = q.v(1, AGE_CURRENT), c_old = q.v(0, AGE_OLD1);
+    q.set_value(0, 0, c_old - c);
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, -(dt * McV * q.g(1, AGE_CURRENT, 0, d)));
+    q.set_value(1, 0, mu - WcV * c * (c - 1.0) * (c - 0.5));
+    for (int d = 0; d < dim; ++d) q.set_grad(1, 0, d, -(KcV * q.g(0, AGE_CURRENT, 0, d)));
+  } else if (block_id == 0 && lhs) {
+    const double c = q.v(0, AGE_CURRENT), dc = q.v(0, AGE_SRC), dmu = q.v(1, AGE_SRC);
+    q.set_value(0, 0, dc);
+    for (int d = 0; d < dim; ++d) q.set_grad(0, 0, d, dt * McV * q.g(1, AGE_SRC, 0, d));
+    const double j_mu_c = -WcV * (0.5 + 3.0 * (c * (c - 1.0))) * dc;
+    q.set_value(1, 0, -j_mu_c - dmu);
+    for (int d = 0; d < dim; ++d) q.set_grad(1, 0, d, KcV * q.g(0, AGE_SRC, 0, d));
+  } else if (block_id == 2 && !lhs) {
+    const double c = q.v(0, AGE_CURRENT);
     double g2 = 0;
     for (int d = 0; d < dim; ++d) g2 += q.g(0, AGE_CURRENT, 0, d) * q.g(0, AGE_CURRENT, 0, d);
     q.set_value(2, 0, c * c * c * c - 2.0 * c * c * c + c * c + 0.5 * KcV * g2);
@@ -593,6 +657,8 @@ static Callback callback_for(int model) {
     case ORC_MODEL_CAHN_HILLIARD: return cb_cahn_hilliard;
     case ORC_MODEL_ESHELBY: return cb_eshelby;
     case ORC_MODEL_COUPLED_ACCH: return cb_coupled;
+    case ORC_MODEL_ALLEN_CAHN_IMPLICIT: return cb_allen_cahn_implicit;
+    case ORC_MODEL_CAHN_HILLIARD_IMPLICIT: return cb_cahn_hilliard_implicit;
     default: return nullptr;
   }
 }
@@ -1264,14 +1330,16 @@ static void init_linear(Problem& P, Block& B) {
   B.lin_init = true;
 }
 
-static double normalization(const Problem& P, const LinParams& p) {
+// LinearSolver::normalization_value (linear_solver.h:414-427)
+static double normalization(const Problem& P, const LinParams& p, int n_fields = 1) {
   double v = 1.0;
   if (p.tol_type == 1 || p.tol_type == 3) {
     double vol = 1.0;
     for (int d = 0; d < P.m.dim; ++d) vol *= P.m.len[d];
     v *= std::sqrt(vol);
   }
-  return v;  // one field: sqrt(n_fields) = 1
+  if (p.tol_type == 1 || p.tol_type == 2) v *= std::sqrt((double)n_fields);
+  return v;
 }
 
 // LinearSolver::solve_impl (linear_solver.h:305-345)
@@ -1342,6 +1410,161 @@ static int linear_solve(Problem& P, Block& B) {
   for (size_t i = 0; i < n; ++i) F.cur[i] = x[i] + g[i];
   distribute(F.cons, F.cur.data());
   return conv ? 0 : 4;
+}
+
+// ---------------------------------------------------------------------------------------
+// Newton solves over all fields of a block (NewtonSolver::solve_impl, newton_solver.h:73-156,
+// with LinearSolver::do_linear_solve, linear_solver.h:348-402). Block vectors concatenate the
+// block's fields in block order.
+// ---------------------------------------------------------------------------------------
+static std::vector<size_t> block_offsets(const Problem& P, const Block& B) {
+  std::vector<size_t> off{0};
+  for (int f : B.fields) off.push_back(off.back() + P.fields[f].cur.size());
+  return off;
+}
+
+// dst = S op(src) over the block fields; which 0: compute_rhs (src unused), 1: compute_lhs
+static void block_op(Problem& P, const Block& B, int which, const double* src, double* dst) {
+  const auto off = block_offsets(P, B);
+  std::vector<const double*> s;
+  std::vector<double*> d;
+  std::vector<const Constraints*> c;
+  for (size_t i = 0; i < B.fields.size(); ++i) {
+    Field& F = P.fields[B.fields[i]];
+    s.push_back(src ? src + off[i] : nullptr);
+    std::fill(dst + off[i], dst + off[i + 1], 0.0);
+    d.push_back(dst + off[i]);
+    c.push_back(&F.cons);
+  }
+  cell_loop(P, B, which == 1, s, d, c, callback_for(P.model));
+  if (scaled(B.lin))
+    for (size_t i = 0; i < B.fields.size(); ++i) {
+      Field& F = P.fields[B.fields[i]];
+      for (size_t j = 0; j < off[i + 1] - off[i]; ++j) dst[off[i] + j] *= P.invm_sqrt[F.rank][j];
+    }
+}
+
+// Krylov solve of S A x = b (SolverCG or SolverBicgstab) from the initial guess in x;
+// preconditioner: identity, or for a single-field block the Chebyshev smoother of the fine
+// level. Returns the number of iterations; *conv tells whether the tolerance was reached.
+static int block_krylov(Problem& P, Block& B, const std::vector<double>& b, std::vector<double>& x, double tol,
+                        bool* conv, double* final_res) {
+  const size_t n = b.size();
+  auto A = [&](const std::vector<double>& v, std::vector<double>& out) { block_op(P, B, 1, v.data(), out.data()); };
+  auto M = [&](const std::vector<double>& rr, std::vector<double>& zz) {
+    if (B.lin.precond == 0) { zz = rr; return; }
+    OLevel& Lf = B.levels.back();
+    Lf.b = rr;
+    chebyshev(Lf, B, true);
+    zz = Lf.x;
+  };
+  std::vector<double> r(n), q(n);
+  A(x, q);
+  for (size_t i = 0; i < n; ++i) r[i] = b[i] - q[i];
+  double res = std::sqrt(dotp(r, r));
+  int it = 0;
+  *conv = res < tol;
+  if (!*conv && B.lin.solver == 0) {
+    std::vector<double> z(n), p(n);
+    M(r, z);
+    p = z;
+    double rz = dotp(r, z);
+    while (it < B.lin.max_its) {
+      A(p, q);
+      const double alpha = rz / dotp(p, q);
+      for (size_t i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
+      ++it;
+      res = std::sqrt(dotp(r, r));
+      if (res < tol) { *conv = true; break; }
+      M(r, z);
+      const double rzn = dotp(r, z);
+      const double beta = rzn / rz;
+      rz = rzn;
+      for (size_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    }
+  } else if (!*conv) {
+    // BiCGStab (van der Vorst), right-preconditioned, with the half-step convergence check
+    std::vector<double> rbar = r, p(n, 0.0), v(n, 0.0), y(n), s(n), zz(n), t(n);
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    while (it < B.lin.max_its) {
+      const double rho_new = dotp(rbar, r);
+      if (rho_new == 0.0 || omega == 0.0) break;  // breakdown
+      const double beta = (rho_new / rho) * (alpha / omega);
+      rho = rho_new;
+      for (size_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+      M(p, y);
+      A(y, v);
+      const double sigma = dotp(rbar, v);
+      if (sigma == 0.0) break;
+      alpha = rho / sigma;
+      for (size_t i = 0; i < n; ++i) s[i] = r[i] - alpha * v[i];
+      ++it;
+      const double sres = std::sqrt(dotp(s, s));
+      if (sres < tol) {
+        for (size_t i = 0; i < n; ++i) x[i] += alpha * y[i];
+        res = sres;
+        *conv = true;
+        break;
+      }
+      M(s, zz);
+      A(zz, t);
+      const double tt = dotp(t, t);
+      omega = tt > 0.0 ? dotp(t, s) / tt : 0.0;
+      for (size_t i = 0; i < n; ++i) {
+        x[i] += alpha * y[i] + omega * zz[i];
+        r[i] = s[i] - omega * t[i];
+      }
+      res = std::sqrt(dotp(r, r));
+      if (res < tol) { *conv = true; break; }
+    }
+  }
+  *final_res = res;
+  return it;
+}
+
+static int newton_solve(Problem& P, Block& B) {
+  const int nbf = (int)B.fields.size();
+  if (B.lin.precond == 2) return 6;               // GMG levels would need the current solution
+  if (B.lin.precond == 1 && nbf != 1) return 6;   // Chebyshev: single-field blocks
+  if (B.lin.precond == 1 && !B.lin_init) init_linear(P, B);
+  const auto off = block_offsets(P, B);
+  const size_t n = off.back();
+  if (B.newton_update.size() != n) B.newton_update.assign(n, 0.0);
+  // start from the previous solution (old_1 where the field keeps one)
+  for (int f : B.fields) {
+    Field& F = P.fields[f];
+    if (F.n_old > 0) F.cur = F.old[0];
+  }
+  const double norm = normalization(P, B.lin, nbf);
+  const double tol = B.newton.tol * norm;
+  const double lin_tol = B.lin.tol * norm;
+  std::vector<double> R(n);
+  double l2 = -1.0;
+  int iter = 0, lin_total = 0;
+  while (iter < B.newton.max_its) {
+    for (int f : B.fields) distribute(P.fields[f].cons, P.fields[f].cur.data());
+    block_op(P, B, 0, nullptr, R.data());
+    l2 = std::sqrt(dotp(R, R));
+    if (!(l2 > tol)) break;
+    if (B.lin.precond == 1) {  // fine-level diagonal of the current Jacobian
+      OLevel& Lf = B.levels.back();
+      compute_inv_diag(P, B, Lf.inv_diag);
+      Lf.eig_done = false;
+      estimate_eig(Lf, B);
+    }
+    bool lconv = false;
+    double lres = 0.0;
+    lin_total += block_krylov(P, B, R, B.newton_update, lin_tol, &lconv, &lres);
+    for (int i = 0; i < nbf; ++i) {
+      Field& F = P.fields[B.fields[i]];
+      for (size_t j = 0; j < off[i + 1] - off[i]; ++j) F.cur[j] += B.newton.step * B.newton_update[off[i] + j];
+    }
+    ++iter;
+  }
+  B.last_newton_its = iter;
+  B.last_newton_lin_its = lin_total;
+  B.last_newton_res = l2 / norm;
+  return iter >= B.newton.max_its ? 4 : 0;
 }
 
 Problem* make_problem(int dim, int degree, const int* subdiv, const double* lower, const double* size, int refine,
@@ -1526,7 +1749,10 @@ int orc_run(void* h, unsigned n_increments, int output_every) {
         // distributed on it at increment 0
       } else {
         if (B.solve_type == 2) linear_solve(*P, B);
-        else explicit_solve(*P, B);
+        else if (B.solve_type == 3) {
+          const int rc = newton_solve(*P, B);
+          if (rc != 0 && rc != 4) return rc;  // non-convergence is a warning in the reference
+        } else explicit_solve(*P, B);
       }
       if (P->increment == 0) {
         for (int f : B.fields) {
@@ -1589,6 +1815,31 @@ int orc_set_linear_params(void* h, int b, const double* p) {
   L.tol_type = (int)p[0]; L.tol = p[1]; L.max_its = (int)p[2]; L.precond = (int)p[3];
   L.mg_depth = (int)p[4]; L.degree = (int)p[5]; L.range = p[6]; L.eig_its = (int)p[7];
   return 0;
+}
+
+int orc_set_solver_type(void* h, int b, int solver) {
+  ((Problem*)h)->blocks[b].lin.solver = solver;
+  return 0;
+}
+
+int orc_set_newton_params(void* h, int b, int max_its, double tol, double step) {
+  NewtonParams& N = ((Problem*)h)->blocks[b].newton;
+  N.max_its = max_its;
+  N.tol = tol;
+  N.step = step;
+  return 0;
+}
+
+// One Newton solve of block b; its = Newton iterations, lin_its = total Krylov iterations,
+// res = final residual norm / normalization
+int orc_newton_solve(void* h, int b, int* its, int* lin_its, double* res) {
+  auto* P = (Problem*)h;
+  Block& B = P->blocks[b];
+  const int rc = newton_solve(*P, B);
+  if (its) *its = B.last_newton_its;
+  if (lin_its) *lin_its = B.last_newton_lin_its;
+  if (res) *res = B.last_newton_res;
+  return rc;
 }
 
 int orc_linear_solve(void* h, int b, int* its, double* res) {

@@ -6,6 +6,8 @@ enum {
   ORC_MODEL_CAHN_HILLIARD = 2,
   ORC_MODEL_ESHELBY = 3,
   ORC_MODEL_COUPLED_ACCH = 4,
+  ORC_MODEL_ALLEN_CAHN_IMPLICIT = 5,
+  ORC_MODEL_CAHN_HILLIARD_IMPLICIT = 6,
 };
 
 enum {

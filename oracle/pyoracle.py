@@ -18,7 +18,8 @@ HERE = Path(__file__).resolve().parent
 SRC = HERE / "oracle.cc"
 LIB = HERE / "build" / "liboracle.so"
 
-MODEL_IDS = {"allen_cahn": 1, "cahn_hilliard": 2, "eshelby": 3, "coupled_acch": 4}
+MODEL_IDS = {"allen_cahn": 1, "cahn_hilliard": 2, "eshelby": 3, "coupled_acch": 4, "allen_cahn_implicit": 5,
+             "cahn_hilliard_implicit": 6}
 
 
 def build(force: bool = False) -> Path:
@@ -73,6 +74,9 @@ def load() -> C.CDLL:
         lib.orc_set_linear_params.argtypes = [C.c_void_p, C.c_int, dp]
         lib.orc_linear_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), dp]
         lib.orc_diagonal.argtypes = [C.c_void_p, C.c_int, dp]
+        lib.orc_set_solver_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        lib.orc_set_newton_params.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+        lib.orc_newton_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), dp]
         _lib = lib
     return _lib
 
@@ -207,10 +211,21 @@ class Oracle:
         return int(self.lib.orc_run(self.h, n_increments, output_every))
 
     def set_linear_params(self, b: int, tolerance_type=0, tolerance=1e-10, max_iterations=100, preconditioner=0,
-                          mg_depth=1, smoother_degree=5, smoothing_range=15.0, eig_cg_iterations=10, **_):
+                          mg_depth=1, smoother_degree=5, smoothing_range=15.0, eig_cg_iterations=10, solver_type=0,
+                          **_):
         p = np.array([tolerance_type, tolerance, max_iterations, preconditioner, mg_depth, smoother_degree,
                       smoothing_range, eig_cg_iterations], dtype=np.float64)
         self.lib.orc_set_linear_params(self.h, b, _dp(p))
+        self.lib.orc_set_solver_type(self.h, b, int(solver_type))
+
+    def set_newton_params(self, b: int, max_iterations=100, tolerance=1e-10, step_length=1.0):
+        self.lib.orc_set_newton_params(self.h, b, int(max_iterations), float(tolerance), float(step_length))
+
+    def newton_solve(self, b: int):
+        """One Newton solve of block b: (rc, Newton iterations, Krylov iterations, residual)."""
+        its, lin, res = C.c_int(), C.c_int(), C.c_double()
+        rc = self.lib.orc_newton_solve(self.h, b, C.byref(its), C.byref(lin), C.byref(res))
+        return rc, its.value, lin.value, res.value
 
     def linear_solve(self, b: int):
         its, res = C.c_int(), C.c_double()

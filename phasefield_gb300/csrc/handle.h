@@ -99,6 +99,16 @@ struct LinearState {
   int last_iterations = 0;
   double last_residual = 0.0;
   double last_rhs_norm = 0.0;
+  // Newton blocks (NonlinearSolverParameters) and their block-vector work space
+  int newton_max_iterations = 100;
+  double newton_tolerance = 1e-10;
+  double newton_step = 1.0;
+  double* newton_update = nullptr;  // the change vector, kept between solves
+  double* kv[8] = {};               // Krylov work vectors of the block length
+  long long block_len = 0;
+  int last_newton_iterations = 0;
+  int last_newton_linear_iterations = 0;
+  double last_newton_residual = 0.0;
 };
 
 struct BlockState {
@@ -175,6 +185,7 @@ double* state_ptr(ppf_handle h, int f, int age);
 int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L, const void* obj, size_t smem);
 int launch_cell(ppf_handle h, int b, int which, const double* const* src);
 int linear_solve(ppf_handle h, int b);
+int newton_solve(ppf_handle h, int b);
 void free_linear(LinearState& L);
 int explicit_solve_entry(ppf_handle h, int b);
 struct AdjointState;

@@ -755,7 +755,8 @@ static int init_linear(ppf_handle h, int b) {
   return PPF_OK;
 }
 
-static double normalization(ppf_handle h, const LinearState& L) {
+// LinearSolver::normalization_value (linear_solver.h:414-427)
+static double normalization(ppf_handle h, const LinearState& L, int n_fields = 1) {
   double v = 1.0;
   const int t = L.params.tolerance_type;
   if (t == 1 || t == 3) {
@@ -763,7 +764,7 @@ static double normalization(ppf_handle h, const LinearState& L) {
     for (int d = 0; d < h->dim; ++d) vol *= h->mesh.size[d];
     v *= std::sqrt(vol);
   }
-  if (t == 1 || t == 2) v *= 1.0;  // sqrt(number of fields) with one field
+  if (t == 1 || t == 2) v *= std::sqrt((double)n_fields);
   return v;
 }
 
@@ -944,8 +945,223 @@ int linear_solve(ppf_handle h, int b) {
   return PPF_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// Newton solves over all fields of a block (NewtonSolver::solve_impl, newton_solver.h:73-156,
+// with LinearSolver::do_linear_solve, linear_solver.h:348-402). Block vectors concatenate the
+// block's fields in block order on the device.
+// ------------------------------------------------------------------------------------------
+// dst = S op(src) on the block (which 0: compute_rhs, 1: compute_lhs with src read through
+// the homogeneous constraints); constrained rows zero
+static int block_op(ppf_handle h, int b, int which, const double* src, double* dst) {
+  return ppf_apply_device(h, b, which, src, dst, scaled(h->blocks[b].lin) ? 2 : 0);
+}
+
+// Krylov solve of S A x = rhs from the initial guess in x (SolverCG or SolverBicgstab);
+// preconditioner: identity, or the fine-level Chebyshev smoother for a single-field block
+static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, double tol, int* its, bool* conv) {
+  BlockState& B = h->blocks[b];
+  LinearState& L = B.lin;
+  const long long n = L.block_len;
+  double** v = L.kv;
+  auto A = [&](const double* in, double* out) { return block_op(h, b, 1, in, out); };
+  auto M = [&](const double* in, double* out) -> int {
+    if (L.params.preconditioner == 0) {
+      PPF_CUDA(h, cudaMemcpyAsync(out, in, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+      return PPF_OK;
+    }
+    return precondition(h, B, in, out);
+  };
+  double* r = v[0];
+  double* q = v[1];
+  int rc = A(x, q);
+  if (rc) return rc;
+  PPF_CUDA(h, cudaMemcpyAsync(r, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  axpby(h, 0, n, -1.0, q, 1.0, r);
+  double rr;
+  rc = dot(h, L, 0, n, r, r, &rr);
+  if (rc) return rc;
+  double res = std::sqrt(rr);
+  int it = 0;
+  *conv = res < tol;
+  if (!*conv && L.params.solver_type == 0) {
+    double* z = v[2];
+    double* p = v[3];
+    if ((rc = M(r, z))) return rc;
+    PPF_CUDA(h, cudaMemcpyAsync(p, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    double rz;
+    if ((rc = dot(h, L, 0, n, r, z, &rz))) return rc;
+    while (it < L.params.max_iterations) {
+      if ((rc = A(p, q))) return rc;
+      double pq;
+      if ((rc = dot(h, L, 0, n, p, q, &pq))) return rc;
+      const double alpha = rz / pq;
+      cg_update_xr_kernel<<<grid_for(n), 256, 0, h->stream>>>(n, alpha, p, q, x, r);
+      h->all_launches++;
+      ++it;
+      if ((rc = dot(h, L, 0, n, r, r, &rr))) return rc;
+      res = std::sqrt(rr);
+      if (!std::isfinite(res)) return fail(h, PPF_ERR_NAN, "non-finite residual in the linear solve");
+      if (res < tol) {
+        *conv = true;
+        break;
+      }
+      if ((rc = M(r, z))) return rc;
+      double rz_new;
+      if ((rc = dot(h, L, 0, n, r, z, &rz_new))) return rc;
+      const double beta = rz_new / rz;
+      rz = rz_new;
+      axpby(h, 0, n, 1.0, z, beta, p);
+    }
+  } else if (!*conv) {
+    // BiCGStab (van der Vorst), right-preconditioned, with the half-step convergence check
+    double* rbar = v[2];
+    double* p = v[3];
+    double* vv = v[4];
+    double* y = v[5];
+    double* sv = v[6];
+    double* t = v[7];
+    double* zz = q;  // q is free from here on
+    PPF_CUDA(h, cudaMemcpyAsync(rbar, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+    PPF_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * n, h->stream));
+    PPF_CUDA(h, cudaMemsetAsync(vv, 0, sizeof(double) * n, h->stream));
+    double rho = 1.0, alpha = 1.0, omega = 1.0;
+    while (it < L.params.max_iterations) {
+      double rho_new;
+      if ((rc = dot(h, L, 0, n, rbar, r, &rho_new))) return rc;
+      if (rho_new == 0.0 || omega == 0.0) break;  // breakdown
+      const double beta = (rho_new / rho) * (alpha / omega);
+      rho = rho_new;
+      axpby(h, 0, n, -omega, vv, 1.0, p);  // p = p - omega v
+      axpby(h, 0, n, 1.0, r, beta, p);     // p = r + beta p
+      if ((rc = M(p, y))) return rc;
+      if ((rc = A(y, vv))) return rc;
+      double sigma;
+      if ((rc = dot(h, L, 0, n, rbar, vv, &sigma))) return rc;
+      if (sigma == 0.0) break;
+      alpha = rho / sigma;
+      PPF_CUDA(h, cudaMemcpyAsync(sv, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+      axpby(h, 0, n, -alpha, vv, 1.0, sv);  // s = r - alpha v
+      ++it;
+      double ss;
+      if ((rc = dot(h, L, 0, n, sv, sv, &ss))) return rc;
+      if (!std::isfinite(ss)) return fail(h, PPF_ERR_NAN, "non-finite residual in the linear solve");
+      if (std::sqrt(ss) < tol) {
+        axpby(h, 0, n, alpha, y, 1.0, x);
+        res = std::sqrt(ss);
+        *conv = true;
+        break;
+      }
+      if ((rc = M(sv, zz))) return rc;
+      if ((rc = A(zz, t))) return rc;
+      double tt, ts;
+      if ((rc = dot(h, L, 0, n, t, t, &tt))) return rc;
+      if ((rc = dot(h, L, 0, n, t, sv, &ts))) return rc;
+      omega = tt > 0.0 ? ts / tt : 0.0;
+      axpby(h, 0, n, alpha, y, 1.0, x);
+      axpby(h, 0, n, omega, zz, 1.0, x);
+      PPF_CUDA(h, cudaMemcpyAsync(r, sv, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+      axpby(h, 0, n, -omega, t, 1.0, r);  // r = s - omega t
+      if ((rc = dot(h, L, 0, n, r, r, &rr))) return rc;
+      res = std::sqrt(rr);
+      if (res < tol) {
+        *conv = true;
+        break;
+      }
+    }
+  }
+  *its = it;
+  return PPF_OK;
+}
+
+int newton_solve(ppf_handle h, int b) {
+  BlockState& B = h->blocks[b];
+  LinearState& L = B.lin;
+  if (!L.params_set) {
+    ppf_default_linear_params(&L.params);
+    L.params_set = true;
+  }
+  const int nbf = B.desc.n_fields;
+  if (!B.plan[0].valid || !B.plan[1].valid)
+    return fail(h, PPF_ERR_ARG, "Newton block needs compute_rhs and compute_lhs dependencies");
+  if (L.params.preconditioner == 2)
+    return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks: GMG levels would need the current solution on every level");
+  if (L.params.preconditioner == 1 && nbf != 1)
+    return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks: the Chebyshev preconditioner needs a single-field block");
+  if (L.params.preconditioner == 1 && !L.initialized) {
+    int rc = init_linear(h, b);
+    if (rc) return rc;
+  }
+  long long off[PPF_MAX_FIELDS + 1] = {0};
+  for (int i = 0; i < nbf; ++i) off[i + 1] = off[i] + h->fields[B.desc.field_indices[i]].len;
+  const long long n = off[nbf];
+  if (L.block_len != n) {
+    cudaFree(L.newton_update);
+    for (double*& p : L.kv) cudaFree(p);
+    PPF_CUDA(h, cudaMalloc(&L.newton_update, sizeof(double) * n));
+    PPF_CUDA(h, cudaMemset(L.newton_update, 0, sizeof(double) * n));
+    for (double*& p : L.kv) PPF_CUDA(h, cudaMalloc(&p, sizeof(double) * n));
+    cudaFree(L.rhs);  // a Newton block's rhs vector holds its block residual
+    PPF_CUDA(h, cudaMalloc(&L.rhs, sizeof(double) * n));
+    if (!L.partial) PPF_CUDA(h, cudaMalloc(&L.partial, sizeof(double) * 1100));
+    L.block_len = n;
+  }
+  double* R = L.rhs;
+  // start from the previous solution (old_1 where the field keeps one)
+  for (int i = 0; i < nbf; ++i) {
+    FieldState& F = h->fields[B.desc.field_indices[i]];
+    if (F.n_old > 0)
+      PPF_CUDA(h, cudaMemcpyAsync(F.cur, F.old[0], sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  const double norm = normalization(h, L, nbf);
+  const double tol = L.newton_tolerance * norm;
+  const double lin_tol = L.params.tolerance * norm;
+  double l2 = -1.0;
+  int iter = 0, lin_total = 0;
+  while (iter < L.newton_max_iterations) {
+    for (int i = 0; i < nbf; ++i) {
+      int rc = ppf_apply_constraints(h, B.desc.field_indices[i]);
+      if (rc) return rc;
+    }
+    int rc = block_op(h, b, 0, nullptr, R);
+    if (rc) return rc;
+    double rr;
+    if ((rc = dot(h, L, 0, n, R, R, &rr))) return rc;
+    l2 = std::sqrt(rr);
+    if (!std::isfinite(l2)) return fail(h, PPF_ERR_NAN, "non-finite Newton residual");
+    if (!(l2 > tol)) break;
+    if (L.params.preconditioner == 1) {  // fine-level diagonal of the current Jacobian
+      MGLevel& fine = L.levels.back();
+      if ((rc = level_diagonal(h, B, fine))) return rc;
+      fine.eig_done = false;
+      if ((rc = estimate_eigenvalues<double>(h, B, fine))) return rc;
+    }
+    int its = 0;
+    bool conv = false;
+    if ((rc = block_krylov(h, b, R, L.newton_update, lin_tol, &its, &conv))) return rc;
+    lin_total += its;
+    for (int i = 0; i < nbf; ++i) {
+      FieldState& F = h->fields[B.desc.field_indices[i]];
+      axpby(h, 0, F.len, L.newton_step, L.newton_update + off[i], 1.0, F.cur);
+    }
+    ++iter;
+  }
+  L.last_newton_iterations = iter;
+  L.last_newton_linear_iterations = lin_total;
+  L.last_newton_residual = l2 / norm;
+  int rc = check_err(h);
+  if (rc) return rc;
+  if (iter >= L.newton_max_iterations) return fail(h, PPF_ERR_NOCONV, "Newton solver did not converge");
+  return PPF_OK;
+}
+
 void free_linear(LinearState& L) {
-  for (double* p : {L.rhs, L.g, L.x_hom, L.r, L.p, L.q, L.z, L.inv_diag, L.partial}) cudaFree(p);
+  for (double* p : {L.rhs, L.g, L.x_hom, L.r, L.p, L.q, L.z, L.inv_diag, L.partial, L.newton_update}) cudaFree(p);
+  for (double*& p : L.kv) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  L.newton_update = nullptr;
+  L.block_len = 0;
   for (auto& lv : L.levels) {
     cudaFree(lv.cmap);
     for (void* p : {lv.invm_sqrt, lv.inv_diag, lv.tables, lv.acc, lv.x, lv.b, lv.r, lv.w0, lv.w1, lv.t0, lv.t1, lv.cvt})
@@ -980,13 +1196,15 @@ int ppf_default_linear_params(ppf_linear_params* p) {
   p->smoothing_range = 15.0;
   p->eig_cg_iterations = 10;
   p->mixed_precision = 0;
+  p->solver_type = 0;
   return PPF_OK;
 }
 
 int ppf_set_linear_params(ppf_handle h, int b, const ppf_linear_params* p) {
   if (!h || !p || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
   if (p->preconditioner < 0 || p->preconditioner > 2 || p->smoother_degree < 1 || p->mg_depth < 1 ||
-      p->max_iterations < 1 || p->eig_cg_iterations < 1 || p->smoothing_range <= 1.0)
+      p->max_iterations < 1 || p->eig_cg_iterations < 1 || p->smoothing_range <= 1.0 || p->solver_type < 0 ||
+      p->solver_type > 1)
     return fail(h, PPF_ERR_ARG, "invalid linear solver parameters");
   LinearState& L = h->blocks[b].lin;
   if (L.initialized) return fail(h, PPF_ERR_ARG, "linear parameters are fixed after the first solve");
@@ -995,6 +1213,27 @@ int ppf_set_linear_params(ppf_handle h, int b, const ppf_linear_params* p) {
   L.params = *p;
   L.params_set = true;
   return PPF_OK;
+}
+
+int ppf_set_newton_params(ppf_handle h, int b, int max_iterations, double tolerance, double step_length) {
+  if (!h || b < 0 || b >= (int)h->blocks.size() || max_iterations < 1 || !(tolerance >= 0.0) || !(step_length > 0.0))
+    return PPF_ERR_ARG;
+  LinearState& L = h->blocks[b].lin;
+  L.newton_max_iterations = max_iterations;
+  L.newton_tolerance = tolerance;
+  L.newton_step = step_length;
+  return PPF_OK;
+}
+
+int ppf_newton_solve(ppf_handle h, int b, int* newton_iterations, int* linear_iterations, double* residual) {
+  if (!h || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  if (h->blocks[b].desc.solve_type != PPF_NEWTON) return fail(h, PPF_ERR_ARG, "block is not Newton");
+  const int rc = newton_solve(h, b);
+  const LinearState& L = h->blocks[b].lin;
+  if (newton_iterations) *newton_iterations = L.last_newton_iterations;
+  if (linear_iterations) *linear_iterations = L.last_newton_linear_iterations;
+  if (residual) *residual = L.last_newton_residual;
+  return rc;
 }
 
 int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual) {

@@ -337,3 +337,99 @@ struct CoupledACCHAdjoint {
 };
 
 }  // namespace ppf
+
+namespace ppf {
+
+// applications/allen_cahn/implicit/custom_pde.h:70-125: backward Euler through a Newton block
+// (block 1: residual old_n - n - dt M f'(n), Jacobian (1 + dt M f''(n)) dn + dt kappa M grad dn)
+// and the post-processing block 2 of the explicit application.
+template <unsigned int dim, unsigned int degree, typename number>
+struct AllenCahnImplicit {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number m_well;
+  number kappa;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 1) {
+      ScalarValue n = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad nx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue old_n = variable_list.template get_value<Scalar, OldOne>(0);
+      ScalarValue f_well = 4.0 * n * (n - 1.0) * (n - 0.5);
+      const number dt = number(sim_timer.get_timestep());
+      variable_list.set_value_term(0, old_n - n - dt * m_well * f_well);
+      variable_list.set_gradient_term(0, -dt * kappa * m_well * nx);
+    } else if (solve_block_id == 2) {
+      ScalarValue n = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad nx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue f_chem = n * n * n * n - 2.0 * n * n * n + n * n;
+      variable_list.set_value_term(1, nx.norm());
+      variable_list.set_value_term(2, f_chem + 0.5 * kappa * nx.norm_square());
+    }
+  }
+
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    if (solve_block_id == 1) {
+      ScalarValue n = variable_list.template get_value<Scalar, Current>(0);
+      ScalarValue dn = variable_list.template get_value<Scalar, Change>(0);
+      ScalarGrad dnx = variable_list.template get_gradient<Scalar, Change>(0);
+      ScalarValue df_well = 12.0 * n * (n - 1.0) + 2.0;
+      const number dt = number(sim_timer.get_timestep());
+      variable_list.set_value_term(0, dn * (1.0 + dt * m_well * df_well));
+      variable_list.set_gradient_term(0, dt * kappa * m_well * dnx);
+    }
+  }
+};
+
+// applications/cahn_hilliard/implicit/custom_pde.h:90-160: one Newton block over (c, mu)
+// (block 0) and the post-processing block 2.
+template <unsigned int dim, unsigned int degree, typename number>
+struct CahnHilliardImplicit {
+  using ScalarValue = dealii::VectorizedArray<number>;
+  using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  number McV;
+  number KcV;
+  number WcV;
+
+  PPF_HD void compute_rhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    const number dt = number(sim_timer.get_timestep());
+    if (solve_block_id == 0) {
+      ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad cx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue mu = variable_list.template get_value<Scalar, Current>(1);
+      ScalarGrad mux = variable_list.template get_gradient<Scalar, Current>(1);
+      ScalarValue c_old = variable_list.template get_value<Scalar, OldOne>(0);
+      variable_list.set_value_term(0, c_old - c);
+      variable_list.set_gradient_term(0, -(dt * McV * mux));
+      variable_list.set_value_term(1, mu - WcV * c * (c - 1.0) * (c - 0.5));
+      variable_list.set_gradient_term(1, -(KcV * cx));
+    } else if (solve_block_id == 2) {
+      ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      ScalarGrad cx = variable_list.template get_gradient<Scalar, Current>(0);
+      ScalarValue f_chem = c * c * c * c - 2.0 * c * c * c + c * c;
+      variable_list.set_value_term(2, f_chem + 0.5 * KcV * cx.norm_square());
+    }
+  }
+
+  PPF_HD void compute_lhs(FieldContainer<dim, degree, number>& variable_list, const SimulationTimer& sim_timer,
+                          unsigned int solve_block_id) const {
+    const number dt = number(sim_timer.get_timestep());
+    if (solve_block_id == 0) {
+      ScalarValue c = variable_list.template get_value<Scalar, Current>(0);
+      ScalarValue dc = variable_list.template get_value<Scalar, Change>(0);
+      ScalarGrad dcx = variable_list.template get_gradient<Scalar, Change>(0);
+      ScalarValue dmu = variable_list.template get_value<Scalar, Change>(1);
+      ScalarGrad dmux = variable_list.template get_gradient<Scalar, Change>(1);
+      ScalarValue j_mu_c = -WcV * (0.5 + 3.0 * (c * (c - 1.0))) * dc;
+      variable_list.set_value_term(0, dc);
+      variable_list.set_gradient_term(0, dt * McV * dmux);
+      variable_list.set_value_term(1, -j_mu_c - dmu);
+      variable_list.set_gradient_term(1, KcV * dcx);
+    }
+  }
+};
+
+}  // namespace ppf

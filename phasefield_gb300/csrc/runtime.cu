@@ -675,8 +675,11 @@ static int solve_increment(ppf_handle h, int output_every) {
     } else if (d.solve_type == PPF_LINEAR) {
       int rc = linear_solve(h, (int)b);
       if (rc && rc != PPF_ERR_NOCONV) return rc;  // non-convergence is logged, not fatal
+    } else if (d.solve_type == PPF_NEWTON) {
+      int rc = newton_solve(h, (int)b);
+      if (rc && rc != PPF_ERR_NOCONV) return rc;  // the reference warns and continues
     } else {
-      return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks are not implemented in this build");
+      return fail(h, PPF_ERR_UNSUPPORTED, "unknown solve type");
     }
     if (inc == 0) {
       for (int i = 0; i < d.n_fields; ++i) {

@@ -246,6 +246,20 @@ class Problem:
         self._check(rc)
         return its.value, res.value
 
+    def set_newton_params(self, b: int, max_iterations: int = 100, tolerance: float = 1e-10,
+                          step_length: float = 1.0):
+        """NonlinearSolverParameters of Newton block b."""
+        self._check(self.lib.ppf_set_newton_params(self.h, b, int(max_iterations), float(tolerance),
+                                                   float(step_length)))
+
+    def newton_solve(self, b: int, allow_noconv: bool = False) -> tuple[int, int, float]:
+        """One Newton solve of block b: (Newton iterations, Krylov iterations, residual)."""
+        its, lin, res = C.c_int(), C.c_int(), C.c_double()
+        rc = self.lib.ppf_newton_solve(self.h, b, C.byref(its), C.byref(lin), C.byref(res))
+        if not (rc == capi.PPF_ERR_NOCONV and allow_noconv):
+            self._check(rc)
+        return its.value, lin.value, res.value
+
     def lhs_diagonal(self, b: int) -> np.ndarray:
         f = self.blocks[b].field_indices[0]
         out = np.empty(self.field_length(f), dtype=np.float64)

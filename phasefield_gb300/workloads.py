@@ -11,6 +11,8 @@ nodal interpolation that ``SolverBase::set_initial_condition`` performs
   eshelby_3d          linear elasticity with eigenstrain of seeded inclusions
                       (applications/mechanics/eshelby_inclusion)
   coupled_acch_2d     coupled Allen-Cahn / Cahn-Hilliard (applications/coupled_allen_cahn_cahn_hilliard)
+  allen_cahn_implicit_2d     Allen-Cahn with a Newton block (applications/allen_cahn/implicit)
+  cahn_hilliard_implicit_2d  Cahn-Hilliard with a two-field Newton block (applications/cahn_hilliard/implicit)
 """
 from __future__ import annotations
 
@@ -18,7 +20,7 @@ from dataclasses import dataclass, field as dfield
 
 import numpy as np
 
-from .problem import (Explicit, FieldAttributes, Linear, PostProcess, Primary, RectangularMesh, Scalar,
+from .problem import (Explicit, FieldAttributes, Linear, Newton, PostProcess, Primary, RectangularMesh, Scalar,
                       Secondary, SolveBlock, Vector, make_dependency_set)
 
 
@@ -172,3 +174,45 @@ def coupled_acch_2d(refine: int = 8, degree: int = 2, seed: int = 99, size: floa
     c0 = 0.009 + (0.125 - 0.009) * n0
     return Workload("coupled_acch_2d", mesh, fields, [exp_block, pp_block], "coupled_acch", [Mc, Mn, Kn], dt,
                     n_steps, {0: c0, 1: n0}, seed)
+
+
+def allen_cahn_implicit_2d(refine: int = 5, degree: int = 1, seed: int = 1234, n_grains: int = 12, size: float = 100.0,
+                           n_steps: int = 20, dt: float = 0.5, m_well: float = 1.0, kappa: float = 2.0) -> Workload:
+    """Implicit Allen-Cahn: fields n, mg_n, f_tot; blocks as applications/allen_cahn/implicit/main.cc.
+
+    Backward Euler through a Newton block (residual old_n - n - dt M f'(n), Jacobian
+    1 + dt M f''(n) plus dt kappa M grad), so time steps far above the explicit limit work."""
+    mesh = RectangularMesh(dim=2, degree=degree, size=(size, size), subdivisions=(1, 1, 1), global_refinement=refine)
+    fields = [FieldAttributes("n", Scalar), FieldAttributes("mg_n", Scalar), FieldAttributes("f_tot", Scalar)]
+    newton = SolveBlock(id=1, solve_type=Newton, solve_timing=Primary, field_indices=[0],
+                        dependencies_rhs=make_dependency_set(fields, {"n", "grad(n)", "old_1(n)"}),
+                        dependencies_lhs=make_dependency_set(fields, {"n", "change(n)", "grad(change(n))"}))
+    pp_block = SolveBlock(id=2, solve_type=Explicit, solve_timing=PostProcess, field_indices=[1, 2],
+                          dependencies_rhs=make_dependency_set(fields, {"n", "grad(n)"}))
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.0, size, size=(n_grains, 2))
+    radii = rng.uniform(5.0, 15.0, size=n_grains)
+    n0 = grain_field(lattice_coordinates(mesh), centres, radii, 2.0)
+    return Workload("allen_cahn_implicit_2d", mesh, fields, [newton, pp_block], "allen_cahn_implicit",
+                    [m_well, kappa], dt, n_steps, {0: n0}, seed)
+
+
+def cahn_hilliard_implicit_2d(refine: int = 4, degree: int = 2, seed: int = 4321, size: float = 16.0,
+                              n_steps: int = 10, dt: float = 0.01, McV: float = 1.0, KcV: float = 1.5,
+                              WcV: float = 4.0) -> Workload:
+    """Implicit Cahn-Hilliard: fields c, mu, f_tot; one Newton block over (c, mu) as
+    applications/cahn_hilliard/implicit/main.cc (its Jacobian is not symmetric: BiCGStab)."""
+    mesh = RectangularMesh(dim=2, degree=degree, size=(size, size), subdivisions=(1, 1, 1), global_refinement=refine)
+    fields = [FieldAttributes("c"), FieldAttributes("mu"), FieldAttributes("f_tot")]
+    newton = SolveBlock(id=0, solve_type=Newton, solve_timing=Primary, field_indices=[0, 1],
+                        dependencies_rhs=make_dependency_set(fields, {"c", "grad(c)", "mu", "grad(mu)", "old_1(c)"}),
+                        dependencies_lhs=make_dependency_set(fields, {"c", "grad(c)", "mu", "grad(mu)", "change(c)",
+                                                                      "grad(change(c))", "change(mu)",
+                                                                      "grad(change(mu))"}))
+    pp_block = SolveBlock(id=2, solve_type=Explicit, solve_timing=PostProcess, field_indices=[2],
+                          dependencies_rhs=make_dependency_set(fields, {"c", "grad(c)"}))
+    rng = np.random.default_rng(seed)
+    N = int(np.prod(mesh.nodes))
+    c0 = 0.5 + 0.05 * rng.uniform(-1.0, 1.0, size=N)
+    return Workload("cahn_hilliard_implicit_2d", mesh, fields, [newton, pp_block], "cahn_hilliard_implicit",
+                    [McV, KcV, WcV], dt, n_steps, {0: c0, 1: np.zeros(N)}, seed)

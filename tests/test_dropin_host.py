@@ -53,7 +53,8 @@ def prm_dump(tmp_path_factory):
 # sources compile unchanged
 # ---------------------------------------------------------------------------------------------
 @needs_gxx
-@pytest.mark.parametrize("app", ["allen_cahn_explicit", "cahn_hilliard_explicit", "eshelby_inclusion"])
+@pytest.mark.parametrize("app", ["allen_cahn_explicit", "allen_cahn_implicit", "cahn_hilliard_explicit",
+                                 "eshelby_inclusion"])
 def test_example_apps_host_syntax(app):
     rc, err = host_syntax(EXAMPLES / app)
     assert rc == 0, err
@@ -81,7 +82,7 @@ def test_reference_apps_host_syntax():
 @pytest.mark.skipif(NVCC is None, reason="nvcc not available")
 @needs_ref
 @pytest.mark.parametrize("app,ok", [("allen_cahn/explicit", True), ("mechanics/eshelby_inclusion", True),
-                                    ("nucleation", False)])
+                                    ("cahn_hilliard/implicit", True), ("nucleation", False)])
 def test_reference_apps_device_compile(tmp_path, app, ok):
     """The cell kernel compiles for the reference's own CustomPDE. An operator whose GPU callback
     calls a host-only function (nucleation's seed_nucleus) is rejected at compile time."""

@@ -194,3 +194,49 @@ set Model constant n_inclusions = {len(incl)}, INT
     u = to_lattice(v, wl.mesh, "u", ncomp=3)
     assert np.abs(u).max() > 1e-4  # the inclusions load the body
     assert rel_l2(u, o.get(0, 0)) < 1e-8
+
+
+def test_implicit_allen_cahn_application_matches_oracle(gpu_lib, tmp_path):
+    """A Newton block through the drop-in: the application's linear/Newton parameters reach the
+    engine by solve-block id and the implicit steps match the oracle's Newton solver."""
+    n = 6
+    build_and_run("allen_cahn_implicit", f"""
+set global refinement = 4
+subsection Rectangular mesh
+  set x size = 100.0
+  set y size = 100.0
+end
+set time step = 1.0
+set number steps = {n}
+subsection output
+  set number = 1
+end
+subsection linear solver parameters: 0
+  set solver_ids = 1
+  set tolerance type = RMSEPerField
+  set tolerance value = 1e-13
+  set max iterations = 3000
+end
+subsection newton solver parameters: 0
+  set solver_ids = 1
+  set max iterations = 50
+  set tolerance value = 1e-12
+end
+subsection miscellaneous
+  set random seed = 7
+end
+set Model constant mobility = 1.0, DOUBLE
+set Model constant kappa = 2.0, DOUBLE
+set Model constant n_grains = 12, INT
+""", tmp_path)
+    wl = W.allen_cahn_implicit_2d(refine=4, dt=1.0)
+    v0 = read_vtu(tmp_path / "solutions" / "solution_0.vtu")
+    wl.initial = {0: to_lattice(v0, wl.mesh, "n")}
+    o = po.Oracle(wl)
+    o.set_linear_params(0, tolerance_type=1, tolerance=1e-13, max_iterations=3000)
+    o.set_newton_params(0, max_iterations=50, tolerance=1e-12)
+    assert o.run(n, n) == 0
+    v1 = read_vtu(tmp_path / "solutions" / f"solution_{n}.vtu")
+    assert rel_l2(to_lattice(v1, wl.mesh, "n"), o.get(0, 1)) < 1e-8
+    assert rel_l2(to_lattice(v1, wl.mesh, "f_tot"), o.get(2, 0)) < 1e-8
+

@@ -188,3 +188,61 @@ def test_gmg_iterations_fall_with_depth_symmetric_scaling():
         assert rc == 0
         its.append(it)
     assert its[0] > its[1] > its[2]
+
+
+# ---------------------------------------------------------------------------------------------
+# Newton solves (newton_solver.h:73-156)
+# ---------------------------------------------------------------------------------------------
+def _implicit_ac(dt=2.0, refine=4):
+    wl = W.allen_cahn_implicit_2d(refine=refine, dt=dt)
+    o = po.Oracle(wl)
+    o.set_linear_params(0, tolerance_type=1, tolerance=1e-12, max_iterations=2000)
+    o.set_newton_params(0, max_iterations=50, tolerance=1e-10)
+    return wl, o
+
+
+def test_newton_allen_cahn_converges_and_is_bounded_at_large_dt():
+    # dt = 2 is 30x the explicit limit of this mesh; backward Euler stays within [0, 1]
+    wl, o = _implicit_ac(dt=2.0)
+    assert o.run(6, 6) == 0
+    n = o.get(0, 1)
+    assert np.all(n > -1e-3) and np.all(n < 1.0 + 1e-3)
+    rc, its, lin, res = o.newton_solve(0)
+    assert rc == 0 and its <= 6 and res < 1e-10
+
+
+def test_newton_allen_cahn_fixed_points():
+    wl, o = _implicit_ac(dt=5.0, refine=3)
+    for value in (0.0, 1.0):
+        v = np.full(o.n_dofs(0), value)
+        o.set(0, v, age=1)
+        o.set(0, v, age=0)
+        rc, its, lin, res = o.newton_solve(0)
+        assert rc == 0 and its == 0  # the residual of a fixed point is already zero
+        assert np.allclose(o.get(0, 0), value, atol=1e-14)
+
+
+def test_newton_cg_and_bicgstab_agree_on_a_symmetric_jacobian():
+    sols = []
+    for solver in (0, 1):
+        wl, o = _implicit_ac(dt=1.0)
+        o.set_linear_params(0, tolerance_type=1, tolerance=1e-13, max_iterations=2000, solver_type=solver)
+        o.set(0, wl.initial[0], age=1)
+        o.set(0, wl.initial[0], age=0)
+        rc, its, lin, res = o.newton_solve(0)
+        assert rc == 0
+        sols.append(o.get(0, 0))
+    assert np.linalg.norm(sols[0] - sols[1]) / np.linalg.norm(sols[1]) < 1e-10
+
+
+def test_newton_cahn_hilliard_two_field_block_conserves_mass():
+    wl = W.cahn_hilliard_implicit_2d(refine=3, dt=0.05)
+    o = po.Oracle(wl)
+    o.set_linear_params(0, tolerance_type=1, tolerance=1e-13, max_iterations=4000, solver_type=1)
+    o.set_newton_params(0, max_iterations=50, tolerance=1e-11)
+    assert o.run(4) == 0
+    m = o.invm(0)
+    mass = np.where(m > 0, 1.0 / np.where(m > 0, m, 1.0), 0.0)
+    assert abs((mass * o.get(0, 1)).sum() - (mass * wl.initial[0]).sum()) < 1e-10 * (mass * wl.initial[0]).sum()
+    # the step is not the identity: the interface has moved
+    assert np.linalg.norm(o.get(0, 1) - wl.initial[0]) > 1e-4
