@@ -217,6 +217,12 @@ int ppf_set_linear_params(ppf_handle h, int block, const ppf_linear_params* p);
  * is reached (the solution is still written, as the reference logs and continues). */
 int ppf_linear_solve(ppf_handle h, int b, int* iterations, double* residual);
 
+/* Wall-clock phases of the last ppf_linear_solve of block b, in ms: construction of the
+ * level hierarchy (first solve only, else 0), per-solve set-up (level diagonals and Chebyshev
+ * eigenvalue estimates), right-hand side (compute_rhs and the inhomogeneous lift), and the CG
+ * iterations. Outputs may be NULL. */
+int ppf_linear_stats(ppf_handle h, int b, double* init_ms, double* setup_ms, double* rhs_ms, double* iterate_ms);
+
 /* NonlinearSolverParameters of Newton block b (solve_parameters.cc:350-470): at most
  * max_iterations Newton steps (default 100), stop when the scaled residual norm is at most
  * tolerance * normalisation (default 1e-10), update u += step_length * change (default 1). */

@@ -51,7 +51,6 @@ struct MGLevel {
   long long N = 0, ncells = 0, len = 0;
   int precision = 0;            // 0 FP64, 1 FP32
   int* cmap = nullptr;          // homogeneous level constraints
-  std::vector<int> h_cmap;
   bool constrained = false;
   void* invm_sqrt = nullptr;    // per node, level precision
   void* inv_diag = nullptr;     // len, level precision
@@ -99,6 +98,16 @@ struct LinearState {
   int last_iterations = 0;
   double last_residual = 0.0;
   double last_rhs_norm = 0.0;
+  // the preconditioner application captured as a CUDA graph (rebuilt for every solve)
+  cudaGraphExec_t pc_graph = nullptr;
+  const void* pc_in = nullptr;
+  void* pc_out = nullptr;
+  int pc_calls = 0;               // applications in the current solve
+  bool pc_nograph = false;        // capture is not possible on the handle's stream
+  double last_init_ms = 0.0;     // hierarchy construction (first solve only)
+  double last_setup_ms = 0.0;    // phases of the last linear solve: diagonals + eigenvalue estimates,
+  double last_rhs_ms = 0.0;      // right-hand side (+ inhomogeneous lift), CG iterations
+  double last_iterate_ms = 0.0;
   // Newton blocks (NonlinearSolverParameters) and their block-vector work space
   int newton_max_iterations = 100;
   double newton_tolerance = 1e-10;

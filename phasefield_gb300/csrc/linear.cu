@@ -21,6 +21,7 @@
 //     g the Dirichlet values (plain read), CG from the previous homogeneous solution,
 //     x = x_hom + g, constraints distributed.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -214,68 +215,82 @@ static void convert(ppf_handle h, int pin, int pout, long long n, const void* x,
 }
 
 // lumped mass on a lattice of nc cells per axis (periodic images condensed), inverted sqrt
-static std::vector<double> level_invm_sqrt(ppf_handle h, const int* nc, const int* nn, const double* hh) {
-  const int dim = h->dim, n = h->n, k = h->k;
-  const GLRule g = gauss_lobatto(n);
-  long long N = 1;
-  for (int d = 0; d < dim; ++d) N *= nn[d];
-  // separable: the lumped mass of a node is the product of 1-D lumped masses
-  std::vector<std::vector<double>> m1(dim);
-  for (int d = 0; d < dim; ++d) {
-    m1[d].assign(nn[d], 0.0);
-    for (int c = 0; c < nc[d]; ++c)
-      for (int a = 0; a < n; ++a) m1[d][k * c + a] += g.w[a] * hh[d];
-    if (h->mesh.periodic[d]) {
-      m1[d][0] += m1[d][nn[d] - 1];
-      m1[d][nn[d] - 1] = 0.0;
+// ------------------------------------------------------------------------------------------
+// level set-up on the device (constraint map, inverse mass root, eigenvalue-estimate pattern)
+// ------------------------------------------------------------------------------------------
+struct LevelGeom {
+  int nn[3];
+  int periodic[3];
+  int dim;
+  long long N;
+};
+
+// pass 1: periodic images fold onto the lower face; free nodes on a Dirichlet face of their
+// component (bit b of dmask[c]) become Dirichlet rows (-1)
+__global__ void level_cmap_kernel(int* __restrict__ cm, LevelGeom g, int ncomp, unsigned dm0, unsigned dm1,
+                                  unsigned dm2) {
+  const long long len = ncomp * g.N;
+  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < len;
+       gi += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(gi / g.N);
+    const long long i = gi - c * g.N;
+    long long I[3] = {i % g.nn[0], (i / g.nn[0]) % g.nn[1], i / ((long long)g.nn[0] * g.nn[1])};
+    long long F[3] = {I[0], I[1], I[2]};
+    for (int d = 0; d < g.dim; ++d)
+      if (g.periodic[d] && F[d] == g.nn[d] - 1) F[d] = 0;
+    const long long m = c * g.N + (F[2] * g.nn[1] + F[1]) * g.nn[0] + F[0];
+    int v = (int)m;
+    if (m == gi) {
+      const unsigned dm = c == 0 ? dm0 : (c == 1 ? dm1 : dm2);
+      for (int b = 0; b < 2 * g.dim; ++b)
+        if ((dm >> b) & 1u) {
+          const int d = b / 2;
+          if ((b % 2 == 0 && I[d] == 0) || (b % 2 == 1 && I[d] == g.nn[d] - 1)) v = -1;
+        }
     }
+    cm[gi] = v;
   }
-  std::vector<double> out(N);
-  for (long long i = 0; i < N; ++i) {
-    long long r = i;
-    double m = 1.0;
-    for (int d = 0; d < dim; ++d) {
-      m *= m1[d][r % nn[d]];
-      r /= nn[d];
-    }
-    out[i] = m == 0.0 ? 0.0 : std::sqrt(1.0 / m);
-  }
-  return out;
 }
 
-static bool on_face(const int* nn, long long node, int bid, int dim) {
-  const int d = bid / 2;
-  if (d >= dim) return false;
-  long long c[3] = {node % nn[0], (node / nn[0]) % nn[1], node / ((long long)nn[0] * nn[1])};
-  return (bid % 2 == 0) ? c[d] == 0 : c[d] == nn[d] - 1;
-}
-
-static std::vector<int> level_cmap(ppf_handle h, const FieldState& F, const int* nn) {
-  const int dim = h->dim;
-  long long N = 1;
-  for (int d = 0; d < dim; ++d) N *= nn[d];
-  std::vector<int> cm(F.ncomp * N);
-  for (int c = 0; c < F.ncomp; ++c)
-    for (long long i = 0; i < N; ++i) {
-      long long I = i % nn[0], J = (i / nn[0]) % nn[1], K = i / ((long long)nn[0] * nn[1]);
-      if (h->mesh.periodic[0] && I == nn[0] - 1) I = 0;
-      if (dim > 1 && h->mesh.periodic[1] && J == nn[1] - 1) J = 0;
-      if (dim > 2 && h->mesh.periodic[2] && K == nn[2] - 1) K = 0;
-      cm[c * N + i] = (int)(c * N + (K * nn[1] + J) * nn[0] + I);
-    }
-  for (int c = 0; c < F.ncomp; ++c)
-    for (int b = 0; b < 2 * dim; ++b) {
-      if (!F.desc.dirichlet[c][b]) continue;
-      for (long long i = 0; i < N; ++i) {
-        const long long gi = c * N + i;
-        if (on_face(nn, i, b, dim) && cm[gi] == (int)gi) cm[gi] = -1;
-      }
-    }
-  for (long long gi = 0; gi < (long long)cm.size(); ++gi) {
+// pass 2: an image whose master is a Dirichlet row becomes a Dirichlet row
+__global__ void level_cmap_close_kernel(int* __restrict__ cm, long long len) {
+  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < len;
+       gi += (long long)gridDim.x * blockDim.x) {
     const int m = cm[gi];
     if (m >= 0 && m != (int)gi && cm[m] < 0) cm[gi] = -1;
   }
-  return cm;
+}
+
+// invM^1/2 per node from the separable 1-D lumped masses m1 (axis d at m1 + off[d])
+template <typename T>
+__global__ void level_invm_sqrt_kernel(T* __restrict__ out, const double* __restrict__ m1, LevelGeom g, int off1,
+                                       int off2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.N; i += (long long)gridDim.x * blockDim.x) {
+    const long long I = i % g.nn[0], J = (i / g.nn[0]) % g.nn[1], K = i / ((long long)g.nn[0] * g.nn[1]);
+    double m = m1[I];
+    if (g.dim > 1) m *= m1[off1 + J];
+    if (g.dim > 2) m *= m1[off2 + K];
+    out[i] = m == 0.0 ? T(0) : T(sqrt(1.0 / m));
+  }
+}
+
+// sum of (i mod 11) over free entries and their count (integers: exact in any order)
+__global__ void pattern_sum_kernel(const int* __restrict__ cm, long long len, unsigned long long* sums) {
+  unsigned long long s = 0, n = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    if (cm[i] == (int)i) {
+      s += (unsigned long long)(i % 11);
+      n += 1;
+    }
+  atomicAdd(sums, s);
+  atomicAdd(sums + 1, n);
+}
+
+// the estimate's start vector: (i mod 11) - mean on free entries, zero on constrained ones
+template <typename T>
+__global__ void pattern_kernel(T* __restrict__ out, const int* __restrict__ cm, long long len, double mean) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < len; i += (long long)gridDim.x * blockDim.x)
+    out[i] = cm[i] == (int)i ? T(double(i % 11) - mean) : T(0);
 }
 
 // 1-D prolongation from a coarse axis with ncc cells to the fine axis with 2 ncc cells
@@ -452,18 +467,18 @@ template <typename T>
 static int estimate_eigenvalues(ppf_handle h, BlockState& B, MGLevel& lv) {
   LinearState& L = B.lin;
   const int prec = lv.precision;
-  std::vector<T> pat(lv.len);
-  std::vector<int>& cm = lv.h_cmap;
-  double mean = 0.0;
-  long long nfree = 0;
-  for (long long i = 0; i < lv.len; ++i)
-    if (cm[i] == (int)i) {
-      mean += double(i % 11);
-      nfree++;
-    }
-  mean /= std::max<long long>(1, nfree);
-  for (long long i = 0; i < lv.len; ++i) pat[i] = cm[i] == (int)i ? T(double(i % 11) - mean) : T(0);
-  PPF_CUDA(h, cudaMemcpyAsync(lv.b, pat.data(), sizeof(T) * lv.len, cudaMemcpyHostToDevice, h->stream));
+  {
+    unsigned long long* d_sums = reinterpret_cast<unsigned long long*>(L.partial);
+    PPF_CUDA(h, cudaMemsetAsync(d_sums, 0, 2 * sizeof(unsigned long long), h->stream));
+    pattern_sum_kernel<<<grid_for(lv.len), 256, 0, h->stream>>>(lv.cmap, lv.len, d_sums);
+    unsigned long long sums[2];
+    PPF_CUDA(h, cudaMemcpyAsync(sums, d_sums, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+    const double mean = double(sums[0]) / double(std::max<unsigned long long>(1, sums[1]));
+    pattern_kernel<T><<<grid_for(lv.len), 256, 0, h->stream>>>((T*)lv.b, lv.cmap, lv.len, mean);
+    h->all_launches += 2;
+    PPF_CUDA(h, cudaGetLastError());
+  }
   T* x = (T*)lv.x;
   T* r = (T*)lv.r;
   T* z = (T*)lv.w0;
@@ -692,14 +707,56 @@ static int init_linear(ppf_handle h, int b) {
     lv.len = F.ncomp * lv.N;
     const bool is_fine = l == depth - 1;
     lv.precision = (L.params.preconditioner == 2 && L.params.mixed_precision && l > 0) ? 1 : 0;
-    lv.h_cmap = level_cmap(h, F, lv.nn);
-    lv.constrained = false;
-    for (long long i = 0; i < lv.len; ++i)
-      if (lv.h_cmap[i] != (int)i) lv.constrained = true;
-    int rc = upload_vec<int>(h, (void**)&lv.cmap, lv.h_cmap);
-    if (rc) return rc;
-    rc = upload_real(h, &lv.invm_sqrt, level_invm_sqrt(h, lv.nc, lv.nn, lv.h), lv.precision);
-    if (rc) return rc;
+    // constraint map and invM^1/2 of the level, built on the device
+    LevelGeom geom;
+    geom.dim = h->dim;
+    geom.N = lv.N;
+    unsigned dmask[3] = {0u, 0u, 0u};
+    bool any_constraint = false;
+    for (int d = 0; d < 3; ++d) {
+      geom.nn[d] = lv.nn[d];
+      geom.periodic[d] = d < h->dim ? h->mesh.periodic[d] : 0;
+      any_constraint |= geom.periodic[d] != 0;
+    }
+    for (int c = 0; c < F.ncomp; ++c)
+      for (int bid = 0; bid < 2 * h->dim; ++bid)
+        if (F.desc.dirichlet[c][bid]) {
+          dmask[c] |= 1u << bid;
+          any_constraint = true;
+        }
+    lv.constrained = any_constraint;
+    PPF_CUDA(h, cudaMalloc(&lv.cmap, sizeof(int) * std::max<long long>(1, lv.len)));
+    level_cmap_kernel<<<grid_for(lv.len), 256, 0, h->stream>>>(lv.cmap, geom, F.ncomp, dmask[0], dmask[1], dmask[2]);
+    level_cmap_close_kernel<<<grid_for(lv.len), 256, 0, h->stream>>>(lv.cmap, lv.len);
+    {
+      std::vector<double> m1;
+      int offs[3] = {0, 0, 0};
+      for (int d = 0; d < h->dim; ++d) {
+        offs[d] = (int)m1.size();
+        std::vector<double> a(lv.nn[d], 0.0);
+        for (int cc = 0; cc < lv.nc[d]; ++cc)
+          for (int q = 0; q < h->n; ++q) a[h->k * cc + q] += g.w[q] * lv.h[d];
+        if (h->mesh.periodic[d]) {
+          a[0] += a[lv.nn[d] - 1];
+          a[lv.nn[d] - 1] = 0.0;
+        }
+        m1.insert(m1.end(), a.begin(), a.end());
+      }
+      void* d_m1 = nullptr;
+      int rc = upload_vec<double>(h, &d_m1, m1);
+      if (rc) return rc;
+      PPF_CUDA(h, cudaMalloc(&lv.invm_sqrt, esize(lv.precision) * std::max<long long>(1, lv.N)));
+      if (lv.precision)
+        level_invm_sqrt_kernel<float><<<grid_for(lv.N), 256, 0, h->stream>>>((float*)lv.invm_sqrt, (const double*)d_m1,
+                                                                             geom, offs[1], offs[2]);
+      else
+        level_invm_sqrt_kernel<double><<<grid_for(lv.N), 256, 0, h->stream>>>((double*)lv.invm_sqrt,
+                                                                              (const double*)d_m1, geom, offs[1], offs[2]);
+      PPF_CUDA(h, cudaGetLastError());
+      PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+      cudaFree(d_m1);
+    }
+    int rc = PPF_OK;
     // LHS tables of this level (the block's LHS dependency slots)
     signed char slot_of[pg::MAX_FIELDS][pg::NAGE];
     signed char slot_comp0[pg::MAX_SLOTS] = {};
@@ -785,12 +842,60 @@ static int precondition(ppf_handle h, BlockState& B, const double* r, double* z)
   return PPF_OK;
 }
 
+// precondition() through a CUDA graph: the first application of a solve runs as plain
+// launches (every kernel is configured then), the second is captured and every later one
+// replays the graph: a V-cycle is a few hundred small launches on the coarse levels, whose
+// launch overhead the graph removes. The graph holds the solve's simulation time and level
+// state, so it is rebuilt for each solve.
+static void drop_pc_graph(LinearState& L) {
+  if (L.pc_graph) cudaGraphExecDestroy(L.pc_graph);
+  L.pc_graph = nullptr;
+  L.pc_calls = 0;
+}
+
+static int precondition_graphed(ppf_handle h, BlockState& B, const double* r, double* z) {
+  LinearState& L = B.lin;
+  if (L.params.preconditioner == 0 || h->timing || !h->use_graph || L.pc_nograph) return precondition(h, B, r, z);
+  if (L.pc_graph && L.pc_in == r && L.pc_out == z) {
+    PPF_CUDA(h, cudaGraphLaunch(L.pc_graph, h->stream));
+    h->all_launches++;
+    return PPF_OK;
+  }
+  if (L.pc_calls++ == 0) return precondition(h, B, r, z);
+  drop_pc_graph(L);
+  L.pc_calls = 2;
+  if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    L.pc_nograph = true;
+    return precondition(h, B, r, z);
+  }
+  int rc = precondition(h, B, r, z);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("preconditioner capture: ") + cudaGetErrorString(e));
+  const cudaError_t ie = cudaGraphInstantiate(&L.pc_graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("preconditioner graph: ") + cudaGetErrorString(ie));
+  L.pc_in = r;
+  L.pc_out = z;
+  PPF_CUDA(h, cudaGraphLaunch(L.pc_graph, h->stream));
+  h->all_launches++;
+  return PPF_OK;
+}
+
 int linear_solve(ppf_handle h, int b) {
   BlockState& B = h->blocks[b];
   LinearState& L = B.lin;
+  L.last_init_ms = 0.0;
   if (!L.initialized) {
+    const auto t0 = std::chrono::steady_clock::now();
     int rc = init_linear(h, b);
     if (rc) return rc;
+    L.last_init_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   const int f = B.desc.field_indices[0];
   FieldState& F = h->fields[f];
@@ -843,6 +948,14 @@ int linear_solve(ppf_handle h, int b) {
     PPF_CUDA(h, cudaGetLastError());
     return PPF_OK;
   };
+  // phase timers (host wall clock; each phase ends on a stream synchronisation)
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+  };
+  drop_pc_graph(L);
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const auto t_start = now();
   // diagonals of every level (recomputed for each solve, as the reference does)
   if (L.params.preconditioner != 0) {
     for (auto& lv : L.levels) {
@@ -854,6 +967,8 @@ int linear_solve(ppf_handle h, int b) {
       }
     }
   }
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const auto t_setup = now();
   // rhs = S * compute_rhs
   {
     PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * n, h->stream));
@@ -880,6 +995,8 @@ int linear_solve(ppf_handle h, int b) {
     if (rc) return rc;
     axpby(h, 0, n, -1.0, L.q, 1.0, L.rhs);
   }
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const auto t_rhs = now();
   // CG on S A x = rhs from the previous homogeneous solution (SolverCG)
   double* x = L.x_hom;
   const double tol = L.params.tolerance * normalization(h, L);
@@ -894,7 +1011,7 @@ int linear_solve(ppf_handle h, int b) {
   int it = 0;
   bool converged = res < tol;
   if (!converged) {
-    rc = precondition(h, B, L.r, L.z);
+    rc = precondition_graphed(h, B, L.r, L.z);
     if (rc) return rc;
     PPF_CUDA(h, cudaMemcpyAsync(L.p, L.z, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
     double rz;
@@ -918,7 +1035,7 @@ int linear_solve(ppf_handle h, int b) {
         converged = true;
         break;
       }
-      rc = precondition(h, B, L.r, L.z);
+      rc = precondition_graphed(h, B, L.r, L.z);
       if (rc) return rc;
       double rz_new;
       rc = dot(h, L, 0, n, L.r, L.z, &rz_new);
@@ -928,6 +1045,11 @@ int linear_solve(ppf_handle h, int b) {
       axpby(h, 0, n, 1.0, L.z, beta, L.p);
     }
   }
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const auto t_end = now();
+  L.last_setup_ms = ms(t_start, t_setup);
+  L.last_rhs_ms = ms(t_setup, t_rhs);
+  L.last_iterate_ms = ms(t_rhs, t_end);
   L.last_iterations = it;
   L.last_residual = res / normalization(h, L);
   double bb;
@@ -1155,6 +1277,7 @@ int newton_solve(ppf_handle h, int b) {
 }
 
 void free_linear(LinearState& L) {
+  drop_pc_graph(L);
   for (double* p : {L.rhs, L.g, L.x_hom, L.r, L.p, L.q, L.z, L.inv_diag, L.partial, L.newton_update}) cudaFree(p);
   for (double*& p : L.kv) {
     cudaFree(p);
@@ -1212,6 +1335,16 @@ int ppf_set_linear_params(ppf_handle h, int b, const ppf_linear_params* p) {
     return fail(h, PPF_ERR_UNSUPPORTED, "mixed precision needs an FP32 instance of the operator");
   L.params = *p;
   L.params_set = true;
+  return PPF_OK;
+}
+
+int ppf_linear_stats(ppf_handle h, int b, double* init_ms, double* setup_ms, double* rhs_ms, double* iterate_ms) {
+  if (!h || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  const LinearState& L = h->blocks[b].lin;
+  if (init_ms) *init_ms = L.last_init_ms;
+  if (setup_ms) *setup_ms = L.last_setup_ms;
+  if (rhs_ms) *rhs_ms = L.last_rhs_ms;
+  if (iterate_ms) *iterate_ms = L.last_iterate_ms;
   return PPF_OK;
 }
 

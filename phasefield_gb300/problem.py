@@ -246,6 +246,12 @@ class Problem:
         self._check(rc)
         return its.value, res.value
 
+    def linear_stats(self, b: int) -> dict:
+        """Wall-clock phases (ms) of the last linear solve of block b."""
+        z, a, r, i = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.ppf_linear_stats(self.h, b, C.byref(z), C.byref(a), C.byref(r), C.byref(i)))
+        return {"init_ms": z.value, "setup_ms": a.value, "rhs_ms": r.value, "iterate_ms": i.value}
+
     def set_newton_params(self, b: int, max_iterations: int = 100, tolerance: float = 1e-10,
                           step_length: float = 1.0):
         """NonlinearSolverParameters of Newton block b."""

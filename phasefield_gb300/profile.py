@@ -50,6 +50,7 @@ def main(argv=None) -> int:
                             preconditioner=args.preconditioner, mg_depth=depth, smoother_degree=4,
                             mixed_precision=args.mixed)
         its, _ = p.linear_solve(0)
+        print("phases (ms):", {k: round(v, 2) for k, v in p.linear_stats(0).items()})
         p.close()
         print(f"eshelby_3d: preconditioner {args.preconditioner} CG {its} iterations ok")
         return 0
