@@ -170,8 +170,11 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads)
               if (active) {
                 const long long idx = node + c * P.N;
                 if (sd.constrained_read) {
-                  const int m = sd.cmap[idx];
-                  v = m >= 0 ? __ldg(ptr + m) : number(0);
+                  // the value load issues with the map load: almost every entry is free, so
+                  // the dependent second load is only paid on constrained entries
+                  const int m = __ldg(sd.cmap + idx);
+                  const number own = __ldg(ptr + idx);
+                  v = m == (int)idx ? own : (m >= 0 ? __ldg(ptr + m) : number(0));
                 } else {
                   v = __ldg(ptr + idx);
                 }
