@@ -944,7 +944,6 @@ int ppf_invm(ppf_handle h, double* out) {
 static int permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
                       bool upload) {
   FieldState& F = h->fields[f];
-  std::vector<double> tmp(F.len);
   if (ordering == PPF_ORDER_LATTICE) {
     if (upload) PPF_CUDA(h, cudaMemcpyAsync(dev_dst, host, sizeof(double) * F.len, cudaMemcpyHostToDevice, h->stream));
     else PPF_CUDA(h, cudaMemcpyAsync(host, dev_src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->stream));
@@ -952,6 +951,7 @@ static int permute_io(ppf_handle h, int f, double* host, const double* dev_src, 
     return PPF_OK;
   }
   if (ordering != PPF_ORDER_DEALII) return fail(h, PPF_ERR_ARG, "unknown ordering");
+  std::vector<double> tmp(F.len);
   auto m = dealii_dof_map(h, F.ncomp);
   if (upload) {
     for (long long i = 0; i < F.len; ++i) tmp[m[i]] = host[i];
