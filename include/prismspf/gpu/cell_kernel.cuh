@@ -37,7 +37,23 @@
 #undef compute_rhs
 #undef compute_lhs
 
+// minimum resident blocks per SM the cell kernels are compiled for (register budget)
+#ifndef PPF_CELL_MIN_BLOCKS
+#define PPF_CELL_MIN_BLOCKS 1
+#endif
+
 namespace ppf {
+
+// An operator may ask for a register budget through `static constexpr int cell_min_blocks`
+// (resident blocks per SM); otherwise the kernels are compiled for PPF_CELL_MIN_BLOCKS.
+template <class PDE, class = void>
+struct CellMinBlocks {
+  static constexpr int value = PPF_CELL_MIN_BLOCKS;
+};
+template <class PDE>
+struct CellMinBlocks<PDE, std::void_t<decltype(PDE::cell_min_blocks)>> {
+  static constexpr int value = PDE::cell_min_blocks;
+};
 
 using prismspf::FieldContainer;
 using prismspf::SimulationTimer;
@@ -115,7 +131,7 @@ __device__ __forceinline__ number integrate_row(const pg::CellTables<dim, degree
 }
 
 template <class PDE, int dim, int degree, int MODE, typename number>
-__global__ void __launch_bounds__(CellShape<dim, degree>::threads)
+__global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks<PDE>::value)
     cell_kernel(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde) {
   using S = CellShape<dim, degree>;
   using Tab = pg::CellTables<dim, degree, number>;

@@ -14,6 +14,10 @@
 #include <prismspf/core/field_container.h>
 #include <prismspf/utilities/mechanics.h>
 
+#ifndef PPF_ESHELBY_F32_MIN_BLOCKS
+#define PPF_ESHELBY_F32_MIN_BLOCKS 6
+#endif
+
 namespace ppf {
 
 using namespace prismspf;
@@ -51,6 +55,9 @@ template <unsigned int dim, unsigned int degree, typename number>
 struct CahnHilliard {
   using ScalarValue = dealii::VectorizedArray<number>;
   using ScalarGrad = dealii::Tensor<1, dim, ScalarValue>;
+  // Q2 3-D: 32 registers and 8 resident blocks per SM measured 2.7 % faster than the free
+  // register budget (6 blocks), despite a 60-byte spill
+  static constexpr int cell_min_blocks = (dim == 3 && degree == 2) ? 8 : 1;
   number McV;
   number KcV;
   number WcV;
@@ -88,6 +95,8 @@ template <unsigned int dim, unsigned int degree, typename number>
 struct Eshelby {
   using ScalarValue = dealii::VectorizedArray<number>;
   using VectorGrad = dealii::Tensor<2, dim, ScalarValue>;
+  // register budget of the FP32 operator (the multigrid smoothing levels)
+  static constexpr int cell_min_blocks = std::is_same_v<number, float> ? PPF_ESHELBY_F32_MIN_BLOCKS : 1;
   static constexpr unsigned int nv = Mechanics::voigt_tensor_size<dim>;
   dealii::Tensor<2, nv, number> stiffness;
   number e0;      // eigenstrain magnitude
