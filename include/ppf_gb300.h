@@ -171,6 +171,15 @@ int ppf_apply_constraints(ppf_handle h, int field);
  * on increments divisible by output_every (never when output_every <= 0). */
 int ppf_run(ppf_handle h, unsigned int n_increments, int output_every);
 
+/* The increment loop split open, for callers that act between blocks (the sharded driver
+ * exchanges halo planes after every block): ppf_increment_block does block b's part of the
+ * current increment exactly as ppf_run would (PostProcess / NucleationRate blocks only when
+ * is_output; Primary blocks keep the initial condition at increment 0; old ages start from
+ * the current vector at increment 0); ppf_end_increment rotates the ages, advances the
+ * timer and reports a non-finite result as PPF_ERR_NAN. */
+int ppf_increment_block(ppf_handle h, int b, int is_output);
+int ppf_end_increment(ppf_handle h);
+
 /* One explicit solve of block index b (ExplicitSolver::solve_impl, explicit_solver.h:63-77). */
 int ppf_solve_block(ppf_handle h, int b);
 

@@ -1736,42 +1736,58 @@ int orc_explicit_block(void* h, int b) {
 
 // The Problem::solve increment loop (explicit blocks only); output_every > 0 makes
 // PostProcess blocks run on increments that are multiples of it.
+// Block b's part of the current increment (Problem::solve_increment, problem.cc:416-557).
+int orc_increment_block(void* h, int b, int is_output) {
+  auto* P = (Problem*)h;
+  Block& B = P->blocks[b];
+  if (B.timing == ORC_TIMING_POSTPROCESS && !is_output) return 0;
+  if (P->increment == 0 && B.timing == ORC_TIMING_PRIMARY) {
+    // initial condition already uploaded into `cur`; like
+    // SolverBase::set_initial_condition (solver_base.h:178-229) no constraints are
+    // distributed on it at increment 0
+  } else {
+    if (B.solve_type == 2) linear_solve(*P, B);
+    else if (B.solve_type == 3) {
+      const int rc = newton_solve(*P, B);
+      if (rc != 0 && rc != 4) return rc;  // non-convergence is a warning in the reference
+    } else explicit_solve(*P, B);
+  }
+  if (P->increment == 0) {
+    for (int f : B.fields) {
+      Field& F = P->fields[f];
+      for (int a = 0; a < F.n_old; ++a) F.old[a] = F.cur;
+    }
+  }
+  return 0;
+}
+
+// End of an increment: NaN check, rotation by swap (group_solution_handler.cc:369-403), time.
+int orc_end_increment(void* h) {
+  auto* P = (Problem*)h;
+  for (auto& F : P->fields)
+    if (!std::isfinite(F.cur.empty() ? 0.0 : F.cur[0])) return ORC_ERR_NAN;
+  for (auto& F : P->fields)
+    for (int age = F.n_old - 1; age >= 0; --age) {
+      if (age > 0) F.old[age].swap(F.old[age - 1]);
+      else F.old[0].swap(F.cur);
+    }
+  P->increment++;
+  P->time += P->dt;
+  return 0;
+}
+
+// The Problem::solve increment loop; output_every > 0 makes PostProcess blocks run on
+// increments that are multiples of it.
 int orc_run(void* h, unsigned n_increments, int output_every) {
   auto* P = (Problem*)h;
   while (P->increment <= n_increments) {
-    for (auto& B : P->blocks) {
-      if (B.timing == ORC_TIMING_POSTPROCESS) {
-        if (output_every <= 0 || (P->increment % (unsigned)output_every) != 0) continue;
-      }
-      if (P->increment == 0 && B.timing == ORC_TIMING_PRIMARY) {
-        // initial condition already uploaded into `cur`; like
-        // SolverBase::set_initial_condition (solver_base.h:178-229) no constraints are
-        // distributed on it at increment 0
-      } else {
-        if (B.solve_type == 2) linear_solve(*P, B);
-        else if (B.solve_type == 3) {
-          const int rc = newton_solve(*P, B);
-          if (rc != 0 && rc != 4) return rc;  // non-convergence is a warning in the reference
-        } else explicit_solve(*P, B);
-      }
-      if (P->increment == 0) {
-        for (int f : B.fields) {
-          Field& F = P->fields[f];
-          for (int a = 0; a < F.n_old; ++a) F.old[a] = F.cur;
-        }
-      }
+    const int is_output = output_every > 0 && (P->increment % (unsigned)output_every) == 0;
+    for (size_t b = 0; b < P->blocks.size(); ++b) {
+      const int rc = orc_increment_block(h, (int)b, is_output);
+      if (rc) return rc;
     }
-    for (auto& F : P->fields) {
-      if (!std::isfinite(F.cur.empty() ? 0.0 : F.cur[0])) return ORC_ERR_NAN;
-    }
-    // rotation by swap (group_solution_handler.cc:369-403)
-    for (auto& F : P->fields)
-      for (int age = F.n_old - 1; age >= 0; --age) {
-        if (age > 0) F.old[age].swap(F.old[age - 1]);
-        else F.old[0].swap(F.cur);
-      }
-    P->increment++;
-    P->time += P->dt;
+    const int rc = orc_end_increment(h);
+    if (rc) return rc;
   }
   return 0;
 }

@@ -74,6 +74,8 @@ def load() -> C.CDLL:
         lib.orc_set_linear_params.argtypes = [C.c_void_p, C.c_int, dp]
         lib.orc_linear_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), dp]
         lib.orc_diagonal.argtypes = [C.c_void_p, C.c_int, dp]
+        lib.orc_increment_block.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        lib.orc_end_increment.argtypes = [C.c_void_p]
         lib.orc_set_solver_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
         lib.orc_set_newton_params.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         lib.orc_newton_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), dp]
@@ -209,6 +211,12 @@ class Oracle:
 
     def run(self, n_increments: int, output_every: int = 0) -> int:
         return int(self.lib.orc_run(self.h, n_increments, output_every))
+
+    def increment_block(self, b: int, is_output: bool = False) -> int:
+        return int(self.lib.orc_increment_block(self.h, b, int(is_output)))
+
+    def end_increment(self) -> int:
+        return int(self.lib.orc_end_increment(self.h))
 
     def set_linear_params(self, b: int, tolerance_type=0, tolerance=1e-10, max_iterations=100, preconditioner=0,
                           mg_depth=1, smoother_degree=5, smoothing_range=15.0, eig_cg_iterations=10, solver_type=0,

@@ -658,39 +658,54 @@ static void rotate(ppf_handle h) {
 
 __global__ void advance_timer_kernel(prismspf::SimulationTimer* t, double dt) { t->increment(dt); }
 
-static int solve_increment(ppf_handle h, int output_every) {
+// The part of Problem::solve_increment (problem.cc:416-557) that belongs to block b: skipped
+// unless due (PostProcess / NucleationRate only on output increments), the initial condition
+// kept at increment 0 for Primary blocks, else the block's solver; at increment 0 the old ages
+// of its fields start from the current vector.
+static int increment_block(ppf_handle h, int b, bool is_output) {
   const unsigned inc = h->timer.get_increment();
-  for (size_t b = 0; b < h->blocks.size(); ++b) {
-    const ppf_block_desc& d = h->blocks[b].desc;
-    if (d.solve_timing == PPF_POSTPROCESS || d.solve_timing == PPF_NUCLEATION_RATE) {
-      if (output_every <= 0 || inc % (unsigned)output_every != 0) continue;
-    }
-    if (inc == 0 && d.solve_timing == PPF_PRIMARY) {
-      // initial condition is the uploaded current vector (SolverBase::solve at increment 0)
-    } else if (d.solve_type == PPF_EXPLICIT) {
-      int rc = explicit_solve(h, (int)b);
-      if (rc) return rc;
-    } else if (d.solve_type == PPF_CONSTANT) {
-      // constant fields keep their values
-    } else if (d.solve_type == PPF_LINEAR) {
-      int rc = linear_solve(h, (int)b);
-      if (rc && rc != PPF_ERR_NOCONV) return rc;  // non-convergence is logged, not fatal
-    } else if (d.solve_type == PPF_NEWTON) {
-      int rc = newton_solve(h, (int)b);
-      if (rc && rc != PPF_ERR_NOCONV) return rc;  // the reference warns and continues
-    } else {
-      return fail(h, PPF_ERR_UNSUPPORTED, "unknown solve type");
-    }
-    if (inc == 0) {
-      for (int i = 0; i < d.n_fields; ++i) {
-        FieldState& F = h->fields[d.field_indices[i]];
-        for (int a = 0; a < F.n_old; ++a)
-          PPF_CUDA(h, cudaMemcpyAsync(F.old[a], F.cur, sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
-      }
+  const ppf_block_desc& d = h->blocks[b].desc;
+  if ((d.solve_timing == PPF_POSTPROCESS || d.solve_timing == PPF_NUCLEATION_RATE) && !is_output) return PPF_OK;
+  if (inc == 0 && d.solve_timing == PPF_PRIMARY) {
+    // initial condition is the uploaded current vector (SolverBase::solve at increment 0)
+  } else if (d.solve_type == PPF_EXPLICIT) {
+    int rc = explicit_solve(h, b);
+    if (rc) return rc;
+  } else if (d.solve_type == PPF_CONSTANT) {
+    // constant fields keep their values
+  } else if (d.solve_type == PPF_LINEAR) {
+    int rc = linear_solve(h, b);
+    if (rc && rc != PPF_ERR_NOCONV) return rc;  // non-convergence is logged, not fatal
+  } else if (d.solve_type == PPF_NEWTON) {
+    int rc = newton_solve(h, b);
+    if (rc && rc != PPF_ERR_NOCONV) return rc;  // the reference warns and continues
+  } else {
+    return fail(h, PPF_ERR_UNSUPPORTED, "unknown solve type");
+  }
+  if (inc == 0) {
+    for (int i = 0; i < d.n_fields; ++i) {
+      FieldState& F = h->fields[d.field_indices[i]];
+      for (int a = 0; a < F.n_old; ++a)
+        PPF_CUDA(h, cudaMemcpyAsync(F.old[a], F.cur, sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
     }
   }
+  return PPF_OK;
+}
+
+// the end of an increment: age rotation by swap and the timer advance
+static void end_increment(ppf_handle h) {
   rotate(h);
   h->timer.increment(h->dt);
+}
+
+static int solve_increment(ppf_handle h, int output_every) {
+  const unsigned inc = h->timer.get_increment();
+  const bool is_output = output_every > 0 && inc % (unsigned)output_every == 0;
+  for (size_t b = 0; b < h->blocks.size(); ++b) {
+    int rc = increment_block(h, (int)b, is_output);
+    if (rc) return rc;
+  }
+  end_increment(h);
   return PPF_OK;
 }
 
@@ -1125,6 +1140,17 @@ int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
     int rc = solve_increment(h, output_every);
     if (rc) return rc;
   }
+  return check_err(h);
+}
+
+int ppf_increment_block(ppf_handle h, int b, int is_output) {
+  if (!h || b < 0 || b >= (int)h->blocks.size()) return PPF_ERR_ARG;
+  return increment_block(h, b, is_output != 0);
+}
+
+int ppf_end_increment(ppf_handle h) {
+  if (!h) return PPF_ERR_ARG;
+  end_increment(h);
   return check_err(h);
 }
 

@@ -216,6 +216,26 @@ class Problem:
         """Problem::solve: increments from the current one through n_increments."""
         self._check(self.lib.ppf_run(self.h, n_increments, output_every))
 
+    def increment_block(self, b: int, is_output: bool = False):
+        """Block b's part of the current increment (ppf_increment_block)."""
+        self._check(self.lib.ppf_increment_block(self.h, b, int(is_output)))
+
+    def end_increment(self):
+        """Age rotation and timer advance at the end of an increment (ppf_end_increment)."""
+        self._check(self.lib.ppf_end_increment(self.h))
+
+    def device_view(self, f: int, age: int = 0):
+        """The device vector of field f at `age` as a torch CUDA tensor (no copy). Valid until
+        the next age rotation; the caller orders its work with the handle's stream."""
+        import torch
+        ptr = C.c_void_p()
+        self._check(self.lib.ppf_state_device_ptr(self.h, f, age, C.byref(ptr)))
+        n = self.field_length(f)
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr.value, False), "version": 3}
+        return torch.as_tensor(_View(), device="cuda")
+
     def solve_block(self, b: int):
         self._check(self.lib.ppf_solve_block(self.h, b))
 

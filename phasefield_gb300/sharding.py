@@ -1,0 +1,352 @@
+"""One simulation sharded over ranks: slab decomposition of the cell lattice along its slowest
+axis with one ghost cell layer per side, and a halo exchange of node planes after every block.
+
+The reference distributes a simulation with deal.II's MPI partitioner: ghost values are
+updated before each operator evaluation and interface contributions are reduce-added after it
+(`update_ghost_values`, `compress`; src/core/group_solution_handler.cc:293-302,
+src/solvers/mf_operator.cc:24). Here each rank instead computes one extra layer of cells on
+each side of its slab, so every node it owns receives all of its cell contributions locally:
+no reduce-add is needed, only ghost node values after a field changes. Vectors are in lattice
+order with the split axis slowest, so a set of node planes is one contiguous range per
+component and travels without packing. The exchange is the only collective of the data path
+(NCCL on GPUs, gloo on CPUs), plus one logical-or of the non-finite flags per increment, as
+`Problem::solve_increment` does (problem.cc:459-477).
+
+Scope: explicit, constant and post-processing blocks (the explicit increment loop). Linear and
+Newton blocks need distributed inner products and are rejected.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from .problem import Constant, Explicit, NucleationRate, PostProcess, Primary, RectangularMesh
+
+
+@dataclass
+class Slab:
+    """The part of a global mesh one rank computes.
+
+    Owned cells [c0, c1) along `axis`; `ghost_lo` / `ghost_hi` tell whether a ghost cell layer
+    precedes / follows them (always with a neighbour or periodicity). Local node planes along the
+    axis (k = degree): [0, k*ghost_lo) left ghosts, then the owned planes, then the right ghosts.
+    """
+    rank: int
+    size: int
+    axis: int
+    degree: int
+    n_cells: int          # global cells along the axis
+    periodic: bool
+    c0: int
+    c1: int
+    ghost_lo: int
+    ghost_hi: int
+    left: int | None      # neighbour ranks (None at a non-periodic end)
+    right: int | None
+    mesh: RectangularMesh  # the local mesh (ghost cells included)
+    plane_size: int       # nodes per node plane (product over the other axes)
+
+    @property
+    def local_cells(self) -> int:
+        return self.c1 - self.c0 + self.ghost_lo + self.ghost_hi
+
+    @property
+    def local_planes(self) -> int:
+        return self.degree * self.local_cells + 1
+
+    @property
+    def n_nodes(self) -> int:
+        return self.local_planes * self.plane_size
+
+    def global_plane(self, local_plane: int) -> int:
+        """Global plane of a local plane, periodic images folded onto their masters."""
+        g = local_plane - self.degree * self.ghost_lo + self.degree * self.c0
+        return g % (self.degree * self.n_cells) if self.periodic else g
+
+
+    # planes this rank sends: to the left neighbour its first k+1 owned planes (the nodes of
+    # the neighbour's right ghost cell), to the right neighbour its last k owned planes (the
+    # neighbour's left ghost cell without the shared plane, which the neighbour owns)
+    def send_left_planes(self) -> tuple[int, int]:
+        k, lo = self.degree, self.degree * self.ghost_lo
+        return lo, lo + k + 1
+
+    def send_right_planes(self) -> tuple[int, int]:
+        k, lo = self.degree, self.degree * self.ghost_lo
+        end = lo + k * (self.c1 - self.c0)
+        return end - k, end
+
+    def recv_right_planes(self) -> tuple[int, int]:
+        start = self.degree * (self.ghost_lo + self.c1 - self.c0)
+        return start, start + self.degree + 1
+
+    def recv_left_planes(self) -> tuple[int, int]:
+        return 0, self.degree
+
+    def owned_planes(self) -> tuple[int, int]:
+        """Local planes whose values this rank contributes to the global vector."""
+        lo = self.degree * self.ghost_lo
+        hi = lo + self.degree * (self.c1 - self.c0)
+        if not self.periodic and self.right is None:
+            hi += 1  # the last plane of a non-periodic axis
+        return lo, hi
+
+
+def partition(mesh: RectangularMesh, rank: int, size: int) -> Slab:
+    """Slab of `rank` among `size` ranks: cells along the slowest axis split as evenly as
+    possible (at least 2 per rank)."""
+    axis = mesh.dim - 1
+    k = mesh.degree
+    nc = mesh.cells[axis]
+    if size > 1 and nc < 2 * size:
+        raise ValueError(f"{nc} cells along the split axis cannot give {size} ranks 2 cells each")
+    base, extra = divmod(nc, size)
+    counts = [base + (1 if r < extra else 0) for r in range(size)]
+    c0 = sum(counts[:rank])
+    c1 = c0 + counts[rank]
+    periodic = bool(mesh.periodic[axis])
+    left = (rank - 1) % size if (rank > 0 or periodic) else None
+    right = (rank + 1) % size if (rank < size - 1 or periodic) else None
+    ghost_lo = 1 if left is not None else 0
+    ghost_hi = 1 if right is not None else 0
+    h = [mesh.size[d] / mesh.cells[d] for d in range(mesh.dim)]
+    cells_local = list(mesh.cells)
+    cells_local[axis] = c1 - c0 + ghost_lo + ghost_hi
+    lower = list(mesh.lower) + [0.0] * (3 - len(mesh.lower))
+    size_local = list(mesh.size)
+    lower[axis] = mesh.lower[axis] + (c0 - ghost_lo) * h[axis]
+    size_local[axis] = cells_local[axis] * h[axis]
+    per = list(mesh.periodic) + [0] * (3 - len(mesh.periodic))
+    per[axis] = 0  # the exchange carries the split axis' periodicity
+    local = RectangularMesh(dim=mesh.dim, degree=k, size=tuple(size_local),
+                            subdivisions=tuple(cells_local) + (1,) * (3 - mesh.dim), lower=tuple(lower),
+                            global_refinement=0, periodic=tuple(per))
+    plane = 1
+    for d in range(mesh.dim - 1):
+        plane *= mesh.nodes[d]
+    return Slab(rank, size, axis, k, nc, periodic, c0, c1, ghost_lo, ghost_hi, left, right, local, plane)
+
+
+def local_from_global(slab: Slab, v: np.ndarray, ncomp: int = 1) -> np.ndarray:
+    """The local lattice vector (ghosts included) of a global lattice vector. Images of the
+    split axis' periodicity take their masters' values: a slab cannot give the two cells that
+    share a seam node different values there. The serial loop, like the reference, keeps an
+    image's own initial value until the first solve distributes the constraints; the two agree
+    whenever the initial condition is periodic along the split axis."""
+    Ng = v.size // ncomp
+    P = slab.plane_size
+    out = np.empty(ncomp * slab.n_nodes)
+    planes = np.array([slab.global_plane(L) for L in range(slab.local_planes)])
+    for c in range(ncomp):
+        g = v[c * Ng:(c + 1) * Ng].reshape(-1, P)
+        out[c * slab.n_nodes:(c + 1) * slab.n_nodes] = g[planes].ravel()
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# local solvers: the GPU engine of one rank, or (for tests) the oracle
+# ---------------------------------------------------------------------------------------------
+class EngineLocal:
+    """The GPU engine on one rank's slab; its work is queued on torch's current stream so the
+    exchange (torch tensors) and the engine order themselves without host synchronisation."""
+
+    def __init__(self, problem):
+        import torch
+        self.p = problem
+        self.torch = torch
+        # torch's default stream is the legacy stream (handle 0); the engine takes it as
+        # cudaStreamLegacy (1) because a null stream selects the handle's own stream
+        problem.lib.ppf_set_stream(problem.h, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream or 1))
+
+    def vector(self, f: int):
+        return self.p.device_view(f, 0)
+
+    def commit(self, f: int, v):  # views write through
+        pass
+
+    def increment_block(self, b: int, is_output: bool):
+        self.p.increment_block(b, is_output)
+
+    def end_increment(self) -> bool:
+        """True when the increment produced a non-finite value."""
+        from . import capi
+        try:
+            self.p.end_increment()
+        except capi.PPFError as e:
+            if e.code == capi.PPF_ERR_NAN:
+                return True
+            raise
+        return False
+
+    def get(self, f: int, age: int) -> np.ndarray:
+        return self.p.download(f, age=age)
+
+
+class OracleLocal:
+    """The oracle on one rank's slab (test infrastructure for the CPU tests of this module)."""
+
+    def __init__(self, oracle):
+        import torch
+        self.o = oracle
+        self.torch = torch
+
+    def vector(self, f: int):
+        return self.torch.from_numpy(self.o.get(f, 0).copy())
+
+    def commit(self, f: int, v):
+        self.o.set(f, v.numpy(), 0)
+
+    def increment_block(self, b: int, is_output: bool):
+        rc = self.o.increment_block(b, is_output)
+        if rc:
+            raise RuntimeError(f"oracle block {b}: status {rc}")
+
+    def end_increment(self) -> bool:
+        return self.o.end_increment() == 2
+
+    def get(self, f: int, age: int) -> np.ndarray:
+        return self.o.get(f, age)
+
+
+# ---------------------------------------------------------------------------------------------
+# halo exchange and the increment loop
+# ---------------------------------------------------------------------------------------------
+class HaloExchange:
+    """Moves ghost node planes between neighbours with torch.distributed point-to-point
+    messages (or a local copy when a rank is its own neighbour)."""
+
+    def __init__(self, slab: Slab, dist=None):
+        self.slab = slab
+        self.dist = dist
+
+    def _ranges(self, planes: tuple[int, int], ncomp: int):
+        P, N = self.slab.plane_size, self.slab.n_nodes
+        return [(c * N + planes[0] * P, c * N + planes[1] * P) for c in range(ncomp)]
+
+    def exchange(self, v, ncomp: int):
+        """Fills the ghost planes of the local lattice vector v (torch tensor) in place."""
+        s = self.slab
+        torch = __import__("torch")
+        gather = lambda rs: torch.cat([v[a:b] for a, b in rs]) if rs else None  # noqa: E731
+
+        def scatter(rs, buf):
+            o = 0
+            for a, b in rs:
+                v[a:b].copy_(buf[o:o + b - a])
+                o += b - a
+
+        to_left = gather(self._ranges(s.send_left_planes(), ncomp)) if s.left is not None else None
+        to_right = gather(self._ranges(s.send_right_planes(), ncomp)) if s.right is not None else None
+        r_right = self._ranges(s.recv_right_planes(), ncomp) if s.right is not None else []
+        r_left = self._ranges(s.recv_left_planes(), ncomp) if s.left is not None else []
+        from_right = torch.empty(sum(b - a for a, b in r_right), dtype=v.dtype, device=v.device) if r_right else None
+        from_left = torch.empty(sum(b - a for a, b in r_left), dtype=v.dtype, device=v.device) if r_left else None
+        if s.size == 1:
+            if from_right is not None:
+                from_right.copy_(to_left)
+            if from_left is not None:
+                from_left.copy_(to_right)
+        else:
+            # With two periodic ranks both neighbours are the same process: messages carry a
+            # direction tag (gloo), and every rank posts in the same order (leftward sends,
+            # rightward sends, receipts of leftward messages, of rightward messages) so that
+            # backends that pair point-to-point messages by order (NCCL) match them too.
+            LEFTWARD, RIGHTWARD = 1, 2
+            reqs = []
+            if s.left is not None:
+                reqs.append(self.dist.isend(to_left.contiguous(), s.left, tag=LEFTWARD))
+            if s.right is not None:
+                reqs.append(self.dist.isend(to_right.contiguous(), s.right, tag=RIGHTWARD))
+            if s.right is not None:
+                reqs.append(self.dist.irecv(from_right, s.right, tag=LEFTWARD))
+            if s.left is not None:
+                reqs.append(self.dist.irecv(from_left, s.left, tag=RIGHTWARD))
+            for r in reqs:
+                r.wait()
+        if from_right is not None:
+            scatter(r_right, from_right)
+        if from_left is not None:
+            scatter(r_left, from_left)
+
+
+class ShardedExplicit:
+    """The explicit increment loop of one simulation over all ranks: after every block that ran,
+    the ghost planes of its fields are refreshed from the neighbours."""
+
+    def __init__(self, slab: Slab, local, fields, blocks, dist=None):
+        for b in blocks:
+            if b.solve_type not in (Explicit, Constant):
+                raise ValueError("the sharded loop runs explicit, constant and post-processing blocks")
+        self.slab, self.local, self.fields, self.blocks = slab, local, fields, blocks
+        self.halo = HaloExchange(slab, dist)
+        self.dist = dist
+        self.increment = 0
+
+    def _ncomp(self, f: int) -> int:
+        return 1 if self.fields[f].field_type == 0 else self.slab.mesh.dim
+
+    def refresh(self, f: int):
+        v = self.local.vector(f)
+        self.halo.exchange(v, self._ncomp(f))
+        self.local.commit(f, v)
+
+    def run(self, n_increments: int, output_every: int = 0):
+        while self.increment <= n_increments:
+            inc = self.increment
+            is_output = output_every > 0 and inc % output_every == 0
+            for b, blk in enumerate(self.blocks):
+                due = blk.solve_timing not in (PostProcess, NucleationRate) or is_output
+                # at increment 0 a Primary block keeps the initial condition, images included
+                due = due and not (inc == 0 and blk.solve_timing == Primary)
+                self.local.increment_block(b, is_output)
+                if due:
+                    for f in blk.field_indices:
+                        self.refresh(f)
+            bad = self.local.end_increment()
+            if self.dist is not None and self.slab.size > 1:
+                torch = __import__("torch")
+                flag = torch.tensor([1 if bad else 0], dtype=torch.int32)
+                self.dist.all_reduce(flag, op=self.dist.ReduceOp.MAX)
+                bad = bool(flag.item())
+            if bad:
+                raise FloatingPointError(f"non-finite value at increment {inc}")
+            self.increment += 1
+
+    def owned(self, f: int, age: int) -> np.ndarray:
+        """This rank's owned planes of field f (all components, component-major)."""
+        v = self.local.get(f, age)
+        n, P = self.slab.n_nodes, self.slab.plane_size
+        lo, hi = self.slab.owned_planes()
+        return np.concatenate([v[c * n + lo * P:c * n + hi * P] for c in range(self._ncomp(f))])
+
+
+def assemble(slabs: list[Slab], parts: list[np.ndarray], mesh: RectangularMesh, ncomp: int = 1) -> np.ndarray:
+    """The global lattice vector from every rank's owned planes (periodic images of the split
+    axis take their master's values, as distributed constraints leave them)."""
+    nn = mesh.nodes
+    P = slabs[0].plane_size
+    nplanes = nn[-1]
+    out = np.empty(ncomp * nplanes * P)
+    for s, part in zip(slabs, parts):
+        lo, hi = s.owned_planes()
+        cnt = (hi - lo) * P
+        g0 = s.global_plane(lo)
+        for c in range(ncomp):
+            out[c * nplanes * P + g0 * P:c * nplanes * P + g0 * P + cnt] = part[c * cnt:(c + 1) * cnt]
+    if slabs[0].periodic:
+        for c in range(ncomp):
+            base = c * nplanes * P
+            out[base + (nplanes - 1) * P:base + nplanes * P] = out[base:base + P]
+    return out
+
+
+def local_workload(wl, slab: Slab):
+    """A copy of a workload restricted to a rank's slab (mesh and initial condition)."""
+    w = copy.copy(wl)
+    w.mesh = slab.mesh
+    w.initial = {f: local_from_global(slab, v, 1 if wl.fields[f].field_type == 0 else wl.mesh.dim)
+                 for f, v in wl.initial.items()}
+    return w

@@ -1,0 +1,133 @@
+"""The sharded explicit loop (phasefield_gb300/sharding.py) on CPU: slab partitions and halo
+plans are checked exactly; the loop itself runs the oracle on every rank's slab (gloo ranks for
+world size 2) and must reproduce a single oracle run of the whole mesh (1e-12 relative L2: the
+same arithmetic, with node sums in a different order)."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from phasefield_gb300 import sharding as S
+from phasefield_gb300 import workloads as W
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _ch(periodic=True):
+    wl = W.cahn_hilliard_3d(refine=3, degree=2, dim=2, size=8.0, dt=2e-5, periodic=periodic)
+    if periodic:  # a periodic initial condition along the split axis (images = masters)
+        P = wl.mesh.nodes[0]
+        c0 = wl.initial[0].copy()
+        c0[-P:] = c0[:P]
+        wl.initial = {0: c0}
+    return wl
+
+
+def _ac():
+    return W.allen_cahn_2d(refine=4, degree=1, dt=0.01)
+
+
+@pytest.mark.parametrize("size", [1, 2, 3])
+@pytest.mark.parametrize("periodic", [0, 1])
+@pytest.mark.parametrize("degree", [1, 2])
+def test_partition_owns_every_plane_once(size, periodic, degree):
+    mesh = W.RectangularMesh(dim=2, degree=degree, size=(4.0, 8.0), subdivisions=(1, 1, 1), global_refinement=3,
+                             periodic=(0, periodic, 0))
+    slabs = [S.partition(mesh, r, size) for r in range(size)]
+    v = np.random.default_rng(0).uniform(size=int(np.prod(mesh.nodes)))
+    if periodic:  # images carry their master's values
+        P = mesh.nodes[0]
+        v[-P:] = v[:P]
+    parts = []
+    for s in slabs:
+        loc = S.local_from_global(s, v)
+        lo, hi = s.owned_planes()
+        parts.append(loc[lo * s.plane_size:hi * s.plane_size])
+        # what a rank sends is what its neighbour expects in its ghost planes
+        if s.left is not None:
+            nb = slabs[s.left]
+            a, b = s.send_left_planes()
+            c, d = nb.recv_right_planes()
+            assert b - a == d - c
+            assert [s.global_plane(x) for x in range(a, b)] == [nb.global_plane(x) for x in range(c, d)]
+        if s.right is not None:
+            nb = slabs[s.right]
+            a, b = s.send_right_planes()
+            c, d = nb.recv_left_planes()
+            assert b - a == d - c
+            assert [s.global_plane(x) for x in range(a, b)] == [nb.global_plane(x) for x in range(c, d)]
+    assert np.array_equal(S.assemble(slabs, parts, mesh), v)
+
+
+def _run_sharded(wl, rank, size, n, every, dist_=None):
+    from oracle import pyoracle as po
+    slab = S.partition(wl.mesh, rank, size)
+    o = po.Oracle(S.local_workload(wl, slab))
+    for f, v in S.local_workload(wl, slab).initial.items():
+        o.set(f, v, 0)
+    run = S.ShardedExplicit(slab, S.OracleLocal(o), wl.fields, wl.blocks, dist_)
+    run.run(n, every)
+    return slab, run
+
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_single_rank_slab_matches_global(periodic):
+    from oracle import pyoracle as po
+    wl = _ch(periodic)
+    n = 12
+    slab, run = _run_sharded(wl, 0, 1, n, 0)
+    o = po.Oracle(wl)
+    assert o.run(n) == 0
+    for f in (0, 1):
+        got = S.assemble([slab], [run.owned(f, 1)], wl.mesh)
+        assert rel_l2(got, o.get(f, 1)) < 1e-12
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, which, results):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import datetime
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=60))
+    try:
+        wl = _ch(True) if which == "ch" else _ac()
+        n, every = (10, 0) if which == "ch" else (12, 6)
+        slab, run = _run_sharded(wl, rank, world, n, every, dist)
+        fields = [(0, 1), (1, 1)] if which == "ch" else [(0, 1), (1, 0), (2, 0)]
+        results[rank] = [run.owned(f, a) for f, a in fields]
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("which", ["ch", "ac"])
+def test_two_gloo_ranks_match_global(which):
+    from oracle import pyoracle as po
+    world = 2
+    with mp.Manager() as m:
+        results = m.dict()
+        mp.spawn(_worker, args=(world, _free_port(), which, results), nprocs=world, join=True)
+        res = dict(results)
+    wl = _ch(True) if which == "ch" else _ac()
+    slabs = [S.partition(wl.mesh, r, world) for r in range(world)]
+    o = po.Oracle(wl)
+    if which == "ch":
+        assert o.run(10) == 0
+        refs = [o.get(0, 1), o.get(1, 1)]
+    else:
+        assert o.run(12, 6) == 0
+        refs = [o.get(0, 1), o.get(1, 0), o.get(2, 0)]
+    for i, ref in enumerate(refs):
+        got = S.assemble(slabs, [res[r][i] for r in range(world)], wl.mesh)
+        assert rel_l2(got, ref) < 1e-12, i
