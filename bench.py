@@ -441,6 +441,114 @@ def run_ours(args):
     return 0
 
 
+def run_sharded(args):
+    """The same workload as one simulation sharded over the ranks (weak scaling: 64^3 cells per
+    GPU, the GPUs' slabs stacked along z into [0,64]^2 x [0,64N], periodic), the halo planes
+    exchanged after every block with NCCL point-to-point messages (phasefield_gb300/sharding.py).
+    `value` counts the DoF updates of the whole simulation."""
+    import torch
+    import torch.distributed as dist
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from phasefield_gb300 import build as pbuild
+    if rank == 0:
+        pbuild.build()
+    if ws > 1:
+        dist.barrier()
+    from phasefield_gb300 import capi
+    from phasefield_gb300 import sharding as S
+    from phasefield_gb300 import workloads as W
+    lib = capi.load()
+
+    wl = W.cahn_hilliard_3d(**WORKLOAD, subdivisions=(1, 1, ws))
+    wl.mesh.size = (64.0, 64.0, 64.0 * ws)
+    P = wl.mesh.nodes[0] * wl.mesh.nodes[1]
+    c0 = wl.initial[0].copy()
+    c0[-P:] = c0[:P]  # periodic along the split axis
+    wl.initial = {0: c0}
+    Ng = int(np.prod(wl.mesh.nodes))
+    slab = S.partition(wl.mesh, rank, ws)
+    lw = S.local_workload(wl, slab)
+    p = lw.make_problem()
+    drv = S.ShardedExplicit(slab, S.EngineLocal(p), wl.fields, wl.blocks, dist if ws > 1 else None)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    drv.run(0)
+    for _ in range(args.warmup):
+        drv.run(drv.increment)
+    torch.cuda.synchronize()
+    lib.ppf_kernel_stats_reset(p.h)
+    lib.ppf_kernel_timing(p.h, 1)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            evs[k][0].record(stream)
+            drv.run(drv.increment)
+            evs[k][1].record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    total_ms = float(sum(a.elapsed_time(b) for a, b in evs))
+    cell_ms = C.c_double()
+    cell_n, all_n = C.c_longlong(), C.c_longlong()
+    lib.ppf_kernel_stats(p.h, C.byref(cell_ms), C.byref(cell_n), C.byref(all_n))
+    lib.ppf_kernel_timing(p.h, 0)
+    from phasefield_gb300 import replicas
+    max_ms, _ = replicas.aggregate(total_ms, 0, dist if ws > 1 else None, dev)
+    value = 2 * Ng * args.steps / (max_ms * 1e-3)
+    # end to end: each rank's slab through the C ABI with host buffers
+    Nl = p.n_nodes
+    pin = [torch.empty(Nl, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+    for f in (0, 1):
+        p.lib.ppf_download_state(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0)
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for f in (0, 1):
+            assert lib.ppf_upload_state(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0) == 0
+        drv.run(drv.increment)
+        for f in (0, 1):
+            assert lib.ppf_download_state(p.h, f, 1, C.cast(pin[2 + f].data_ptr(), C.POINTER(C.c_double)), 0) == 0
+    torch.cuda.synchronize()
+    e2e_ms, _ = replicas.aggregate((time.perf_counter() - t0) * 1e3, 0, dist if ws > 1 else None, dev)
+    if rank == 0:
+        peak, peak_src = measured_peaks()
+        avg_launch_s = cell_ms.value * 1e-3 / max(cell_n.value, 1)
+        bytes_per_launch = 20 * Nl
+        achieved = bytes_per_launch / avg_launch_s / 1e9
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": {"workload": f"cahn_hilliard_3d explicit sharded: [0,64]^2 x [0,{64 * ws}], "
+                                       f"64x64x{64 * ws} cells, FE_Q(2) on GL points, periodic, dt=1e-4",
+                           "dofs_per_field": Ng, "fields_updated_per_step": 2,
+                           "l2": "flushed between timed steps (256 MiB write)",
+                           "parallelism": f"slab sharding x{ws}, ghost cells + NCCL halo planes"},
+                "e2e": {"value": 2 * Ng * e2e_steps / (e2e_ms * 1e-3), "unit": UNIT,
+                        "h2d_bytes_per_step": 2 * 8 * Nl * ws, "d2h_bytes_per_step": 2 * 8 * Nl * ws},
+                "gpu_launches": int(all_n.value), "clocks": clk.summary(),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": TRAFFIC_PER_LAUNCH * Nl / 129 ** 3,
+                             "traffic_unit": "bytes/launch (scaled from the 64^3 capture)",
+                             "peak_source": peak_src, "kernel": "cell_kernel<CahnHilliard<3,2>>",
+                             "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3},
+                "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+    p.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -448,10 +556,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-extras", action="store_true", help="omit the GMG-CG and ensemble measurements")
+    ap.add_argument("--sharded", action="store_true",
+                    help="run the sharded simulation also on one GPU (more than one GPU always shards)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         return run_reference(args)
+    if args.sharded or dist_env()[0] > 1:
+        return run_sharded(args)
     return run_ours(args)
 
 

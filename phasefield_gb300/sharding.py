@@ -153,6 +153,8 @@ class EngineLocal:
     """The GPU engine on one rank's slab; its work is queued on torch's current stream so the
     exchange (torch tensors) and the engine order themselves without host synchronisation."""
 
+    device = "cuda"
+
     def __init__(self, problem):
         import torch
         self.p = problem
@@ -187,6 +189,8 @@ class EngineLocal:
 
 class OracleLocal:
     """The oracle on one rank's slab (test infrastructure for the CPU tests of this module)."""
+
+    device = "cpu"
 
     def __init__(self, oracle):
         import torch
@@ -308,7 +312,7 @@ class ShardedExplicit:
             bad = self.local.end_increment()
             if self.dist is not None and self.slab.size > 1:
                 torch = __import__("torch")
-                flag = torch.tensor([1 if bad else 0], dtype=torch.int32)
+                flag = torch.tensor([1 if bad else 0], dtype=torch.int32, device=self.local.device)
                 self.dist.all_reduce(flag, op=self.dist.ReduceOp.MAX)
                 bad = bool(flag.item())
             if bad:
