@@ -60,6 +60,12 @@ def test_example_apps_host_syntax(app):
     assert rc == 0, err
 
 
+@needs_gxx
+def test_derivative_test_app_host_syntax():
+    rc, err = host_syntax(ROOT / "tests" / "dropin" / "derivatives")
+    assert rc == 0, err
+
+
 def _reference_app_dirs():
     if not REF_APPS.is_dir():
         return []

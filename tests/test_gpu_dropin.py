@@ -240,3 +240,29 @@ set Model constant n_grains = 12, INT
     assert rel_l2(to_lattice(v1, wl.mesh, "n"), o.get(0, 1)) < 1e-8
     assert rel_l2(to_lattice(v1, wl.mesh, "f_tot"), o.get(2, 0)) < 1e-8
 
+
+def test_derivative_getters_are_exact_on_quadratics(gpu_lib, tmp_path):
+    """Hessian, Hessian diagonal, Laplacian, divergence, curl, symmetric gradient, quadrature
+    point and element volume through the drop-in, on inputs FE_Q(2) represents exactly (two
+    post-processing blocks)."""
+    from phasefield_gb300 import app_build
+    src = ROOT / "tests" / "dropin" / "derivatives"
+    exe = app_build.compile_app(src, tmp_path / "derivatives")
+    (tmp_path / "parameters.prm").write_text("""
+set global refinement = 2
+subsection Rectangular mesh
+  set x size = 2.0
+  set y size = 2.0
+end
+set number steps = 0
+""")
+    r = subprocess.run([str(exe), "-i", "parameters.prm"], cwd=tmp_path, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    v = read_vtu(tmp_path / "solutions" / "solution_0.vtu")
+    x, y = v["Points"][:, 0], v["Points"][:, 1]
+    vol = (2.0 / 4) ** 2
+    expect = {"lap_u": 6.0 + 0 * x, "hess_u": 531.0 + 0 * x, "div_w": 3.0 * x, "curl_w": y - 1.0,
+              "sym_w_xy": 0.5 * (1.0 + y), "x_plus_vol": x + vol}
+    for name, ref in expect.items():
+        assert np.abs(v[name] - ref).max() < 1e-10, name
+
