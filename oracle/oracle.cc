@@ -192,7 +192,24 @@ struct Mesh {
   GL gl;
   DofHandler dh[2];  // [0] scalar FE_Q, [1] FESystem(FE_Q, dim)
   int nnode[3] = {1, 1, 1};
+  // adaptive meshes: `cells` holds coordinates at each cell's own level `lev`; node
+  // positions are integers in units of the node spacing at level `maxlev`
+  bool adaptive = false;
+  std::vector<int> lev;
+  int sub[3] = {1, 1, 1};
+  int maxlev = 0;
+  long E[3] = {1, 1, 1};                  // extent in position units
+  std::vector<std::array<long, 3>> pos;   // node position of every scalar DoF
 };
+
+// cell extent (per-cell on adaptive meshes; the same expression len / (sub * 2^level) as the
+// uniform mesh's h, so a uniform adaptive mesh has bit-identical geometry)
+static inline void cell_h(const Mesh& m, long c, double* h) {
+  for (int d = 0; d < 3; ++d) {
+    if (!m.adaptive || d >= m.dim) h[d] = m.h[d];
+    else h[d] = m.len[d] / (int)((long)m.sub[d] << m.lev[c]);
+  }
+}
 
 // refine_global: children of a cell ordered lexicographically (x fastest), recursively.
 static void build_cells(Mesh& m, const int* subdiv, int refine) {
@@ -422,6 +439,11 @@ struct Problem {
   std::string err;
   int subdiv[3] = {1, 1, 1};
   int refine = 0;
+  // mesh adaptivity (SpatialDiscretization: min/max refinement, remeshing period, criteria)
+  struct Criterion { int field, flags; double vlo, vhi, glo; };
+  int min_level = 0, max_level = 0, period = 0;
+  std::vector<Criterion> criteria;
+  Constraints hanging;  // closed hanging-node lines of the scalar DoFs
   ~Problem();
 };
 
@@ -712,7 +734,13 @@ static bool on_boundary(const Mesh& m, const std::array<int, 4>& L, int bid) {
   return (bid % 2 == 0) ? L[dir] == 0 : L[dir] == m.nnode[dir] - 1;
 }
 
+static void make_field_constraints_adaptive(Problem& P, int f);
+
 static void make_field_constraints(Problem& P, int f) {
+  if (P.m.adaptive) {
+    make_field_constraints_adaptive(P, f);
+    return;
+  }
   Field& F = P.fields[f];
   const int which = F.rank;
   const DofHandler& d = P.m.dh[which];
@@ -766,12 +794,12 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
       } else vec = F.old[age - 1].data();
       slots.push_back({f, age, fl, vec, &F.cons, cread, F.rank == 0 ? 1 : dim});
     }
-  const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
   const GL& gl = m.gl;
   // colouring for thread safety of the scatter: cell parity per axis
   int ncol = 1 << dim;
   bool serial = false;
   for (int d = 0; d < dim; ++d) if (m.periodic[d] && (m.nc[d] % 2)) serial = true;
+  if (m.adaptive) serial = true;  // cells of different levels share DoFs across parity colours
   std::vector<std::vector<long>> colours(ncol);
   for (long c = 0; c < m.ncells; ++c) {
     auto& cc = m.cells[c];
@@ -794,6 +822,9 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
       for (long ci = 0; ci < ncl; ++ci) {
         const long c = cl[ci];
         const auto& cc = m.cells[c];
+        double hc[3];
+        cell_h(m, c, hc);
+        const double detJ = hc[0] * hc[1] * (dim == 3 ? hc[2] : 1.0);
         // gather + evaluate each dependency
         for (size_t s = 0; s < slots.size(); ++s) {
           const DepSlot& S = slots[s];
@@ -821,7 +852,7 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
                 double acc = 0.0;
                 int base = l - idx[d] * stride[d];
                 for (int j = 0; j < n; ++j) acc += gl.D[idx[d]][j] * u[base + j * stride[d]];
-                grads[((s * 3 + comp) * 3 + d) * nloc + l] = acc / m.h[d];
+                grads[((s * 3 + comp) * 3 + d) * nloc + l] = acc / hc[d];
               }
             }
           }
@@ -844,9 +875,9 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
           q.out_val = &ov[(size_t)l * nf * 3]; q.out_grad = &og[(size_t)l * nf * 9];
           q.out_flags = oflag.data(); q.nf = nf;
           int a = l % n, b = (l / n) % n, e = l / (n * n);
-          q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * m.h[0];
-          q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * m.h[1];
-          q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * m.h[2] : 0.0;
+          q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * hc[0];
+          q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * hc[1];
+          q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * hc[2] : 0.0;
           q.vol = detJ;
           cb(P, q, B.id, lhs);
         }
@@ -873,7 +904,7 @@ static void cell_loop(Problem& P, const Block& B, bool lhs, const std::vector<co
                     double wqq = gl.w[aq] * gl.w[bq] * (dim == 3 ? gl.w[eq] : 1.0);
                     acc += og[(((size_t)lq * nf + f) * 3 + comp) * 3 + d] * gl.D[qd][idx[d]] * wqq;
                   }
-                  r += acc * detJ / m.h[d];
+                  r += acc * detJ / hc[d];
                 }
               }
               res[comp * nloc + l] = r;
@@ -911,7 +942,6 @@ static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
   const int ncomp = F0.rank == 0 ? 1 : dim;
   const DofHandler& dh = m.dh[ncomp == 1 ? 0 : 1];
   const int nf = (int)P.fields.size();
-  const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
   const GL& gl = m.gl;
   Callback cb = callback_for(P.model);
   diag.assign(dh.ndofs, 0.0);
@@ -921,6 +951,9 @@ static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
   std::vector<double> grads((size_t)3 * 3 * nloc), vals((size_t)3 * nloc), cdiag((size_t)3 * nloc);
   for (long c = 0; c < m.ncells; ++c) {
     const auto& cc = m.cells[c];
+    double hc[3];
+    cell_h(m, c, hc);
+    const double detJ = hc[0] * hc[1] * (dim == 3 ? hc[2] : 1.0);
     for (int i = 0; i < nloc; ++i) {
       // probe: identity at node i for every component
       for (int comp = 0; comp < ncomp; ++comp)
@@ -934,7 +967,7 @@ static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
             double acc = 0.0;
             int base = l - idx[d] * stride[d];
             for (int j = 0; j < n; ++j) acc += gl.D[idx[d]][j] * vals[comp * nloc + base + j * stride[d]];
-            grads[(comp * 3 + d) * nloc + l] = acc / m.h[d];
+            grads[(comp * 3 + d) * nloc + l] = acc / hc[d];
           }
         }
       std::fill(ov.begin(), ov.end(), 0.0);
@@ -951,9 +984,9 @@ static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
         q.out_val = &ov[(size_t)l * nf * 3]; q.out_grad = &og[(size_t)l * nf * 9];
         q.out_flags = oflag.data(); q.nf = nf;
         int a = l % n, b = (l / n) % n, e = l / (n * n);
-        q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * m.h[0];
-        q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * m.h[1];
-        q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * m.h[2] : 0.0;
+        q.x[0] = m.lo[0] + (cc[0] + gl.x[a]) * hc[0];
+        q.x[1] = m.lo[1] + (cc[1] + gl.x[b]) * hc[1];
+        q.x[2] = dim == 3 ? m.lo[2] + (cc[2] + gl.x[e]) * hc[2] : 0.0;
         q.vol = detJ;
         cb(P, q, B.id, true);
       }
@@ -975,7 +1008,7 @@ static void diag_loop(Problem& P, const Block& B, std::vector<double>& diag) {
               double wqq = gl.w[aq] * gl.w[bq] * (dim == 3 ? gl.w[eq] : 1.0);
               acc += og[(((size_t)lq * nf + f0) * 3 + comp) * 3 + d] * gl.D[qd][idx[d]] * wqq;
             }
-            r += acc * detJ / m.h[d];
+            r += acc * detJ / hc[d];
           }
         cdiag[comp * nloc + i] = r;
       }
@@ -1001,12 +1034,27 @@ static void compute_invm(Problem& P) {
     DofHandler& d = m.dh[which];
     Constraints& C = P.generic[which];
     C.reinit(d.ndofs);
-    make_periodic(m, which, C);
+    if (!m.adaptive) {
+      make_periodic(m, which, C);
+    } else {
+      // adaptive meshes merge periodic images; hanging nodes are condensed because deal.II's
+      // MatrixFree resolves them from the mesh (its hanging-node masks) whatever the generic
+      // constraints hold
+      const long N = (long)m.pos.size();
+      for (int comp = 0; comp < d.ncomp; ++comp)
+        for (long p = 0; p < N; ++p) {
+          if (!P.hanging.is_constrained(p)) continue;
+          C.add_line(comp * N + p);
+          for (auto& e : P.hanging.entries[p]) C.entries[comp * N + p].push_back({comp * N + e.first, e.second});
+        }
+    }
     C.close();
     P.jxw[which].assign(d.ndofs, 0.0);
     const int dim = m.dim, n = m.n, nloc = m.nloc;
-    const double detJ = m.h[0] * m.h[1] * (dim == 3 ? m.h[2] : 1.0);
-    for (long c = 0; c < m.ncells; ++c)
+    for (long c = 0; c < m.ncells; ++c) {
+      double hc[3];
+      cell_h(m, c, hc);
+      const double detJ = hc[0] * hc[1] * (dim == 3 ? hc[2] : 1.0);
       for (int comp = 0; comp < d.ncomp; ++comp)
         for (int l = 0; l < nloc; ++l) {
           int a = l % n, b = (l / n) % n, e = l / (n * n);
@@ -1015,6 +1063,7 @@ static void compute_invm(Problem& P) {
           if (C.is_constrained(g)) { for (auto& e2 : C.entries[g]) P.jxw[which][e2.first] += e2.second * r; }
           else P.jxw[which][g] += r;
         }
+    }
     P.invm[which].resize(d.ndofs);
     P.invm_sqrt[which].resize(d.ndofs);
     for (long i = 0; i < d.ndofs; ++i) {
@@ -1606,6 +1655,465 @@ void finalize_fields(Problem& P) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Adaptive meshes: RefinementManager (src/core/refinement_manager.cc:42-439) with deal.II's
+// refinement smoothing, hanging-node constraints and SolutionTransfer, restated by brute
+// force for small meshes (every geometric query scans all cells).
+//
+//  * A cell is (level l, integer coordinates i at level l); with M the maximum refinement
+//    level it spans [i k, (i+1) k] 2^(M-l) in node units. Degrees 1 and 2: their Gauss-Lobatto
+//    points (0, 1 / 0, 1/2, 1) nest under bisection, so node positions are the integers
+//    (i k + a) 2^(M-l). Periodic positions wrap modulo the extent: a periodic image is the
+//    same DoF as its master (the state deal.II's periodicity constraints distribute).
+//  * Active cells are kept in tree order: coarse cells lexicographically (x fastest), the
+//    children of a refined cell depth-first in lexicographic child order. DoFs are numbered
+//    by first touch over that order, cell nodes lexicographically; vector fields are
+//    component-major.
+//  * A DoF is hanging when an active cell contains it without having it as a node; its line
+//    is that cell's interpolant, weights prod_d L_a(xi_d), closed over chains
+//    (DoFTools::make_hanging_node_constraints + AffineConstraints::close,
+//    constraint_manager.cc:288-294). Dirichlet lines are added afterwards for boundary DoFs
+//    that are not already constrained.
+//  * The lumped mass condenses hanging nodes (hanging rows get invM = 0): the reference's
+//    generic constraints hold periodicity only (constraint_manager.cc:156-170), but deal.II's
+//    MatrixFree resolves hanging nodes from the mesh itself, so integrate_scatter in
+//    InvMManager::compute_local_scalar (invm_manager.h:173-190) condenses them.
+//  * Marking (refinement_manager.cc:161-363): a cell is flagged for refinement when any
+//    criterion holds at any of its quadrature points (value in the open range; gradient
+//    magnitude above the bound; vector fields by their l2 norms, the gradient of a vector
+//    field compared with the value range as the reference does), below max refinement;
+//    otherwise it is flagged for coarsening above min refinement.
+//  * Smoothing, iterated to a fixed point (each rule only moves flags towards refinement,
+//    so the result does not depend on the visiting order): coarsening only of complete
+//    families of active, coarsening-flagged siblings; 2:1 balance between every two cells
+//    that touch (share at least a vertex) after the change; an unrefined cell whose face
+//    neighbours are mostly refined (finer, or flagged for refinement) is refined
+//    (smoothing_on_refinement = limit_level_difference_at_vertices +
+//    eliminate_unrefined_islands, triangulation_manager.cc:32-38).
+//  * Transfer (group_solution_handler.cc:248-288): a node that existed before keeps its old
+//    value; a new node takes the interpolant of the first old cell (in old order) that
+//    contains it; then the new constraints are distributed on every age.
+// ---------------------------------------------------------------------------------------
+enum { REFINE_VALUE = 1, REFINE_GRADIENT = 2 };
+
+static double lagrange_exact(int k, int a, double xi) {
+  static const double q1[2] = {0.0, 1.0};
+  static const double q2[3] = {0.0, 0.5, 1.0};
+  const double* x = k == 1 ? q1 : q2;
+  double v = 1.0;
+  for (int b = 0; b <= k; ++b)
+    if (b != a) v *= (xi - x[b]) / (x[a] - x[b]);
+  return v;
+}
+
+static long span_w(const Mesh& m, long c) { return (long)m.k << (m.maxlev - m.lev[c]); }
+static long span_lo(const Mesh& m, long c, int d) { return ((long)m.cells[c][d] * m.k) << (m.maxlev - m.lev[c]); }
+
+static std::array<long, 3> node_position(const Mesh& m, long c, int l) {
+  const int n = m.n;
+  const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
+  std::array<long, 3> P{0, 0, 0};
+  for (int d = 0; d < m.dim; ++d) {
+    long p = ((long)m.cells[c][d] * m.k + idx[d]) << (m.maxlev - m.lev[c]);
+    if (m.periodic[d] && p == m.E[d]) p = 0;
+    P[d] = p;
+  }
+  return P;
+}
+
+// offsets of position P inside the closure of cell c (periodic images unwrapped)
+static bool local_offset(const Mesh& m, long c, const std::array<long, 3>& P, long* off) {
+  const long w = span_w(m, c);
+  for (int d = 0; d < m.dim; ++d) {
+    const long lo = span_lo(m, c, d);
+    long x = P[d];
+    if (m.periodic[d] && x == 0 && lo + w == m.E[d]) x = m.E[d];
+    if (x < lo || x > lo + w) return false;
+    off[d] = x - lo;
+  }
+  return true;
+}
+
+static void adaptive_dofs(Mesh& m) {
+  const int dim = m.dim, nloc = m.nloc;
+  std::map<std::array<long, 3>, long> id;
+  m.pos.clear();
+  std::vector<long> cd((size_t)m.ncells * nloc);
+  for (long c = 0; c < m.ncells; ++c)
+    for (int l = 0; l < nloc; ++l) {
+      const auto P = node_position(m, c, l);
+      auto it = id.find(P);
+      if (it == id.end()) {
+        it = id.emplace(P, (long)m.pos.size()).first;
+        m.pos.push_back(P);
+      }
+      cd[(size_t)c * nloc + l] = it->second;
+    }
+  const long N = (long)m.pos.size();
+  for (int which = 0; which < 2; ++which) {
+    DofHandler& d = m.dh[which];
+    d.ncomp = which == 0 ? 1 : dim;
+    d.ndofs = N * d.ncomp;
+    d.cell_dofs.assign((size_t)m.ncells * d.ncomp * nloc, 0);
+    d.lattice.assign(d.ndofs, {0, 0, 0, 0});
+    for (long c = 0; c < m.ncells; ++c)
+      for (int comp = 0; comp < d.ncomp; ++comp)
+        for (int l = 0; l < nloc; ++l) d.cell_dofs[((size_t)c * d.ncomp + comp) * nloc + l] = comp * N + cd[(size_t)c * nloc + l];
+    for (int comp = 0; comp < d.ncomp; ++comp)
+      for (long i = 0; i < N; ++i)
+        d.lattice[comp * N + i] = {(int)m.pos[i][0], (int)m.pos[i][1], (int)m.pos[i][2], comp};
+  }
+}
+
+// hanging-node lines of the scalar DoFs, closed, entries in ascending master order
+static void hanging_lines(Problem& P) {
+  const Mesh& m = P.m;
+  const long N = (long)m.pos.size();
+  const int n = m.n, nloc = m.nloc;
+  Constraints& H = P.hanging;
+  H.reinit(N);
+  for (long p = 0; p < N; ++p) {
+    for (long c = 0; c < m.ncells; ++c) {
+      long off[3] = {0, 0, 0};
+      if (!local_offset(m, c, m.pos[p], off)) continue;
+      const long step = 1L << (m.maxlev - m.lev[c]);
+      bool node = true;
+      for (int d = 0; d < m.dim; ++d) node &= (off[d] % step) == 0;
+      if (node) continue;
+      const double w = (double)span_w(m, c);
+      H.add_line(p);
+      for (int l = 0; l < nloc; ++l) {
+        const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
+        double wl = 1.0;
+        for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(m.k, idx[d], off[d] / w);
+        if (wl != 0.0) H.entries[p].push_back({m.dh[0].cell_dofs[(size_t)c * nloc + l], wl});
+      }
+      break;
+    }
+  }
+  H.close();
+  for (auto& e : H.entries) std::sort(e.begin(), e.end());
+}
+
+static bool on_boundary_pos(const Mesh& m, const std::array<long, 3>& P, int bid) {
+  const int d = bid / 2;
+  if (d >= m.dim || m.periodic[d]) return false;
+  return (bid % 2 == 0) ? P[d] == 0 : P[d] == m.E[d];
+}
+
+static void make_field_constraints_adaptive(Problem& P, int f) {
+  Field& F = P.fields[f];
+  const Mesh& m = P.m;
+  const DofHandler& d = m.dh[F.rank];
+  const long N = (long)m.pos.size();
+  F.cons.reinit(d.ndofs);
+  for (int comp = 0; comp < d.ncomp; ++comp)
+    for (long p = 0; p < N; ++p) {
+      if (!P.hanging.is_constrained(p)) continue;
+      const long i = comp * N + p;
+      F.cons.add_line(i);
+      for (auto& e : P.hanging.entries[p]) F.cons.entries[i].push_back({comp * N + e.first, e.second});
+    }
+  for (int comp = 0; comp < d.ncomp; ++comp)
+    for (int bid = 0; bid < 2 * m.dim; ++bid) {
+      if (!F.dir_on[comp][bid]) continue;
+      for (long p = 0; p < N; ++p) {
+        const long i = comp * N + p;
+        if (!on_boundary_pos(m, m.pos[p], bid) || F.cons.is_constrained(i)) continue;
+        F.cons.add_line(i);
+        F.cons.inhom[i] = F.dir_val[comp][bid];
+      }
+    }
+  F.cons.close();
+}
+
+// per-cell flags from the refinement criteria: 1 refine, -1 coarsen, 0 keep
+static std::vector<int> mark_cells(Problem& P) {
+  const Mesh& m = P.m;
+  const int dim = m.dim, n = m.n, nloc = m.nloc;
+  std::vector<int> flag(m.ncells, 0);
+  std::vector<double> u((size_t)3 * nloc);
+  for (long c = 0; c < m.ncells; ++c) {
+    double hc[3];
+    cell_h(m, c, hc);
+    bool refine = false;
+    for (const auto& K : P.criteria) {
+      const Field& F = P.fields[K.field];
+      const int ncomp = F.rank == 0 ? 1 : dim;
+      const DofHandler& dh = m.dh[F.rank];
+      for (int comp = 0; comp < ncomp; ++comp)
+        for (int l = 0; l < nloc; ++l) u[comp * nloc + l] = F.cur[dh.cell_dofs[((size_t)c * ncomp + comp) * nloc + l]];
+      for (int l = 0; l < nloc && !refine; ++l) {
+        if (K.flags & REFINE_VALUE) {
+          double v;
+          if (ncomp == 1) v = u[l];
+          else {
+            double s2 = 0.0;
+            for (int comp = 0; comp < ncomp; ++comp) s2 += u[comp * nloc + l] * u[comp * nloc + l];
+            v = std::sqrt(s2);
+          }
+          if (v > K.vlo && v < K.vhi) refine = true;
+        }
+        if (!refine && (K.flags & REFINE_GRADIENT)) {
+          const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
+          const int stride[3] = {1, n, n * n};
+          double mag2 = 0.0;
+          for (int comp = 0; comp < ncomp; ++comp) {
+            double g2 = 0.0;
+            for (int d = 0; d < dim; ++d) {
+              const int base = l - idx[d] * stride[d];
+              double acc = 0.0;
+              for (int j = 0; j < n; ++j) acc += m.gl.D[idx[d]][j] * u[comp * nloc + base + j * stride[d]];
+              const double g = acc / hc[d];
+              g2 += g * g;
+            }
+            if (ncomp == 1) mag2 = g2;
+            else {
+              const double gm = std::sqrt(g2);
+              mag2 += gm * gm;
+            }
+          }
+          const double mag = std::sqrt(mag2);
+          if (ncomp == 1 ? mag > K.glo : (mag > K.vlo && mag < K.vhi)) refine = true;
+        }
+      }
+      if (refine) break;
+    }
+    if (refine) flag[c] = m.lev[c] < P.max_level ? 1 : 0;
+    else flag[c] = m.lev[c] > P.min_level ? -1 : 0;
+  }
+  return flag;
+}
+
+static bool overlap(long a0, long a1, long b0, long b1) { return a0 <= b1 && b0 <= a1; }
+static bool open_overlap(long a0, long a1, long b0, long b1) { return a0 < b1 && b0 < a1; }
+
+// closures of cells a and b intersect (periodic directions wrap)
+static bool cells_touch(const Mesh& m, long a, long b) {
+  const long wa = span_w(m, a), wb = span_w(m, b);
+  for (int d = 0; d < m.dim; ++d) {
+    const long a0 = span_lo(m, a, d), b0 = span_lo(m, b, d);
+    bool hit = overlap(a0, a0 + wa, b0, b0 + wb);
+    if (!hit && m.periodic[d])
+      hit = overlap(a0, a0 + wa, b0 + m.E[d], b0 + wb + m.E[d]) || overlap(a0, a0 + wa, b0 - m.E[d], b0 + wb - m.E[d]);
+    if (!hit) return false;
+  }
+  return true;
+}
+
+// b lies across face (dir, side) of a: touches that face and overlaps it with positive measure
+static bool across_face(const Mesh& m, long a, long b, int dir, int side) {
+  const long wa = span_w(m, a), wb = span_w(m, b);
+  for (int d = 0; d < m.dim; ++d) {
+    const long a0 = span_lo(m, a, d), b0 = span_lo(m, b, d);
+    bool ok = false;
+    for (int sh = -1; sh <= 1 && !ok; ++sh) {
+      if (sh != 0 && !m.periodic[d]) continue;
+      const long s0 = b0 + sh * m.E[d];
+      if (d == dir) ok = side ? s0 == a0 + wa : s0 + wb == a0;
+      else ok = open_overlap(a0, a0 + wa, s0, s0 + wb);
+    }
+    if (!ok) return false;
+  }
+  return true;
+}
+
+typedef std::array<int, 4> CellKey;  // level, i, j, k
+
+static CellKey parent_key(const Mesh& m, long c) {
+  return {m.lev[c] - 1, m.cells[c][0] >> 1, m.cells[c][1] >> 1, m.cells[c][2] >> 1};
+}
+
+// refinement smoothing of the flags to a fixed point
+static void smooth_flags(Problem& P, std::vector<int>& flag) {
+  const Mesh& m = P.m;
+  const long nc = m.ncells;
+  const int nchild = 1 << m.dim;
+  for (;;) {
+    bool changed = false;
+    std::map<CellKey, int> fam;
+    for (long c = 0; c < nc; ++c)
+      if (flag[c] == -1) fam[parent_key(m, c)]++;
+    for (long c = 0; c < nc; ++c)
+      if (flag[c] == -1 && fam[parent_key(m, c)] != nchild) { flag[c] = 0; changed = true; }
+    for (long a = 0; a < nc; ++a) {
+      const int ta = m.lev[a] + (flag[a] == 1) - (flag[a] == -1);
+      for (long b = 0; b < nc; ++b) {
+        if (a == b) continue;
+        const int tb = m.lev[b] + (flag[b] == 1) - (flag[b] == -1);
+        if (ta <= tb + 1 || !cells_touch(m, a, b)) continue;
+        const int nf = flag[b] == -1 ? 0 : 1;
+        if (nf != flag[b]) {
+          flag[b] = nf;
+          changed = true;
+        }
+      }
+    }
+    for (long a = 0; a < nc; ++a) {
+      if (flag[a] == 1) continue;
+      int refined = 0, unrefined = 0;
+      for (int dir = 0; dir < m.dim; ++dir)
+        for (int side = 0; side < 2; ++side) {
+          bool any = false, fine = false;
+          for (long b = 0; b < nc; ++b) {
+            if (b == a || !across_face(m, a, b, dir, side)) continue;
+            any = true;
+            if (m.lev[b] > m.lev[a] || (m.lev[b] == m.lev[a] && flag[b] == 1)) fine = true;
+          }
+          if (!any) continue;  // domain boundary
+          if (fine) ++refined;
+          else ++unrefined;
+        }
+      if (refined > unrefined && m.lev[a] < P.max_level) {
+        flag[a] = 1;
+        changed = true;
+      }
+    }
+    if (!changed) break;
+  }
+}
+
+static void tree_order(const Mesh& m, const std::map<CellKey, CellKey>& act, int l, int i, int j, int k,
+                       std::vector<CellKey>& out) {
+  auto it = act.find(CellKey{l, i, j, k});
+  if (it != act.end()) {
+    out.push_back(it->second);
+    return;
+  }
+  if (l >= m.maxlev) return;
+  for (int ch = 0; ch < (1 << m.dim); ++ch)
+    tree_order(m, act, l + 1, 2 * i + (ch & 1), 2 * j + ((ch >> 1) & 1), m.dim == 3 ? 2 * k + ((ch >> 2) & 1) : 0, out);
+}
+
+static void set_cells(Mesh& m, const std::vector<CellKey>& cells) {
+  std::map<CellKey, CellKey> act;
+  for (auto& c : cells) act[c] = c;
+  std::vector<CellKey> ordered;
+  for (int k = 0; k < (m.dim == 3 ? m.sub[2] : 1); ++k)
+    for (int j = 0; j < m.sub[1]; ++j)
+      for (int i = 0; i < m.sub[0]; ++i) tree_order(m, act, 0, i, j, k, ordered);
+  m.ncells = (long)ordered.size();
+  m.cells.resize(m.ncells);
+  m.lev.resize(m.ncells);
+  for (long c = 0; c < m.ncells; ++c) {
+    m.lev[c] = ordered[c][0];
+    m.cells[c] = {ordered[c][1], ordered[c][2], ordered[c][3]};
+  }
+}
+
+static void rebuild_mesh(Problem& P) {
+  adaptive_dofs(P.m);
+  hanging_lines(P);
+  compute_invm(P);
+  for (size_t f = 0; f < P.fields.size(); ++f) make_field_constraints(P, (int)f);
+}
+
+// one remesh pass (RefinementManager::do_adaptive_refinement): mark, smooth, refine/coarsen,
+// renumber, transfer every stored age, distribute the new constraints
+static void remesh(Problem& P) {
+  Mesh& m = P.m;
+  std::vector<int> flag = mark_cells(P);
+  smooth_flags(P, flag);
+  std::vector<CellKey> nxt;
+  std::map<CellKey, int> parents_done;
+  for (long c = 0; c < m.ncells; ++c) {
+    const int l = m.lev[c];
+    const auto& x = m.cells[c];
+    if (flag[c] == 1) {
+      for (int ch = 0; ch < (1 << m.dim); ++ch)
+        nxt.push_back({l + 1, 2 * x[0] + (ch & 1), 2 * x[1] + ((ch >> 1) & 1), m.dim == 3 ? 2 * x[2] + ((ch >> 2) & 1) : 0});
+    } else if (flag[c] == -1) {
+      if (parents_done[parent_key(m, c)]++ == 0) nxt.push_back({l - 1, x[0] >> 1, x[1] >> 1, x[2] >> 1});
+    } else {
+      nxt.push_back({l, x[0], x[1], x[2]});
+    }
+  }
+  const Mesh old = m;
+  set_cells(m, nxt);
+  rebuild_mesh(P);
+  // transfer plan per new scalar DoF: (old dof, weight) entries
+  std::map<std::array<long, 3>, long> oldpos;
+  for (long i = 0; i < (long)old.pos.size(); ++i) oldpos[old.pos[i]] = i;
+  const long N = (long)m.pos.size(), No = (long)old.pos.size();
+  const int n = m.n, nloc = m.nloc;
+  std::vector<std::vector<std::pair<long, double>>> plan(N);
+  for (long p = 0; p < N; ++p) {
+    auto it = oldpos.find(m.pos[p]);
+    if (it != oldpos.end()) {
+      plan[p].push_back({it->second, 1.0});
+      continue;
+    }
+    for (long c = 0; c < old.ncells; ++c) {
+      long off[3] = {0, 0, 0};
+      if (!local_offset(old, c, m.pos[p], off)) continue;
+      const double w = (double)span_w(old, c);
+      for (int l = 0; l < nloc; ++l) {
+        const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
+        double wl = 1.0;
+        for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(m.k, idx[d], off[d] / w);
+        if (wl != 0.0) plan[p].push_back({old.dh[0].cell_dofs[(size_t)c * nloc + l], wl});
+      }
+      break;
+    }
+  }
+  for (auto& F : P.fields) {
+    const int ncomp = F.rank == 0 ? 1 : m.dim;
+    auto move = [&](std::vector<double>& v) {
+      if (v.empty()) return;
+      std::vector<double> nv((size_t)ncomp * N, 0.0);
+      for (int comp = 0; comp < ncomp; ++comp)
+        for (long p = 0; p < N; ++p) {
+          double s = 0.0;
+          for (auto& e : plan[p]) s += e.second * v[comp * No + e.first];
+          nv[comp * N + p] = s;
+        }
+      distribute(F.cons, nv.data());
+      v.swap(nv);
+    };
+    move(F.cur);
+    for (int a = 0; a < F.n_old; ++a) move(F.old[a]);
+  }
+}
+
+static int enable_adaptivity(Problem& P, int min_level, int max_level, int period) {
+  Mesh& m = P.m;
+  if (m.dim < 2 || m.k > 2 || min_level < 0 || max_level < P.refine || min_level > P.refine || max_level > 18)
+    return -1;
+  for (int d = 0; d < m.dim; ++d)
+    if (m.periodic[d] && ((long)P.subdiv[d] << min_level) < 2) return -1;
+  m.adaptive = true;
+  m.maxlev = max_level;
+  for (int d = 0; d < 3; ++d) {
+    m.sub[d] = P.subdiv[d];
+    m.E[d] = d < m.dim ? ((long)m.sub[d] * m.k) << max_level : 1;
+  }
+  m.lev.assign(m.ncells, P.refine);
+  std::vector<CellKey> cells;
+  for (long c = 0; c < m.ncells; ++c) cells.push_back({P.refine, m.cells[c][0], m.cells[c][1], m.cells[c][2]});
+  set_cells(m, cells);
+  P.min_level = min_level;
+  P.max_level = max_level;
+  P.period = period;
+  rebuild_mesh(P);
+  return 0;
+}
+
+// the refinement step of Problem::solve_increment (problem.cc:488-499): at increment 0 up to
+// max - min passes, stopping when the DoF count no longer changes; later every `period`
+// increments one pass
+static void remesh_if_due(Problem& P) {
+  if (!P.m.adaptive) return;
+  if (P.increment == 0) {
+    for (int r = 0; r < P.max_level - P.min_level; ++r) {
+      const size_t n0 = P.m.pos.size();
+      remesh(P);
+      if (P.m.pos.size() == n0) break;
+    }
+  } else if (P.period > 0 && P.increment % (unsigned)P.period == 0) {
+    remesh(P);
+  }
+}
+
 }  // namespace orc
 
 using namespace orc;
@@ -1786,10 +2294,77 @@ int orc_run(void* h, unsigned n_increments, int output_every) {
       const int rc = orc_increment_block(h, (int)b, is_output);
       if (rc) return rc;
     }
+    remesh_if_due(*P);
     const int rc = orc_end_increment(h);
     if (rc) return rc;
   }
   return 0;
+}
+
+// ---- adaptive meshes -------------------------------------------------------------------
+// Mesh adaptivity (SpatialDiscretization::has_adaptivity): call after the fields are added
+// and before orc_finalize. criteria: n entries of (field, flags 1 value | 2 gradient, value
+// lower, value upper, gradient lower). The mesh starts uniform at the global refinement.
+int orc_set_adaptivity(void* h, int min_level, int max_level, int period, int n, const int* fields,
+                       const int* flags, const double* vlo, const double* vhi, const double* glo) {
+  auto* P = (Problem*)h;
+  P->criteria.clear();
+  for (int i = 0; i < n; ++i) P->criteria.push_back({fields[i], flags[i], vlo[i], vhi[i], glo[i]});
+  return enable_adaptivity(*P, min_level, max_level, period);
+}
+
+// one remesh pass (mark, smooth, refine/coarsen, transfer)
+int orc_adapt(void* h) {
+  auto* P = (Problem*)h;
+  if (!P->m.adaptive) return -1;
+  remesh(*P);
+  return 0;
+}
+
+// the refinement step of the current increment, as orc_run does it after the blocks
+int orc_remesh_if_due(void* h) {
+  remesh_if_due(*(Problem*)h);
+  return 0;
+}
+
+long orc_n_nodes(void* h) {
+  auto* P = (Problem*)h;
+  return P->m.adaptive ? (long)P->m.pos.size() : P->m.dh[0].ndofs;
+}
+
+// active cells in tree order: level, i, j, k per cell
+void orc_cells(void* h, int* out) {
+  auto& m = ((Problem*)h)->m;
+  for (long c = 0; c < m.ncells; ++c) {
+    out[c * 4] = m.adaptive ? m.lev[c] : ((Problem*)h)->refine;
+    for (int d = 0; d < 3; ++d) out[c * 4 + 1 + d] = m.cells[c][d];
+  }
+}
+
+// coordinates of the scalar DoFs of an adaptive mesh: lower + size * (position / extent)
+void orc_node_points(void* h, double* out) {
+  auto& m = ((Problem*)h)->m;
+  for (size_t i = 0; i < m.pos.size(); ++i)
+    for (int d = 0; d < 3; ++d) out[i * 3 + d] = d < m.dim ? m.lo[d] + m.len[d] * ((double)m.pos[i][d] / (double)m.E[d]) : 0.0;
+}
+
+// closed hanging-node lines of the scalar DoFs: per DoF the entry count (0 when free), then
+// the entries (master, weight) in ascending master order. Returns the total entry count;
+// call with null outputs to size them.
+long orc_hanging(void* h, int* count, long* master, double* weight) {
+  auto& H = ((Problem*)h)->hanging;
+  long t = 0;
+  for (size_t i = 0; i < H.constrained.size(); ++i) {
+    const long c = H.constrained[i] ? (long)H.entries[i].size() : 0;
+    if (count) count[i] = (int)c;
+    if (H.constrained[i])
+      for (auto& e : H.entries[i]) {
+        if (master) master[t] = e.first;
+        if (weight) weight[t] = e.second;
+        ++t;
+      }
+  }
+  return t;
 }
 
 // Operator apply of block b: which = 0 rhs (plain read), 1 lhs (src read with constraints).

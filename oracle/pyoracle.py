@@ -79,6 +79,16 @@ def load() -> C.CDLL:
         lib.orc_set_solver_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
         lib.orc_set_newton_params.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         lib.orc_newton_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), dp]
+        lib.orc_set_adaptivity.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int),
+                                           dp, dp, dp]
+        lib.orc_adapt.argtypes = [C.c_void_p]
+        lib.orc_remesh_if_due.argtypes = [C.c_void_p]
+        lib.orc_n_nodes.argtypes = [C.c_void_p]
+        lib.orc_n_nodes.restype = C.c_long
+        lib.orc_cells.argtypes = [C.c_void_p, P(C.c_int)]
+        lib.orc_node_points.argtypes = [C.c_void_p, dp]
+        lib.orc_hanging.argtypes = [C.c_void_p, P(C.c_int), P(C.c_long), dp]
+        lib.orc_hanging.restype = C.c_long
         _lib = lib
     return _lib
 
@@ -97,7 +107,10 @@ def gl_rule(n: int):
 class Oracle:
     """The workload's problem restated on the CPU."""
 
-    def __init__(self, wl, threads: int = 0):
+    def __init__(self, wl, threads: int = 0, adaptivity: dict | None = None):
+        """adaptivity: {min_level, max_level, period, criteria: [(field, flags, vlo, vhi, glo)]}
+        (flags 1 value, 2 gradient); the mesh starts uniform at the global refinement and the
+        vectors of this wrapper are then in the adaptive DoF order (``*_native``)."""
         self.lib = load()
         self.wl = wl
         m = wl.mesh
@@ -122,13 +135,28 @@ class Oracle:
             tl = dep_table(b.dependencies_lhs)[:nf].astype(np.int32).ravel()
             self.lib.orc_add_block(self.h, b.id, b.solve_type, b.solve_timing, fi, len(b.field_indices),
                                    tr.ctypes.data_as(C.POINTER(C.c_int)), tl.ctypes.data_as(C.POINTER(C.c_int)))
+        self.adaptive = adaptivity is not None
+        if self.adaptive:
+            # node positions are in units of the node spacing at max_level
+            self._shift = int(adaptivity["max_level"]) - m.global_refinement
+            crit = adaptivity.get("criteria", [])
+            ci = lambda k: (C.c_int * max(1, len(crit)))(*[int(c[k]) for c in crit])
+            cd = lambda k: (C.c_double * max(1, len(crit)))(*[float(c[k]) for c in crit])
+            rc = self.lib.orc_set_adaptivity(self.h, int(adaptivity["min_level"]), int(adaptivity["max_level"]),
+                                             int(adaptivity.get("period", 0)), len(crit), ci(0), ci(1), cd(2), cd(3),
+                                             cd(4))
+            if rc != 0:
+                raise RuntimeError("oracle: adaptivity parameters rejected")
         consts = np.ascontiguousarray(np.asarray(wl.constants, dtype=np.float64))
         rc = self.lib.orc_finalize(self.h, MODEL_IDS[wl.model], _dp(consts), len(consts), float(wl.dt))
         if rc != 0:
             raise RuntimeError("oracle: finalize failed")
         self._perm = {}
         for f, v in wl.initial.items():
-            self.set(f, v)
+            if self.adaptive:
+                self.set_native(f, self.lattice_to_native(f, v))
+            else:
+                self.set(f, v)
 
     def close(self):
         if getattr(self, "h", None):
@@ -202,6 +230,68 @@ class Oracle:
         out = np.zeros(p.size)
         out[p] = v
         return out
+
+    # --- adaptive meshes (native = adaptive DoF order, vector fields component-major) -------
+    def n_nodes(self) -> int:
+        return int(self.lib.orc_n_nodes(self.h))
+
+    def n_cells(self) -> int:
+        return int(self.lib.orc_n_cells(self.h))
+
+    def cells(self) -> np.ndarray:
+        """Active cells in tree order: (level, i, j, k)."""
+        out = np.zeros((self.n_cells(), 4), np.int32)
+        self.lib.orc_cells(self.h, out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out
+
+    def node_points(self) -> np.ndarray:
+        out = np.zeros((self.n_nodes(), 3))
+        self.lib.orc_node_points(self.h, _dp(out))
+        return out
+
+    def hanging(self):
+        """Closed hanging-node lines of the scalar DoFs: (count per DoF, masters, weights)."""
+        n = self.n_nodes()
+        t = int(self.lib.orc_hanging(self.h, None, None, None))
+        cnt = np.zeros(n, np.int32)
+        mas = np.zeros(max(t, 1), np.int64)
+        w = np.zeros(max(t, 1))
+        self.lib.orc_hanging(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int)), mas.ctypes.data_as(C.POINTER(C.c_long)),
+                             _dp(w))
+        return cnt, mas[:t], w[:t]
+
+    def lattice_to_native(self, f: int, lattice_values: np.ndarray) -> np.ndarray:
+        """A lattice-order vector of the initial uniform mesh in the adaptive DoF order."""
+        m = self.wl.mesh
+        nn = m.nodes + [1] * (3 - m.dim)
+        L = self.lattice(self._rank(f)).astype(np.int64)
+        I = L[:, :3] >> self._shift
+        idx = L[:, 3] * int(np.prod(nn)) + (I[:, 2] * nn[1] + I[:, 1]) * nn[0] + I[:, 0]
+        return np.asarray(lattice_values, dtype=np.float64)[idx]
+
+    def set_native(self, f: int, values: np.ndarray, age: int = 0):
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.float64))
+        if self.lib.orc_set_vector(self.h, f, age, _dp(v)) != 0:
+            raise RuntimeError("oracle: age not stored")
+
+    def get_native(self, f: int, age: int = 0) -> np.ndarray:
+        v = np.zeros(self.n_dofs(self._rank(f)))
+        if self.lib.orc_get_vector(self.h, f, age, _dp(v)) != 0:
+            raise RuntimeError("oracle: age not stored")
+        return v
+
+    def invm_native(self, rank: int = 0) -> np.ndarray:
+        v = np.zeros(self.n_dofs(rank))
+        self.lib.orc_invm(self.h, rank, _dp(v))
+        return v
+
+    def adapt(self):
+        """One remesh pass (mark, smooth, refine/coarsen, transfer)."""
+        if self.lib.orc_adapt(self.h) != 0:
+            raise RuntimeError("oracle: mesh is not adaptive")
+
+    def remesh_if_due(self):
+        self.lib.orc_remesh_if_due(self.h)
 
     def set_time(self, increment: int, time: float):
         self.lib.orc_set_time(self.h, increment, time)

@@ -63,6 +63,9 @@ class Workload:
     n_steps: int
     initial: dict = dfield(default_factory=dict)  # field index -> lattice-order vector
     seed: int = 0
+    # mesh adaptivity: {min_level, max_level, period, criteria: [(field, flags, vlo, vhi, glo)]}
+    # (flags 1 value, 2 gradient); None for a uniform mesh
+    adaptivity: dict | None = None
 
     def make_problem(self):
         from .problem import Problem
@@ -96,6 +99,36 @@ def allen_cahn_2d(refine: int = 7, degree: int = 1, seed: int = 1234, n_grains: 
     n0 = grain_field(x, centres, radii, 2.0)
     return Workload("allen_cahn_2d", mesh, fields, [exp_block, pp_block], "allen_cahn", [m_well, kappa], dt,
                     n_steps, {0: n0}, seed)
+
+
+def allen_cahn_amr_2d(refine: int = 4, degree: int = 2, min_level: int = 3, max_level: int = 6, period: int = 10,
+                      seed: int = 1234, n_grains: int = 6, size: float = 100.0, n_steps: int = 100,
+                      dt: float = 0.01) -> Workload:
+    """Allen-Cahn 2-D on an adaptive mesh refined where 0.01 < n < 0.99 (the interfaces), as
+    applications/allen_cahn/explicit with `mesh adaptivity = true` in its parameters."""
+    wl = allen_cahn_2d(refine=refine, degree=degree, seed=seed, n_grains=n_grains, size=size, n_steps=n_steps, dt=dt)
+    wl.name = "allen_cahn_amr_2d"
+    wl.adaptivity = dict(min_level=min_level, max_level=max_level, period=period,
+                         criteria=[(0, 1, 0.01, 0.99, 0.0)])
+    return wl
+
+
+def cahn_hilliard_amr(dim: int = 2, refine: int = 3, degree: int = 2, min_level: int = 2, max_level: int = 5,
+                      period: int = 5, seed: int = 4321, size: float = 32.0, n_steps: int = 50,
+                      dt: float = 1e-3, gradient_bound: float = 0.25) -> Workload:
+    """Periodic Cahn-Hilliard on an adaptive mesh refined where the concentration gradient is
+    large (a smooth two-phase initial field), fields c, mu, f_tot."""
+    wl = cahn_hilliard_3d(refine=refine, degree=degree, seed=seed, size=size, n_steps=n_steps, dt=dt, dim=dim)
+    x = lattice_coordinates(wl.mesh)
+    rng = np.random.default_rng(seed)
+    k = 2.0 * np.pi / size
+    phase = rng.uniform(0.0, 2.0 * np.pi, size=2)
+    c0 = 0.5 + 0.4 * np.tanh(4.0 * np.sin(k * x[:, 0] + phase[0]) * np.cos(k * x[:, 1] + phase[1]))
+    wl.initial = {0: c0}
+    wl.name = "cahn_hilliard_amr_%dd" % dim
+    wl.adaptivity = dict(min_level=min_level, max_level=max_level, period=period,
+                         criteria=[(0, 2, 0.0, 0.0, gradient_bound)])
+    return wl
 
 
 def cahn_hilliard_3d(refine: int = 6, degree: int = 2, seed: int = 4321, size: float = 64.0, n_steps: int = 200,
