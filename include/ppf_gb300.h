@@ -13,6 +13,9 @@
  *   PPF_ORDER_DEALII   the DoF numbering deal.II's DoFHandler::distribute_dofs produces for
  *                      the same mesh (cells in refinement order; per cell vertices, lines,
  *                      quads, hex interior; FESystem components per object).
+ *   PPF_ORDER_NATIVE   the handle's own order: the lattice order on uniform meshes; on
+ *                      adaptive meshes the DoFs in first-touch order over the active cells
+ *                      (see ppf_set_adaptivity), vector fields component-major.
  *
  * Threading: a handle is not thread-safe; it owns one CUDA stream. Errors never throw:
  * every call returns PPF_OK or a PPF_ERR_* code, and ppf_last_error() gives the message.
@@ -41,7 +44,7 @@ enum ppf_status {
   PPF_ERR_TIMEOUT = 7       /* a bounded device-side wait gave up */
 };
 
-enum ppf_ordering { PPF_ORDER_LATTICE = 0, PPF_ORDER_DEALII = 1 };
+enum ppf_ordering { PPF_ORDER_LATTICE = 0, PPF_ORDER_DEALII = 1, PPF_ORDER_NATIVE = 2 };
 
 /* dependency flags (dependencies.h:134-213: values, grad(), hess()/lap()/hessdiag()) */
 enum ppf_dep_flag { PPF_DEP_VALUE = 1, PPF_DEP_GRADIENT = 2, PPF_DEP_HESSIAN = 4 };
@@ -249,6 +252,83 @@ int ppf_newton_solve(ppf_handle h, int b, int* newton_iterations, int* linear_it
  * tolerance type is not AbsoluteResidual, zero entries set to one
  * (MFOperator::compute_diagonal, mf_operator.cc:82-101); lattice order, host output. */
 int ppf_lhs_diagonal(ppf_handle h, int b, double* out);
+
+/* ---- Adaptive meshes ----------------------------------------------------------------------
+ * Mesh adaptivity of RefinementManager (src/core/refinement_manager.cc:42-439) with deal.II's
+ * refinement smoothing, hanging-node constraints and solution transfer, for degrees 1 and 2 and
+ * Explicit, Constant and PostProcess blocks.
+ *
+ * The mesh is a forest of quadtrees / octrees over the coarse subdivided rectangle. It starts
+ * uniform at the global refinement (the initial condition is uploaded on that mesh, in lattice
+ * order, as for a uniform handle). In the increment loop (problem.cc:488-499) the remeshing step
+ * runs after the blocks of an increment: at increment 0 up to max - min passes (stopping when
+ * the DoF count no longer changes), later one pass every remeshing_period increments. A pass
+ * flags cells whose fields meet a criterion at any quadrature point for refinement (below
+ * max_refinement) and the others for coarsening (above min_refinement), smooths the flags
+ * (complete families only, 2:1 balance across faces, edges and vertices, refinement of
+ * unrefined islands), refines/coarsens, renumbers, transfers every stored age (old nodes keep
+ * their values, new nodes interpolate the old cell containing them), recomputes the inverse
+ * lumped mass and distributes the new constraints.
+ *
+ * Numbering (PPF_ORDER_NATIVE): active cells in tree order (coarse cells lexicographic, children
+ * depth-first in lexicographic child order), DoFs by first touch with lexicographic cell nodes.
+ * Periodic images are one DoF. Hanging DoFs hold their interpolated values and have invM = 0.
+ * ppf_n_nodes / ppf_n_cells / ppf_field_length report the current mesh. */
+enum ppf_refine_flag { PPF_REFINE_VALUE = 1, PPF_REFINE_GRADIENT = 2 };
+
+/* SpatialDiscretization (spatial_discretization.cc:372-523): levels count from the coarse mesh
+ * (0); criteria as RefinementCriterion (grid_refiner_criterion.h): value in the open range
+ * (value_lower, value_upper), gradient magnitude above gradient_lower; vector fields use their
+ * l2 norms (and compare the gradient norm with the value range, as the reference does). */
+typedef struct {
+  int min_refinement;
+  int max_refinement;
+  int remeshing_period;    /* <= 0: only the passes at increment 0 */
+  int n_criteria;
+  int criterion_field[PPF_MAX_FIELDS];
+  int criterion_flags[PPF_MAX_FIELDS];
+  double value_lower[PPF_MAX_FIELDS];
+  double value_upper[PPF_MAX_FIELDS];
+  double gradient_lower[PPF_MAX_FIELDS];
+} ppf_adaptivity;
+
+/* Makes the handle's mesh adaptive; call right after ppf_create / ppf_create_custom (field
+ * states are reset). Fails with PPF_ERR_UNSUPPORTED for degree > 2, Linear or Newton blocks,
+ * or meshes too fine for the position encoding. */
+int ppf_set_adaptivity(ppf_handle h, const ppf_adaptivity* a);
+
+/* One remeshing pass now (RefinementManager::do_adaptive_refinement). */
+int ppf_adapt(ppf_handle h);
+
+/* The remeshing step of the current increment, as ppf_run does it after the blocks (for callers
+ * of ppf_increment_block / ppf_end_increment). */
+int ppf_remesh_if_due(ppf_handle h);
+
+/* Counts mesh changes (0 before the first); callers that cache geometry compare it. */
+long long ppf_mesh_version(ppf_handle h);
+
+/* Active cells in tree order, 4 ints each: level, x, y, z (integer coordinates at that level;
+ * the cell spans lower + size * [x, x+1] / (subdivisions * 2^level) per axis). Uniform handles
+ * report their lattice cells at the global refinement. */
+int ppf_cells(ppf_handle h, int* out);
+
+/* DoF indices (PPF_ORDER_NATIVE) of every active cell's (degree+1)^dim nodes, lexicographic. */
+int ppf_cell_dofs(ppf_handle h, int* out);
+
+/* Coordinates of the DoFs (3 doubles each, PPF_ORDER_NATIVE). */
+int ppf_node_points(ppf_handle h, double* out);
+
+/* Closed hanging-node lines: count[p] entries for DoF p (0 when not hanging), then the
+ * (master, weight) entries in ascending master order. Returns the total entry count (outputs
+ * may be NULL to size them), or -1. */
+long long ppf_hanging(ppf_handle h, int* count, int* master, double* weight);
+
+/* Values of the non-uniform Dirichlet conditions of field f (set_dirichlet,
+ * pde_operator_base.h:68-76) on adaptive meshes: the engine calls fn at every Dirichlet node of
+ * every mesh it builds; without it the per-face constants of ppf_field_desc apply. */
+typedef double (*ppf_dirichlet_fn)(void* user, int field, int component, int boundary_id, const double* point,
+                                   double time);
+int ppf_set_dirichlet_function(ppf_handle h, int field, ppf_dirichlet_fn fn, void* user);
 
 /* ---- Ensembles --------------------------------------------------------------------------
  * Many independent explicit Allen-Cahn simulations (block 1 of

@@ -108,7 +108,12 @@ int launch_user_operator(int d, int k, int mode, int precision, const void* cell
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   using Op = UserOperator<PDE>;
   if (mode == ppf::MODE_RHS) return (int)ppf::launch_cell_kernel<Op, dim, degree, ppf::MODE_RHS, double>(P, object, smem, s);
+  // adaptive meshes: the launch record is an AmrCellLaunch
+  if (mode == (ppf::MODE_RHS | ppf::MODE_AMR))
+    return (int)ppf::launch_amr_operator<Op, dim, degree, ppf::MODE_RHS>(cell_launch, object, smem, s);
   if constexpr (lhs) {
+    if (mode == (ppf::MODE_LHS | ppf::MODE_AMR))
+      return (int)ppf::launch_amr_operator<Op, dim, degree, ppf::MODE_LHS>(cell_launch, object, smem, s);
     if (mode == ppf::MODE_LHS)
       return (int)ppf::launch_cell_kernel<Op, dim, degree, ppf::MODE_LHS, double>(P, object, smem, s);
     if (mode == ppf::MODE_DIAG)

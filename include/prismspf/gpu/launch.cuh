@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <prismspf/gpu/amr_cell_kernel.cuh>
 #include <prismspf/gpu/cell_kernel.cuh>
 
 namespace ppf {
@@ -40,6 +41,18 @@ cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj));
   return cudaGetLastError();
+}
+
+// The adaptive-mesh kernel for a mode without the MODE_AMR flag; `rec` is an AmrCellLaunch.
+// Adaptive meshes exist for degrees 1 and 2 (nested Gauss-Lobatto points), so only those are
+// instantiated.
+template <class PDE, int dim, int degree, int mode>
+cudaError_t launch_amr_operator(const void* rec, const void* obj, size_t smem, cudaStream_t s) {
+  if constexpr (degree <= 2 && dim >= 2)
+    return launch_amr_cell_kernel<PDE, dim, degree, mode, double>(*static_cast<const AmrCellLaunch*>(rec), obj, smem,
+                                                                  s);
+  else
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace ppf

@@ -26,6 +26,10 @@ PPF_ERR_TIMEOUT = 7
 
 ORDER_LATTICE = 0
 ORDER_DEALII = 1
+ORDER_NATIVE = 2
+
+REFINE_VALUE = 1
+REFINE_GRADIENT = 2
 
 # exported symbols of include/ppf_gb300.h (checked by the CPU test suite)
 EXPORTED = [
@@ -44,6 +48,9 @@ EXPORTED = [
     "ppf_adjoint_forward", "ppf_adjoint_backward", "ppf_tangent_linear", "ppf_checkpoint_schedule_cost",
     # operators compiled by the caller (bound from C++ by prismspf/core/problem.h)
     "ppf_create_custom", "ppf_set_dirichlet_values", "ppf_dealii_cell_nodes", "ppf_download_solution",
+    # adaptive meshes
+    "ppf_set_adaptivity", "ppf_adapt", "ppf_remesh_if_due", "ppf_mesh_version", "ppf_cells", "ppf_cell_dofs",
+    "ppf_node_points", "ppf_hanging", "ppf_set_dirichlet_function",
 ]
 
 
@@ -77,6 +84,23 @@ class LinearParams(C.Structure):
         ("smoothing_range", C.c_double), ("eig_cg_iterations", C.c_int), ("mixed_precision", C.c_int),
         ("solver_type", C.c_int),
     ]
+
+
+class Adaptivity(C.Structure):
+    _fields_ = [
+        ("min_refinement", C.c_int),
+        ("max_refinement", C.c_int),
+        ("remeshing_period", C.c_int),
+        ("n_criteria", C.c_int),
+        ("criterion_field", C.c_int * PPF_MAX_FIELDS),
+        ("criterion_flags", C.c_int * PPF_MAX_FIELDS),
+        ("value_lower", C.c_double * PPF_MAX_FIELDS),
+        ("value_upper", C.c_double * PPF_MAX_FIELDS),
+        ("gradient_lower", C.c_double * PPF_MAX_FIELDS),
+    ]
+
+
+DIRICHLET_FN = C.CFUNCTYPE(C.c_double, C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_double)
 
 
 class PPFError(RuntimeError):
@@ -147,6 +171,17 @@ def load() -> C.CDLL:
     lib.ppf_tangent_linear.argtypes = [H, C.c_int, C.c_int, dp, dp, dp]
     lib.ppf_checkpoint_schedule_cost.argtypes = [C.c_int, C.c_int]
     lib.ppf_checkpoint_schedule_cost.restype = C.c_longlong
+    lib.ppf_set_adaptivity.argtypes = [H, P(Adaptivity)]
+    lib.ppf_adapt.argtypes = [H]
+    lib.ppf_remesh_if_due.argtypes = [H]
+    lib.ppf_mesh_version.argtypes = [H]
+    lib.ppf_mesh_version.restype = C.c_longlong
+    lib.ppf_cells.argtypes = [H, P(C.c_int)]
+    lib.ppf_cell_dofs.argtypes = [H, P(C.c_int)]
+    lib.ppf_node_points.argtypes = [H, dp]
+    lib.ppf_hanging.argtypes = [H, P(C.c_int), P(C.c_int), dp]
+    lib.ppf_hanging.restype = C.c_longlong
+    lib.ppf_set_dirichlet_function.argtypes = [H, C.c_int, DIRICHLET_FN, C.c_void_p]
     _lib = lib
     return lib
 

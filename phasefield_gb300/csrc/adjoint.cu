@@ -216,6 +216,7 @@ int reverse(ppf_handle h, AdjointState& A, int a, int b, int s) {
 
 int check_block(ppf_handle h, int b) {
   if (b < 0 || b >= (int)h->blocks.size()) return fail(h, PPF_ERR_ARG, "bad block");
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "the adjoint runs on uniform meshes");
   const ppf_block_desc& d = h->blocks[b].desc;
   if (std::strcmp(h->model->name, "coupled_acch") != 0 || d.n_fields != 2 || d.solve_type != PPF_EXPLICIT)
     return fail(h, PPF_ERR_UNSUPPORTED, "the adjoint is implemented for the coupled_acch explicit block");

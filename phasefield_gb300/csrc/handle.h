@@ -40,6 +40,11 @@ struct BlockPlan {
   int nrows_in = 0, nrows_out = 0;
   void* d_tables = nullptr;
   bool valid = false;
+  // the slot tables of the plan (host copies; adaptive meshes build one CellTables per level)
+  signed char slot_of[pg::MAX_FIELDS][pg::NAGE];
+  signed char slot_comp0[pg::MAX_SLOTS];
+  signed char out_of[pg::MAX_FIELDS];
+  signed char out_row0[pg::MAX_OUTS];
 };
 
 // One mesh of a multigrid hierarchy for a single-field linear block (the finest level is the
@@ -78,6 +83,7 @@ struct MGLevel {
 };
 
 struct AdjointState;
+struct AmrState;
 
 struct LinearState {
   ppf_linear_params params;
@@ -157,6 +163,8 @@ struct ppf_handle_s {
   double* d_scratch_dst = nullptr;
   long long scratch_len = 0;
   ppf::AdjointState* adj = nullptr;  // adjoint / tangent-linear state (created on first use)
+  ppf::AmrState* amr = nullptr;      // adaptive mesh (ppf_set_adaptivity), else null
+  long long mesh_version = 0;
   // CUDA graph of the explicit increment loop
   prismspf::SimulationTimer* d_timer = nullptr;
   cudaGraphExec_t run_graph = nullptr;
@@ -199,5 +207,13 @@ void free_linear(LinearState& L);
 int explicit_solve_entry(ppf_handle h, int b);
 struct AdjointState;
 void free_adjoint(AdjointState* A);
+// adaptive meshes (amr.cu)
+int amr_launch_cell(ppf_handle h, int b, int which, const CellLaunch& L);
+int amr_finalize_explicit(ppf_handle h, FieldState& F);
+int amr_remesh_if_due(ppf_handle h);
+int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
+                   bool upload);
+int amr_apply_constraints(ppf_handle h, FieldState& F, double* v);
+void free_amr(AmrState* A);
 
 }  // namespace ppf

@@ -514,6 +514,10 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
   auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0);
   if (tab.empty()) return fail(h, PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
+  std::memcpy(P.slot_of, slot_of, sizeof(slot_of));
+  std::memcpy(P.slot_comp0, slot_comp0, sizeof(slot_comp0));
+  std::memcpy(P.out_of, out_of, sizeof(out_of));
+  std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
   P.valid = true;
@@ -576,6 +580,7 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
   L.timer_dev = h->capturing ? h->d_timer : nullptr;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
+  if (h->amr) return amr_launch_cell(h, b, which, L);
   const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
   return timed_cell_launch(h, 0, which == 1 ? MODE_LHS : MODE_RHS, L, h->model_obj.data(), smem);
 }
@@ -622,6 +627,11 @@ static int explicit_solve(ppf_handle h, int b) {
   if (rc) return rc;
   for (int i = 0; i < B.desc.n_fields; ++i) {
     FieldState& F = h->fields[B.desc.field_indices[i]];
+    if (h->amr) {
+      rc = amr_finalize_explicit(h, F);
+      if (rc) return rc;
+      continue;
+    }
     dim3 grid(grid_for(h->N), F.ncomp);
     finalize_explicit_kernel<<<grid, 256, 0, h->stream>>>(F.cur, F.acc, h->d_invm, F.constrained ? F.cmap : nullptr,
                                                           F.dvals, h->N, h->d_err);
@@ -703,6 +713,11 @@ static int solve_increment(ppf_handle h, int output_every) {
   const bool is_output = output_every > 0 && inc % (unsigned)output_every == 0;
   for (size_t b = 0; b < h->blocks.size(); ++b) {
     int rc = increment_block(h, (int)b, is_output);
+    if (rc) return rc;
+  }
+  if (h->amr) {
+    // the refinement step of Problem::solve_increment (problem.cc:488-499), before the rotation
+    int rc = amr_remesh_if_due(h);
     if (rc) return rc;
   }
   end_increment(h);
@@ -916,6 +931,7 @@ void ppf_destroy(ppf_handle h) {
     free_linear(B.lin);
   }
   free_adjoint(h->adj);
+  free_amr(h->amr);
   if (h->run_graph) cudaGraphExecDestroy(h->run_graph);
   cudaFree(h->d_timer);
   cudaFree(h->d_invm);
@@ -939,6 +955,7 @@ long long ppf_field_length(ppf_handle h, int f) {
 
 int ppf_dof_map(ppf_handle h, int rank, long long* out) {
   if (!h || !out || rank < 0 || rank > 1) return PPF_ERR_ARG;
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "deal.II numbering of an adaptive mesh (use PPF_ORDER_NATIVE)");
   auto m = dealii_dof_map(h, rank == 0 ? 1 : h->dim);
   std::memcpy(out, m.data(), sizeof(long long) * m.size());
   return PPF_OK;
@@ -958,7 +975,9 @@ int ppf_invm(ppf_handle h, double* out) {
 
 static int permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
                       bool upload) {
+  if (h->amr) return amr_permute_io(h, f, host, dev_src, dev_dst, ordering, upload);
   FieldState& F = h->fields[f];
+  if (ordering == PPF_ORDER_NATIVE) ordering = PPF_ORDER_LATTICE;
   if (ordering == PPF_ORDER_LATTICE) {
     if (upload) PPF_CUDA(h, cudaMemcpyAsync(dev_dst, host, sizeof(double) * F.len, cudaMemcpyHostToDevice, h->stream));
     else PPF_CUDA(h, cudaMemcpyAsync(host, dev_src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->stream));
@@ -1015,6 +1034,8 @@ int ppf_set_dirichlet_values(ppf_handle h, int f, const double* values) {
 
 int ppf_dealii_cell_nodes(ppf_handle h, long long first, long long count, long long* out) {
   if (!h || !out || first < 0 || count < 0 || first + count > h->ncells) return PPF_ERR_ARG;
+  if (h->amr && h->mesh_version > 0)
+    return fail(h, PPF_ERR_UNSUPPORTED, "deal.II cell order of an adaptive mesh after remeshing (use ppf_cells)");
   const int k = h->k;
   const auto objs = dealii_cell_objects(h->dim, k);
   long long cell = 0, o = 0;
@@ -1031,6 +1052,12 @@ int ppf_dealii_cell_nodes(ppf_handle h, long long first, long long count, long l
 int ppf_apply_constraints(ppf_handle h, int f) {
   if (!h || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
   FieldState& F = h->fields[f];
+  if (h->amr) {
+    int rc = amr_apply_constraints(h, F, F.cur);
+    if (rc) return rc;
+    PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PPF_OK;
+  }
   if (!F.constrained) return PPF_OK;
   distribute_kernel<<<grid_for(F.len), 256, 0, h->stream>>>(F.cur, F.cmap, F.dvals, F.len);
   PPF_CUDA(h, cudaGetLastError());
@@ -1051,8 +1078,9 @@ int ppf_solve_block(ppf_handle h, int b) {
 // were), each followed by a device-side timer advance; callbacks read the timer from device
 // memory during replays, so time-dependent operators see the right time.
 static bool graph_eligible(ppf_handle h, int output_every) {
-  // per-launch event timing needs plain launches; postprocess increments are not periodic
-  if (!h->use_graph || h->timing || output_every > 0) return false;
+  // per-launch event timing needs plain launches; postprocess increments are not periodic;
+  // adaptive meshes change their vectors when they remesh
+  if (!h->use_graph || h->timing || output_every > 0 || h->amr) return false;
   for (auto& B : h->blocks) {
     const int t = B.desc.solve_type;
     if (t != PPF_EXPLICIT && t != PPF_CONSTANT) return false;

@@ -197,16 +197,79 @@ class Problem:
         return out
 
     # --- state ----------------------------------------------------------------------------
+    def _io_length(self, f: int, ordering: int) -> int:
+        # lattice-order vectors keep the initial lattice's length on adaptive meshes too
+        if ordering == capi.ORDER_NATIVE or not getattr(self, "adaptive", False):
+            return self.field_length(f)
+        ncomp = 1 if self.fields[f].field_type == 0 else self.mesh.dim
+        return ncomp * int(np.prod(self.mesh.nodes))
+
     def upload(self, f: int, values: np.ndarray, age: int = 0, ordering: int = capi.ORDER_LATTICE):
         v = np.ascontiguousarray(values, dtype=np.float64).ravel()
-        if v.size != self.field_length(f):
+        if v.size != self._io_length(f, ordering):
             raise ValueError("wrong vector length")
         self._check(self.lib.ppf_upload_state(self.h, f, age, capi.dptr(v), ordering))
 
     def download(self, f: int, age: int = 0, ordering: int = capi.ORDER_LATTICE) -> np.ndarray:
-        out = np.empty(self.field_length(f), dtype=np.float64)
+        out = np.empty(self._io_length(f, ordering), dtype=np.float64)
         self._check(self.lib.ppf_download_state(self.h, f, age, capi.dptr(out), ordering))
         return out
+
+    # --- adaptive meshes --------------------------------------------------------------------
+    def set_adaptivity(self, adaptivity: dict):
+        """{min_level, max_level, period, criteria: [(field, flags, vlo, vhi, glo)]} (flags 1 value,
+        2 gradient); the mesh starts uniform at the global refinement (ppf_set_adaptivity)."""
+        a = capi.Adaptivity()
+        a.min_refinement = int(adaptivity["min_level"])
+        a.max_refinement = int(adaptivity["max_level"])
+        a.remeshing_period = int(adaptivity.get("period", 0))
+        crit = adaptivity.get("criteria", [])
+        a.n_criteria = len(crit)
+        for i, (f, fl, vlo, vhi, glo) in enumerate(crit):
+            a.criterion_field[i], a.criterion_flags[i] = int(f), int(fl)
+            a.value_lower[i], a.value_upper[i], a.gradient_lower[i] = float(vlo), float(vhi), float(glo)
+        self._check(self.lib.ppf_set_adaptivity(self.h, C.byref(a)))
+        self.adaptive = True
+
+    def adapt(self):
+        self._check(self.lib.ppf_adapt(self.h))
+
+    def remesh_if_due(self):
+        self._check(self.lib.ppf_remesh_if_due(self.h))
+
+    @property
+    def mesh_version(self) -> int:
+        return int(self.lib.ppf_mesh_version(self.h))
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.lib.ppf_n_cells(self.h))
+
+    def cells(self) -> np.ndarray:
+        """Active cells: (level, x, y, z) each, tree order on adaptive meshes."""
+        out = np.empty((self.n_cells, 4), dtype=np.int32)
+        self._check(self.lib.ppf_cells(self.h, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def cell_dofs(self) -> np.ndarray:
+        out = np.empty(self.n_cells * (self.mesh.degree + 1) ** self.mesh.dim, dtype=np.int32)
+        self._check(self.lib.ppf_cell_dofs(self.h, out.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+    def node_points(self) -> np.ndarray:
+        out = np.empty((self.n_nodes, 3), dtype=np.float64)
+        self._check(self.lib.ppf_node_points(self.h, capi.dptr(out)))
+        return out
+
+    def hanging(self):
+        """Closed hanging-node lines: (count per DoF, masters, weights)."""
+        t = int(self.lib.ppf_hanging(self.h, None, None, None))
+        cnt = np.empty(self.n_nodes, dtype=np.int32)
+        mas = np.empty(max(t, 1), dtype=np.int32)
+        w = np.empty(max(t, 1), dtype=np.float64)
+        self.lib.ppf_hanging(self.h, cnt.ctypes.data_as(C.POINTER(C.c_int)), mas.ctypes.data_as(C.POINTER(C.c_int)),
+                             capi.dptr(w))
+        return cnt, mas[:t], w[:t]
 
     def apply_constraints(self, f: int):
         self._check(self.lib.ppf_apply_constraints(self.h, f))

@@ -70,6 +70,8 @@ class Workload:
     def make_problem(self):
         from .problem import Problem
         p = Problem(self.fields, self.blocks, self.mesh, self.model, self.constants, self.dt)
+        if self.adaptivity is not None:
+            p.set_adaptivity(self.adaptivity)
         for f, v in self.initial.items():
             p.upload(f, v)
         return p
