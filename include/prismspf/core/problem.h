@@ -19,10 +19,17 @@
 //   * output increments from the "output" subsection: VTU (or a one-piece PVTU) of every
 //     field and the reference's log lines (field l2-norm and integrated value,
 //     problem.cc:505-552);
-//   * a non-finite solution writes the output of that increment and throws ExcNaN.
-// Not carried over: adaptive refinement (runs on the uniform mesh), nucleation, checkpoints,
-// initial conditions from files, pre/post_solve_block hooks, user stop. Newton blocks run
-// with cg or bicgstab (no preconditioner, or Chebyshev for single-field blocks).
+//   * a non-finite solution writes the output of that increment and throws ExcNaN;
+//   * "mesh adaptivity = true": the engine's adaptive mesh (ppf_set_adaptivity) with the
+//     parameter file's min/max refinement, remeshing period and refinement criteria, for
+//     degrees 1 and 2 and Explicit, Constant and PostProcess blocks (other configurations run
+//     on the uniform mesh with a note); the initial condition is set on the initial uniform
+//     mesh and carried through the refinement passes as the reference's solution transfer does,
+//     Dirichlet values come from set_dirichlet at the nodes of every mesh, and the output
+//     writes the active cells of the current mesh.
+// Not carried over: nucleation, checkpoints, initial conditions from files,
+// pre/post_solve_block hooks, user stop. Newton blocks run with cg or bicgstab (no
+// preconditioner, or Chebyshev for single-field blocks).
 #pragma once
 
 #include <cmath>
@@ -223,9 +230,26 @@ class Problem {
     if (handle) return;
     const auto& sd = user_inputs->spatial_discretization;
     const auto& mesh = sd.rectangular_mesh;
-    if (sd.has_adaptivity)
-      std::cout << "note: mesh adaptivity is not applied; running on the uniform mesh (global refinement "
-                << sd.global_refinement << ")" << std::endl;
+    // adaptive meshes (refinement_manager.cc) for degrees 1 and 2 with Explicit, Constant and
+    // PostProcess blocks; other configurations run on the uniform mesh with a note
+    adaptive = false;
+    if (sd.has_adaptivity) {
+      std::string why;
+      if (dim < 2) why = "one-dimensional meshes";
+      else if (degree > 2) why = "degree > 2";
+      for (const auto& sb : solve_blocks)
+        if (sb.solve_type == SolveType::Linear || sb.solve_type == SolveType::Newton) why = "Linear or Newton blocks";
+      if (why.empty()) {
+        if (sd.max_refinement < sd.global_refinement)
+          throw std::invalid_argument("The maximum refinement level must be greater than or equal to the global refinement level.");
+        if (sd.min_refinement > sd.global_refinement)
+          throw std::invalid_argument("The minimum refinement level must be less than or equal to the global refinement level.");
+        adaptive = true;
+      } else {
+        std::cout << "note: mesh adaptivity is not applied with " << why << "; running on the uniform mesh (global refinement "
+                  << sd.global_refinement << ")" << std::endl;
+      }
+    }
     for (const auto& s : user_inputs->not_applied) std::cout << "note: not applied: " << s << std::endl;
     if (field_attributes.empty() || field_attributes.size() > PPF_MAX_FIELDS)
       throw std::invalid_argument("between 1 and 8 fields are supported");
@@ -329,6 +353,28 @@ class Problem {
           "set-up");
     if (user_inputs->temporal_discretization.initial_time != 0.0)
       check(ppf_set_time(handle, 0, user_inputs->temporal_discretization.initial_time), "start time");
+    if (adaptive) {
+      ppf_adaptivity a{};
+      a.min_refinement = (int)sd.min_refinement;
+      a.max_refinement = (int)sd.max_refinement;
+      // remeshing period: increments between passes (the default UINT_MAX: only increment 0)
+      a.remeshing_period = sd.remeshing_period > (unsigned)INT32_MAX ? 0 : (int)sd.remeshing_period;
+      for (const auto& [name, c] : sd.refinement_criteria) {
+        if (c.criterion == RefinementFlags::Nothing) continue;
+        int f = -1;
+        for (size_t i = 0; i < field_attributes.size(); ++i)
+          if (field_attributes[i].name == name) f = (int)i;
+        if (f < 0) throw std::invalid_argument("refinement criterion for an unknown field " + name);
+        if (a.n_criteria >= PPF_MAX_FIELDS) throw std::invalid_argument("too many refinement criteria");
+        a.criterion_field[a.n_criteria] = f;
+        a.criterion_flags[a.n_criteria] = (int)c.criterion;
+        a.value_lower[a.n_criteria] = c.value_lower_bound;
+        a.value_upper[a.n_criteria] = c.value_upper_bound;
+        a.gradient_lower[a.n_criteria] = c.gradient_lower_bound;
+        a.n_criteria++;
+      }
+      check(ppf_set_adaptivity(handle, &a), "mesh adaptivity");
+    }
 
     // linear (and Newton) solver parameters (linear_solver.h:220-402, newton_solver.h:73-156)
     for (size_t b = 0; b < solve_blocks.size(); ++b) {
@@ -375,6 +421,23 @@ class Problem {
     return p;
   }
 
+  // set_dirichlet at one boundary point, for the engine's Dirichlet nodes of adaptive meshes
+  static double dirichlet_point(void* user, int field, int comp, int bid, const double* x, double time) {
+    const Problem* self = static_cast<const Problem*>(user);
+    const auto& T = self->user_inputs->temporal_discretization;
+    SimulationTimer timer(T.dt, time);
+    timer.set_increment(T.dt != 0.0 ? (unsigned int)std::llround((time - T.initial_time) / T.dt) : 0u);
+    dealii::Point<dim> p;
+    for (unsigned int d = 0; d < dim; ++d) p[d] = x[d];
+    number s[3] = {0, 0, 0};
+    if (self->field_attributes[(size_t)field].field_type != TensorRank::Vector) {
+      self->pde->set_dirichlet((unsigned)field, (unsigned)bid, 0, p, timer, s[0], s[0]);
+      return s[0];
+    }
+    self->pde->set_dirichlet((unsigned)field, (unsigned)bid, (unsigned)comp, p, timer, s[0], s[comp]);
+    return s[comp];
+  }
+
   void apply_initial_conditions() {
     std::set<unsigned int> ic_fields;
     for (const auto& sb : solve_blocks)
@@ -383,7 +446,9 @@ class Problem {
     const long long ncells = ppf_n_cells(handle);
     const int ppc = (int)std::pow(degree + 1, dim);
     std::vector<std::vector<double>> vals(field_attributes.size());
-    for (unsigned int f : ic_fields) vals[f].assign((size_t)ppf_field_length(handle, (int)f), 0.0);
+    // lattice-order vectors of the initial mesh (adaptive meshes start from it too)
+    for (unsigned int f : ic_fields)
+      vals[f].assign((size_t)((field_attributes[f].field_type == TensorRank::Vector ? dim : 1) * lattice.N), 0.0);
     const long long chunk = 1 << 15;
     std::vector<long long> nodes;
     for (long long c0 = 0; c0 < ncells; c0 += chunk) {
@@ -416,6 +481,13 @@ class Problem {
     timer.set_increment(increment);
     for (size_t f = 0; f < field_attributes.size(); ++f) {
       if (!dirichlet_fields[f]) continue;
+      if (adaptive) {
+        // the engine evaluates set_dirichlet at the Dirichlet nodes of every mesh it builds,
+        // at its current time
+        check(ppf_set_dirichlet_function(handle, (int)f, &Problem::dirichlet_point, const_cast<Problem*>(this)),
+              "Dirichlet function");
+        continue;
+      }
       const int ncomp = field_attributes[f].field_type == TensorRank::Vector ? (int)dim : 1;
       const long long len = ppf_field_length(handle, (int)f);
       std::vector<int> cmap((size_t)len);
@@ -464,7 +536,9 @@ class Problem {
     inc << std::setw(digits) << std::setfill('0') << increment;
     std::vector<std::vector<double>> sol(field_attributes.size());
     std::vector<output::OutputField> of;
-    std::vector<double> invm((size_t)lattice.N);
+    // the handle's own order: the lattice on uniform meshes, the DoF list on adaptive ones
+    const long long N = ppf_n_nodes(handle);
+    std::vector<double> invm((size_t)N);
     check(ppf_invm(handle, invm.data()), "inverse mass");
     double t = 0.0;
     unsigned int cur = 0;
@@ -473,7 +547,7 @@ class Problem {
     std::cout << "Iteration " << increment << " Time " << t << std::endl;
     for (size_t f = 0; f < field_attributes.size(); ++f) {
       sol[f].resize((size_t)ppf_field_length(handle, (int)f));
-      check(ppf_download_solution(handle, (int)f, sol[f].data(), PPF_ORDER_LATTICE), "download");
+      check(ppf_download_solution(handle, (int)f, sol[f].data(), PPF_ORDER_NATIVE), "download");
       const int ncomp = field_attributes[f].field_type == TensorRank::Vector ? (int)dim : 1;
       double l2 = 0.0;
       for (double x : sol[f]) l2 += x * x;
@@ -481,8 +555,8 @@ class Problem {
                 << " integrated value ";
       for (int c = 0; c < ncomp; ++c) {
         double integral = 0.0;
-        for (long long i = 0; i < lattice.N; ++i)
-          if (invm[(size_t)i] > 0.0) integral += sol[f][(size_t)(c * lattice.N + i)] / invm[(size_t)i];
+        for (long long i = 0; i < N; ++i)
+          if (invm[(size_t)i] > 0.0) integral += sol[f][(size_t)(c * N + i)] / invm[(size_t)i];
         std::cout << integral << (c + 1 < ncomp ? " " : "");
       }
       std::cout << std::endl;
@@ -491,7 +565,25 @@ class Problem {
     }
     std::cout << std::endl;
     const std::string prefix = (std::filesystem::path(O.folder) / O.file_name).string();
-    output::VTUWriter writer(lattice, O.patch_subdivisions);
+    output::CellList cl;
+    std::vector<int> cells, cell_dofs;
+    if (adaptive) {
+      cl.ncells = ppf_n_cells(handle);
+      cells.resize((size_t)(4 * cl.ncells));
+      cell_dofs.resize((size_t)(cl.ncells * (long long)std::pow(degree + 1, dim)));
+      check(ppf_cells(handle, cells.data()), "cells");
+      check(ppf_cell_dofs(handle, cell_dofs.data()), "cell DoFs");
+      cl.cells = cells.data();
+      cl.cell_dofs = cell_dofs.data();
+      cl.N = N;
+      const auto& rm = user_inputs->spatial_discretization.rectangular_mesh;
+      for (unsigned int d = 0; d < dim; ++d) {
+        cl.subdivisions[d] = (int)rm.subdivisions[d];
+        cl.size[d] = rm.size[d] - rm.lower_bound[d];
+      }
+    }
+    output::VTUWriter writer = adaptive ? output::VTUWriter(lattice, cl, O.patch_subdivisions)
+                                        : output::VTUWriter(lattice, O.patch_subdivisions);
     if (O.file_type == FieldOutputParameters::PVTU) {
       const std::string piece = prefix + "_" + inc.str() + ".0.vtu";
       writer.write(piece, of, t, increment);
@@ -518,6 +610,7 @@ class Problem {
   output::Lattice lattice;
   std::vector<bool> dirichlet_fields;
   bool time_dependent = false;
+  bool adaptive = false;
   bool warned_format = false;
 };
 

@@ -65,12 +65,34 @@ struct Lattice {
 struct OutputField {
   std::string name;
   int ncomp = 1;                   // 1 or dim
-  const double* values = nullptr;  // lattice order, component-major
+  const double* values = nullptr;  // lattice (or cell-list DoF) order, component-major
+};
+
+// The active cells of an adaptive mesh: level and integer coordinates at that level per cell
+// (4 ints each), the DoF index of each cell's (degree+1)^dim lexicographic nodes, the DoF
+// count per component, and the coarse mesh (subdivisions, size) the levels refine.
+struct CellList {
+  long long ncells = 0;
+  const int* cells = nullptr;
+  const int* cell_dofs = nullptr;
+  long long N = 0;
+  int subdivisions[3] = {1, 1, 1};
+  double size[3] = {1, 1, 1};
 };
 
 class VTUWriter {
  public:
   VTUWriter(const Lattice& L, unsigned int n_subdivisions) : lat(L), ns(n_subdivisions ? n_subdivisions : L.degree) {
+    init();
+  }
+  // cells of an adaptive mesh; `L` gives dim, degree and the lower corner
+  VTUWriter(const Lattice& L, const CellList& C, unsigned int n_subdivisions)
+      : lat(L), cl(&C), ns(n_subdivisions ? n_subdivisions : L.degree) {
+    lat.N = C.N;
+    init();
+  }
+
+  void init() {
     nodes = gauss_lobatto_unit(lat.degree);
     std::vector<double> xe(ns + 1);
     for (unsigned i = 0; i <= ns; ++i) xe[i] = double(i) / ns;
@@ -80,7 +102,7 @@ class VTUWriter {
   void write(const std::string& filename, const std::vector<OutputField>& fields, double time, unsigned int cycle) const {
     const int dim = lat.dim, k = lat.degree;
     const int np1 = ns + 1;
-    const long long ncells = (long long)lat.nc[0] * lat.nc[1] * lat.nc[2];
+    const long long ncells = cl ? cl->ncells : (long long)lat.nc[0] * lat.nc[1] * lat.nc[2];
     const long long ppc = dim == 2 ? (long long)np1 * np1 : (long long)np1 * np1 * np1;  // points per cell
     const long long scc = dim == 2 ? (long long)ns * ns : (long long)ns * ns * ns;        // sub-cells per cell
     const long long npts = ncells * ppc, nsub = ncells * scc;
@@ -90,17 +112,28 @@ class VTUWriter {
     const int n = k + 1;
     std::vector<double> cellv(n * n * (dim == 3 ? n : 1));
     long long p = 0;
+    const int ncn = dim == 3 ? n * n * n : n * n;
     for (long long c = 0; c < ncells; ++c) {
-      const int cx = (int)(c % lat.nc[0]);
-      const int cy = (int)((c / lat.nc[0]) % lat.nc[1]);
-      const int cz = (int)(c / ((long long)lat.nc[0] * lat.nc[1]));
+      int cx, cy, cz;
+      double hc[3] = {lat.h[0], lat.h[1], lat.h[2]};
+      if (cl) {
+        const int lev = cl->cells[4 * c];
+        cx = cl->cells[4 * c + 1];
+        cy = cl->cells[4 * c + 2];
+        cz = cl->cells[4 * c + 3];
+        for (int d = 0; d < dim; ++d) hc[d] = cl->size[d] / (int)((long long)cl->subdivisions[d] << lev);
+      } else {
+        cx = (int)(c % lat.nc[0]);
+        cy = (int)((c / lat.nc[0]) % lat.nc[1]);
+        cz = (int)(c / ((long long)lat.nc[0] * lat.nc[1]));
+      }
       for (int pz = 0; pz < (dim == 3 ? np1 : 1); ++pz)
         for (int py = 0; py < np1; ++py)
           for (int px = 0; px < np1; ++px) {
             const long long q = p + (dim == 3 ? ((long long)pz * np1 + py) * np1 + px : (long long)py * np1 + px);
-            pts[3 * q + 0] = lat.lower[0] + lat.h[0] * (cx + double(px) / ns);
-            pts[3 * q + 1] = lat.lower[1] + lat.h[1] * (cy + double(py) / ns);
-            pts[3 * q + 2] = dim == 3 ? lat.lower[2] + lat.h[2] * (cz + double(pz) / ns) : 0.0;
+            pts[3 * q + 0] = lat.lower[0] + hc[0] * (cx + double(px) / ns);
+            pts[3 * q + 1] = lat.lower[1] + hc[1] * (cy + double(py) / ns);
+            pts[3 * q + 2] = dim == 3 ? lat.lower[2] + hc[2] * (cz + double(pz) / ns) : 0.0;
           }
       for (size_t f = 0; f < fields.size(); ++f) {
         const OutputField& F = fields[f];
@@ -110,7 +143,8 @@ class VTUWriter {
             for (int b = 0; b < n; ++b)
               for (int a = 0; a < n; ++a)
                 cellv[(c3 * n + b) * n + a] =
-                    u[((long long)(k * cz + c3) * lat.nn[1] + (k * cy + b)) * lat.nn[0] + (k * cx + a)];
+                    cl ? u[cl->cell_dofs[c * ncn + (c3 * n + b) * n + a]]
+                       : u[((long long)(k * cz + c3) * lat.nn[1] + (k * cy + b)) * lat.nn[0] + (k * cx + a)];
           for (int pz = 0; pz < (dim == 3 ? np1 : 1); ++pz)
             for (int py = 0; py < np1; ++py)
               for (int px = 0; px < np1; ++px) {
@@ -200,6 +234,7 @@ class VTUWriter {
 
  private:
   Lattice lat;
+  const CellList* cl = nullptr;
   unsigned int ns;
   std::vector<double> nodes;
   std::vector<std::vector<double>> I;

@@ -2,15 +2,15 @@
 // user_input_parameters.h:27-146 and the declare/assign pairs in src/user_inputs/*.cc):
 // rectangular mesh and global refinement, time stepping, boundary conditions, linear solver
 // parameters per solve block, output schedule, the random seed and the Model constants.
-// Entry names and aliases are the reference's. Adaptive-refinement, nucleation, checkpoint
-// and initial-condition-file entries are read and reported as not applied (uniform meshes,
-// analytic initial conditions).
+// Entry names and aliases are the reference's. Nucleation, checkpoint and initial-condition-file
+// entries are read and reported as not applied (analytic initial conditions).
 #pragma once
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <iostream>
+#include <map>
 #include <random>
 #include <set>
 #include <stdexcept>
@@ -18,6 +18,7 @@
 #include <vector>
 
 #include <prismspf/config.h>
+#include <prismspf/core/grid_refiner_criterion.h>
 #include <prismspf/core/type_enums.h>
 #include <prismspf/dealii_shim.h>
 #include <prismspf/user_inputs/constraint_parameters.h>
@@ -48,6 +49,11 @@ struct SpatialDiscretization {
   unsigned int max_refinement = 0;
   unsigned int min_refinement = 0;
   unsigned int remeshing_period = UINT32_MAX;
+  // refinement criteria by field name (spatial_discretization.cc:462-496)
+  std::map<std::string, RefinementCriterion> refinement_criteria;
+
+  // whether the increment is a remeshing increment (spatial_discretization.cc:608-611)
+  [[nodiscard]] bool should_refine_mesh(unsigned int increment) const { return increment % remeshing_period == 0; }
 
   // Euclidean distance between two points (SpatialDiscretization::distance)
   template <typename T>
@@ -185,10 +191,22 @@ class UserInputParameters {
       std::string v;
       if (P.find("", {"remeshing period"}, v)) spatial_discretization.remeshing_period = (unsigned int)prm::to_int(v);
     }
-    if (spatial_discretization.has_adaptivity) not_applied.push_back("mesh adaptivity (runs on the uniform mesh)");
+    // refinement criteria (spatial_discretization.cc:395-496): type none | value | gradient |
+    // value_and_gradient for the listed fields
     for (const auto& sec : P.subsections_with_prefix("refinement criterion: ")) {
       P.mark_used_prefix(sec + "/");
-      not_applied.push_back(sec);
+      const std::string type = P.get(sec, {"type"}, "none");
+      RefinementFlags flags = RefinementFlags::Nothing;
+      if (type == "value") flags = RefinementFlags::Value;
+      else if (type == "gradient") flags = RefinementFlags::Gradient;
+      else if (type == "value_and_gradient") flags = RefinementFlags::Value | RefinementFlags::Gradient;
+      else if (type != "none" && !type.empty()) throw std::invalid_argument(sec + ": unknown refinement criterion type " + type);
+      const RefinementCriterion c(flags, prm::to_double(P.get(sec, {"value lower bound"}, "0.0")),
+                                  prm::to_double(P.get(sec, {"value upper bound"}, "0.0")),
+                                  prm::to_double(P.get(sec, {"gradient magnitude lower bound", "gradient lower bound"},
+                                                       "2147483647")));
+      for (const auto& name : prm::split_list(P.get(sec, {"variables"}, "")))
+        if (!name.empty()) spatial_discretization.refinement_criteria[name] = c;
     }
 
     // time (temporal_discretization.cc:33-110)

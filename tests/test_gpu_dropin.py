@@ -266,3 +266,64 @@ set number steps = 0
     for name, ref in expect.items():
         assert np.abs(v[name] - ref).max() < 1e-10, name
 
+
+def test_allen_cahn_application_on_an_adaptive_mesh_matches_oracle(gpu_lib, tmp_path):
+    """`mesh adaptivity = true` with the reference application's criterion (0.01 < n < 0.99):
+    the initial condition comes from a uniform run of the same application at increment 0, the
+    oracle refines, steps and remeshes from it, and the adaptive run's output patches must carry
+    the oracle's values at their points."""
+    common = """
+subsection Rectangular mesh
+  set x size = 100.0
+  set y size = 100.0
+end
+set time step = 0.01
+subsection miscellaneous
+  set random seed = 99
+end
+set Model constant mobility = 1.0, DOUBLE
+set Model constant kappa = 2.0, DOUBLE
+set Model constant n_grains = 12, INT
+"""
+    n = 30
+    uni = tmp_path / "uniform"
+    uni.mkdir()
+    build_and_run("allen_cahn_explicit", "set global refinement = 5\nset number steps = 0\n" + common, uni)
+    wl = W.allen_cahn_amr_2d(refine=5, degree=1, min_level=3, max_level=6, period=10, dt=0.01)
+    wl.initial = {0: to_lattice(read_vtu(uni / "solutions" / "solution_0.vtu"), wl.mesh, "n")}
+    ada = tmp_path / "adaptive"
+    ada.mkdir()
+    out = build_and_run("allen_cahn_explicit", f"""
+set global refinement = 5
+set max refinement = 6
+set min refinement = 3
+set mesh adaptivity = true
+set remeshing period = 10
+subsection refinement criterion: 0
+  set type = value
+  set value lower bound = 0.01
+  set value upper bound = 0.99
+  set variables = n
+end
+set number steps = {n}
+subsection output
+  set number = 1
+end
+""" + common, ada)
+    assert "not applied" not in out
+    o = po.Oracle(wl, adaptivity=wl.adaptivity)
+    assert o.run(n, n) == 0
+    assert len(np.unique(o.cells()[:, 0])) > 1
+    v = read_vtu(ada / "solutions" / f"solution_{n}.vtu")
+    # one Q1 patch (4 points) per active cell of the oracle's mesh
+    assert len(v["Points"]) == 4 * o.n_cells()
+    h_min = wl.mesh.size[0] / (wl.mesh.subdivisions[0] << wl.adaptivity["max_level"])
+    key = lambda x: tuple(np.rint(x[:, :2] / h_min).astype(np.int64).T)
+    where = {k: i for i, k in enumerate(zip(*key(o.node_points())))}
+    idx = np.array([where[k] for k in zip(*key(v["Points"]))])
+    assert rel_l2(v["n"], o.get_native(0, 1)[idx]) < 1e-9
+    for f, name in ((1, "mg_n"), (2, "f_tot")):
+        assert rel_l2(v[name], o.get_native(f, 0)[idx]) < 1e-9, name
+    norms = logged_norms(out, n)
+    assert norms["n"] == pytest.approx(np.linalg.norm(o.get_native(0, 1)), rel=1e-5)
+
