@@ -228,6 +228,63 @@ def gmg_cg_measure(refine=6, depth=7):
     return out
 
 
+def amr_measure():
+    """The reference Allen-Cahn application's adaptive configuration
+    (applications/allen_cahn/explicit/parameters.prm: [0,100]^2, global refinement 8, min 3,
+    max 8, remeshing period 800, refinement where 0.01 < n < 0.99; Q1) on seeded grains: the
+    initial refinement passes, the explicit increments 3..799 (no remeshing), the remeshing
+    increment 800, and the same number of increments on the uniform 256^2 mesh of the finest
+    level."""
+    import numpy as np
+    import torch
+    from phasefield_gb300 import workloads as W
+    wl = W.allen_cahn_amr_2d(refine=8, degree=1, min_level=3, max_level=8, period=800, n_grains=12, size=100.0,
+                             dt=0.01)
+    p = wl.make_problem()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p.solve(0)
+    torch.cuda.synchronize()
+    init_s = time.perf_counter() - t0
+    dofs0 = p.n_nodes
+    levels0 = np.bincount(p.cells()[:, 0], minlength=9).tolist()
+    p.solve(2)
+    torch.cuda.synchronize()
+    # increments 3 .. 799 hold no remeshing step; increment 800 remeshes
+    t0 = time.perf_counter()
+    p.solve(799)
+    torch.cuda.synchronize()
+    ada_s = time.perf_counter() - t0
+    v0 = p.mesh_version
+    t0 = time.perf_counter()
+    p.solve(800)
+    torch.cuda.synchronize()
+    remesh_s = time.perf_counter() - t0
+    assert p.mesh_version == v0 + 1
+    dofs1 = p.n_nodes
+    p.close()
+    steps = 797
+    wu = W.allen_cahn_2d(refine=8, degree=1, n_grains=12, size=100.0, dt=0.01)
+    pu = wu.make_problem()
+    pu.solve(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pu.solve(2 + steps)
+    torch.cuda.synchronize()
+    uni_s = time.perf_counter() - t0
+    dofs_u = pu.n_nodes
+    pu.close()
+    return {"workload": "Allen-Cahn [0,100]^2 Q1, 12 seeded grains, global refinement 8, min 3, max 8, "
+                        "remeshing period 800, refine where 0.01 < n < 0.99, dt 0.01",
+            "steps": steps, "initial_refinement_s": init_s, "dofs_after_initial_refinement": dofs0,
+            "cells_per_level": levels0, "dofs_after_remesh": dofs1,
+            "adaptive_ms_per_step": ada_s / steps * 1e3,
+            "adaptive_dof_updates_per_s": dofs0 * steps / ada_s,
+            "remeshing_increment_ms": remesh_s * 1e3,
+            "uniform_finest_dofs": dofs_u, "uniform_finest_ms_per_step": uni_s / steps * 1e3,
+            "speedup_adaptive_vs_uniform_finest": uni_s / ada_s}
+
+
 def ensemble_measure(steps=30):
     """Aggregate DoF-updates/s of the 256-instance Allen-Cahn ensemble (cells per side
     32..256, Q1/Q2, per-instance m_well/kappa, grain ICs), one persistent launch per step
@@ -420,6 +477,7 @@ def run_ours(args):
         gmg = gmg_cg_measure() if not args.skip_extras else None
         ens = ensemble_measure() if not args.skip_extras else None
         adj = adjoint_measure() if not args.skip_extras else None
+        amr = amr_measure() if not args.skip_extras else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": max_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -433,7 +491,7 @@ def run_ours(args):
                 "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
                                   "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
                                   "flops_per_launch": flops_per_launch, "peak_source": "measured in this run"},
-                "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens, "adjoint": adj}
+                "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens, "adjoint": adj, "amr": amr}
         print(json.dumps(line), flush=True)
     p.close()
     if ws > 1:
@@ -555,7 +613,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--skip-extras", action="store_true", help="omit the GMG-CG and ensemble measurements")
+    ap.add_argument("--skip-extras", action="store_true", help="omit the GMG-CG, ensemble, adjoint and adaptive-mesh measurements")
     ap.add_argument("--sharded", action="store_true",
                     help="run the sharded simulation also on one GPU (more than one GPU always shards)")
     args = ap.parse_args()

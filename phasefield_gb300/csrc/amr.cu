@@ -43,18 +43,39 @@ struct AmrState {
 
 namespace {
 
-// u = invM (.) acc on free rows, Dirichlet values on Dirichlet rows; hanging rows are written by
-// amr_hanging_kernel afterwards (the reference's invM is 0 there and distribute() sets them)
+// value of a free or Dirichlet row after the explicit update
+__device__ __forceinline__ double amr_final_value(const double* __restrict__ acc, const double* __restrict__ invm,
+                                                  const int* __restrict__ cmap, const double* __restrict__ dvals,
+                                                  long long gi, long long i) {
+  const int cm = cmap ? cmap[gi] : (int)gi;
+  return cm == (int)gi ? invm[i] * acc[gi] : dvals[-1 - cm];
+}
+
+// The explicit update u = invM (.) acc followed by distribute(): free rows scale their
+// accumulator, Dirichlet rows take their values, hanging rows the interpolant of their masters'
+// final values (computed here from the masters' accumulators, so one launch does all rows; the
+// reference's invM is 0 on hanging rows and distribute() sets them)
 __global__ void amr_finalize_kernel(double* __restrict__ u, const double* __restrict__ acc,
                                     const double* __restrict__ invm, const int* __restrict__ cmap,
-                                    const double* __restrict__ dvals, long long N, int* err) {
+                                    const double* __restrict__ dvals, const int* __restrict__ h_ptr,
+                                    const int* __restrict__ h_idx, const double* __restrict__ h_w, long long N,
+                                    int* err) {
   const long long base = blockIdx.y * N;
   int bad = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
     const long long gi = base + i;
     const int cm = cmap ? cmap[gi] : (int)gi;
-    if (cm >= AMR_HANG_BASE) continue;
-    const double v = cm == (int)gi ? invm[i] * acc[gi] : dvals[-1 - cm];
+    double v;
+    if (cm >= AMR_HANG_BASE) {
+      const int r = cm - AMR_HANG_BASE;
+      v = 0.0;
+      for (int e = h_ptr[r]; e < h_ptr[r + 1]; ++e) {
+        const long long m = h_idx[e];
+        v += h_w[e] * amr_final_value(acc, invm, cmap, dvals, base + m, m);
+      }
+    } else {
+      v = cm == (int)gi ? invm[i] * acc[gi] : dvals[-1 - cm];
+    }
     bad |= !isfinite(v);
     u[gi] = v;
   }
@@ -340,16 +361,20 @@ int amr_finalize_explicit(ppf_handle h, FieldState& F) {
   AmrState& S = *h->amr;
   dim3 grid(grid_for(h->N), F.ncomp);
   amr_finalize_kernel<<<grid, 256, 0, h->stream>>>(F.cur, F.acc, h->d_invm, F.constrained ? F.cmap : nullptr, F.dvals,
-                                                   h->N, h->d_err);
+                                                   S.d_h_ptr, S.d_h_idx, S.d_h_w, h->N, h->d_err);
   PPF_CUDA(h, cudaGetLastError());
   h->all_launches++;
-  if (S.nrows > 0) {
-    dim3 g2(grid_for(S.nrows), F.ncomp);
-    amr_hanging_kernel<<<g2, 256, 0, h->stream>>>(F.cur, S.d_h_dof, S.d_h_ptr, S.d_h_idx, S.d_h_w, S.nrows, h->N);
-    PPF_CUDA(h, cudaGetLastError());
-    h->all_launches++;
-  }
   return PPF_OK;
+}
+
+// the first increment at or after `inc` whose remeshing step runs (UINT_MAX: none)
+unsigned amr_next_remesh(ppf_handle h, unsigned inc) {
+  const AmrState& S = *h->amr;
+  if (inc == 0) return 0;
+  if (S.period <= 0) return ~0u;
+  const unsigned p = (unsigned)S.period;
+  const unsigned long long next = ((unsigned long long)inc + p - 1) / p * p;
+  return next > 0xfffffffeULL ? ~0u : (unsigned)next;
 }
 
 int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
@@ -382,15 +407,15 @@ int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, dou
         for (int d = 0; d < h->dim; ++d)
           if (m.periodic[d] && p[d] == m.E[d]) p[d] = 0;
         if (h->dim < 3) p[2] = 0;
-        auto it = m.node_of.find(m.pos_key(p));
-        if (it == m.node_of.end()) return fail(h, PPF_ERR_CUDA, "internal: lattice node without a DoF");
+        const int dof = m.node_of.find(m.pos_key(p));
+        if (dof < 0) return fail(h, PPF_ERR_CUDA, "internal: lattice node without a DoF");
         // a periodic image reads its master on download; on upload the master's value is kept
         const bool image = (p[0] != (I << shift)) || (p[1] != (J << shift)) || (h->dim == 3 && p[2] != (K << shift));
         for (int c = 0; c < F.ncomp; ++c) {
           if (upload) {
-            if (!image) nat[c * m.N + it->second] = host[c * nlat + lat];
+            if (!image) nat[c * m.N + dof] = host[c * nlat + lat];
           } else {
-            host[c * nlat + lat] = nat[c * m.N + it->second];
+            host[c * nlat + lat] = nat[c * m.N + dof];
           }
         }
       }

@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <functional>
+#include <thread>
+#include <unordered_map>
 #include <unordered_set>
 
 namespace ppf {
@@ -56,7 +58,35 @@ void covering(const AmrMesh& m, int lev, long long y0, long long y1, long long y
     out.push_back(i);
     return;
   }
-  for (int l = lev - 1; l >= 0; --l) {
+  // a balanced mesh has the region's parent or its children active: try those first
+  if (lev > 0) {
+    const int a = m.find(lev - 1, y0 >> 1, y1 >> 1, y2 >> 1);
+    if (a >= 0) {
+      out.push_back(a);
+      return;
+    }
+  }
+  if (lev < m.maxlev) {
+    const size_t before = out.size();
+    bool all = true;
+    for (int ch = 0; ch < (1 << m.dim) && all; ++ch) {
+      long long c[3] = {0, 0, 0};
+      bool ok = true;
+      for (int d = 0; d < m.dim; ++d) {
+        const int b = (ch >> d) & 1;
+        if (dir[d] > 0 && b != 1) ok = false;
+        if (dir[d] < 0 && b != 0) ok = false;
+        c[d] = 2 * (d == 0 ? y0 : d == 1 ? y1 : y2) + b;
+      }
+      if (!ok) continue;
+      const int j = m.find(lev + 1, c[0], c[1], c[2]);
+      if (j >= 0) out.push_back(j);
+      else all = false;
+    }
+    if (all && out.size() > before) return;
+    out.resize(before);
+  }
+  for (int l = lev - 2; l >= 0; --l) {
     const int s = lev - l;
     const int a = m.find(l, y0 >> s, y1 >> s, y2 >> s);
     if (a >= 0) {
@@ -79,29 +109,28 @@ void covering(const AmrMesh& m, int lev, long long y0, long long y1, long long y
   }
 }
 
-// active cells touching cell c (sharing at least a vertex); with face_axis >= 0 only the cells
-// across face (face_axis, face_side)
-void touching(const AmrMesh& m, int c, std::vector<int>& out, int face_axis = -1, int face_side = 0) {
-  out.clear();
+// Neighbours of cell c: the active cells touching it (sharing at least a vertex), appended to
+// `touch` without c itself or repeats, and per face (axis, side) whether a neighbour exists and
+// whether one of them is finer than c or flagged for refinement at c's level (`fine` per face
+// is filled by the caller from `faces`, the face neighbours appended per face).
+void neighbours(const AmrMesh& m, int c, std::vector<int>& touch, std::vector<int> faces[6], std::vector<int>& scratch) {
   const AmrCell& C = m.cells[c];
   const int nd = m.dim;
   int total = 1;
   for (int d = 0; d < nd; ++d) total *= 3;
+  const size_t t0 = touch.size();
   for (int t = 0; t < total; ++t) {
     int delta[3] = {0, 0, 0};
-    int r = t;
-    bool zero = true;
+    int r = t, nz = 0, axis = -1;
     for (int d = 0; d < nd; ++d) {
       delta[d] = r % 3 - 1;
       r /= 3;
-      zero &= delta[d] == 0;
+      if (delta[d] != 0) {
+        ++nz;
+        axis = d;
+      }
     }
-    if (zero) continue;
-    if (face_axis >= 0) {
-      bool ok = true;
-      for (int d = 0; d < nd; ++d) ok &= d == face_axis ? delta[d] == (face_side ? 1 : -1) : delta[d] == 0;
-      if (!ok) continue;
-    }
+    if (nz == 0) continue;
     long long y[3] = {0, 0, 0};
     bool inside = true;
     for (int d = 0; d < nd; ++d) {
@@ -110,11 +139,16 @@ void touching(const AmrMesh& m, int c, std::vector<int>& out, int face_axis = -1
     }
     if (!inside) continue;
     const int back[3] = {-delta[0], -delta[1], -delta[2]};
-    covering(m, C.lev, y[0], y[1], y[2], back, out);
+    scratch.clear();
+    covering(m, C.lev, y[0], y[1], y[2], back, scratch);
+    for (int b : scratch) {
+      if (b == c) continue;
+      touch.push_back(b);
+      if (nz == 1) faces[2 * axis + (delta[axis] > 0)].push_back(b);
+    }
   }
-  std::sort(out.begin(), out.end());
-  out.erase(std::unique(out.begin(), out.end()), out.end());
-  out.erase(std::remove(out.begin(), out.end(), c), out.end());
+  std::sort(touch.begin() + t0, touch.end());
+  touch.erase(std::unique(touch.begin() + t0, touch.end()), touch.end());
 }
 
 uint64_t path_key(const AmrMesh& m, const AmrCell& c) {
@@ -161,6 +195,58 @@ int first_containing(const AmrMesh& m, int lev, const std::array<long long, 3>& 
 
 }  // namespace
 
+static inline uint64_t mix64(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdULL;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ULL;
+  k ^= k >> 33;
+  return k;
+}
+
+void KeyTable::reset(size_t expected) {
+  size_t cap = 16;
+  while (cap < 2 * expected + 2) cap <<= 1;
+  keys_.assign(cap, EMPTY);
+  vals_.assign(cap, -1);
+  mask_ = cap - 1;
+  count_ = 0;
+}
+
+int KeyTable::find(uint64_t key) const {
+  if (keys_.empty()) return -1;
+  for (uint64_t i = mix64(key) & mask_;; i = (i + 1) & mask_) {
+    if (keys_[i] == key) return vals_[i];
+    if (keys_[i] == EMPTY) return -1;
+  }
+}
+
+void KeyTable::grow() {
+  std::vector<uint64_t> k = std::move(keys_);
+  std::vector<int> v = std::move(vals_);
+  reset(k.size());
+  bool ins;
+  for (size_t i = 0; i < k.size(); ++i)
+    if (k[i] != EMPTY) insert(k[i], v[i], ins);
+}
+
+int KeyTable::insert(uint64_t key, int value, bool& inserted) {
+  if (keys_.empty() || 2 * (count_ + 1) > keys_.size()) grow();
+  for (uint64_t i = mix64(key) & mask_;; i = (i + 1) & mask_) {
+    if (keys_[i] == key) {
+      inserted = false;
+      return vals_[i];
+    }
+    if (keys_[i] == EMPTY) {
+      keys_[i] = key;
+      vals_[i] = value;
+      ++count_;
+      inserted = true;
+      return value;
+    }
+  }
+}
+
 uint64_t AmrMesh::cell_key(int lev, long long x, long long y, long long z) const {
   return ((uint64_t)lev << (3 * KEY_BITS)) | ((uint64_t)z << (2 * KEY_BITS)) | ((uint64_t)y << KEY_BITS) | (uint64_t)x;
 }
@@ -170,8 +256,7 @@ uint64_t AmrMesh::pos_key(const std::array<long long, 3>& p) const {
 }
 
 int AmrMesh::find(int lev, long long x, long long y, long long z) const {
-  auto it = index.find(cell_key(lev, x, y, z));
-  return it == index.end() ? -1 : it->second;
+  return index.find(cell_key(lev, x, y, z));
 }
 
 void amr_set_cells(AmrMesh& m, std::vector<AmrCell> cells) {
@@ -192,12 +277,12 @@ void amr_set_cells(AmrMesh& m, std::vector<AmrCell> cells) {
     return a.coarse != b.coarse ? a.coarse < b.coarse : a.path < b.path;
   });
   m.cells.resize(items.size());
-  m.index.clear();
-  m.index.reserve(items.size() * 2);
+  m.index.reset(items.size());
   for (size_t i = 0; i < items.size(); ++i) {
     m.cells[i] = items[i].c;
     const AmrCell& c = m.cells[i];
-    m.index[m.cell_key(c.lev, c.x[0], c.x[1], c.x[2])] = (int)i;
+    bool ins;
+    m.index.insert(m.cell_key(c.lev, c.x[0], c.x[1], c.x[2]), (int)i, ins);
   }
 }
 
@@ -242,8 +327,7 @@ void amr_build(AmrMesh& m) {
   const long long nc = m.ncells();
   m.cell_dofs.assign((size_t)nc * nq, 0);
   m.pos.clear();
-  m.node_of.clear();
-  m.node_of.reserve((size_t)nc * nq);
+  m.node_of.reset((size_t)nc * (m.dim == 2 ? 2 : 3));
   std::vector<int> minlev;
   for (long long c = 0; c < nc; ++c) {
     const AmrCell& C = m.cells[c];
@@ -257,15 +341,12 @@ void amr_build(AmrMesh& m) {
         p[d] = q;
       }
       const uint64_t key = m.pos_key(p);
-      auto it = m.node_of.find(key);
-      int dof;
-      if (it == m.node_of.end()) {
-        dof = (int)m.pos.size();
-        m.node_of.emplace(key, dof);
+      bool fresh;
+      const int dof = m.node_of.insert(key, (int)m.pos.size(), fresh);
+      if (fresh) {
         m.pos.push_back(p);
         minlev.push_back(C.lev);
       } else {
-        dof = it->second;
         minlev[dof] = std::min(minlev[dof], C.lev);
       }
       m.cell_dofs[(size_t)c * nq + l] = dof;
@@ -336,30 +417,85 @@ void amr_build(AmrMesh& m) {
 void amr_smooth(const AmrMesh& m, std::vector<signed char>& flag, int max_level) {
   const int nc = (int)m.ncells();
   const int nchild = 1 << m.dim;
-  std::vector<std::vector<int>> touch(nc);
-  for (int c = 0; c < nc; ++c) touching(m, c, touch[c]);
-  std::vector<std::vector<std::vector<int>>> faces(nc, std::vector<std::vector<int>>(2 * m.dim));
-  for (int c = 0; c < nc; ++c)
-    for (int d = 0; d < m.dim; ++d)
-      for (int s = 0; s < 2; ++s) touching(m, c, faces[c][2 * d + s], d, s);
-  auto parent = [&](int c) {
+  const int nf = 2 * m.dim;
+  // neighbour lists, flat: touching cells and face neighbours per (cell, face); built by
+  // independent chunks of cells on host threads, then joined in cell order
+  std::vector<int> t_ptr(nc + 1, 0), touch, f_ptr((size_t)nc * nf + 1, 0), fnb;
+  {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int nchunk = (int)std::min<long long>(hw, std::max(1, nc / 2048));
+    struct Part {
+      std::vector<int> touch, tcount, fnb, fcount;
+    };
+    std::vector<Part> parts(nchunk);
+    auto work = [&](int k) {
+      Part& P = parts[k];
+      const int c0 = (int)((long long)nc * k / nchunk), c1 = (int)((long long)nc * (k + 1) / nchunk);
+      std::vector<int> faces[6], scratch;
+      for (int c = c0; c < c1; ++c) {
+        for (int f = 0; f < nf; ++f) faces[f].clear();
+        const size_t t0 = P.touch.size();
+        neighbours(m, c, P.touch, faces, scratch);
+        P.tcount.push_back((int)(P.touch.size() - t0));
+        for (int f = 0; f < nf; ++f) {
+          std::sort(faces[f].begin(), faces[f].end());
+          faces[f].erase(std::unique(faces[f].begin(), faces[f].end()), faces[f].end());
+          P.fnb.insert(P.fnb.end(), faces[f].begin(), faces[f].end());
+          P.fcount.push_back((int)faces[f].size());
+        }
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int k = 1; k < nchunk; ++k) pool.emplace_back(work, k);
+    work(0);
+    for (auto& t : pool) t.join();
+    int c = 0;
+    size_t cf = 0;
+    for (const Part& P : parts) {
+      touch.insert(touch.end(), P.touch.begin(), P.touch.end());
+      fnb.insert(fnb.end(), P.fnb.begin(), P.fnb.end());
+      for (int n : P.tcount) {
+        t_ptr[c + 1] = t_ptr[c] + n;
+        ++c;
+      }
+      for (int n : P.fcount) {
+        f_ptr[cf + 1] = f_ptr[cf] + n;
+        ++cf;
+      }
+    }
+  }
+  // in tree order a family of active siblings is the 2^dim consecutive cells starting at the
+  // first child: complete when all of them are active at the child's level under one parent
+  auto complete_family = [&](int c) {
     const AmrCell& C = m.cells[c];
-    return m.cell_key(C.lev - 1, C.x[0] >> 1, C.x[1] >> 1, C.x[2] >> 1);
+    int ci = 0;
+    for (int d = 0; d < m.dim; ++d) ci |= (C.x[d] & 1) << d;
+    const int s = c - ci;
+    if (s < 0 || s + nchild > nc) return false;
+    for (int j = 0; j < nchild; ++j) {
+      const AmrCell& S = m.cells[s + j];
+      if (S.lev != C.lev || flag[s + j] != -1) return false;
+      for (int d = 0; d < m.dim; ++d)
+        if ((S.x[d] >> 1) != (C.x[d] >> 1) || (S.x[d] & 1) != ((j >> d) & 1)) return false;
+    }
+    return true;
   };
   auto target = [&](int c) { return m.cells[c].lev + (flag[c] == 1) - (flag[c] == -1); };
+  std::vector<char> clear;
   for (;;) {
     bool changed = false;
-    std::unordered_map<uint64_t, int> fam;
+    clear.assign(nc, 0);
     for (int c = 0; c < nc; ++c)
-      if (flag[c] == -1) fam[parent(c)]++;
+      if (flag[c] == -1 && !complete_family(c)) clear[c] = 1;
     for (int c = 0; c < nc; ++c)
-      if (flag[c] == -1 && fam[parent(c)] != nchild) {
+      if (clear[c]) {
         flag[c] = 0;
         changed = true;
       }
     for (int a = 0; a < nc; ++a) {
       const int ta = target(a);
-      for (int b : touch[a]) {
+      for (int e = t_ptr[a]; e < t_ptr[a + 1]; ++e) {
+        const int b = touch[e];
         if (ta <= target(b) + 1) continue;
         const signed char nf = flag[b] == -1 ? 0 : 1;
         if (nf != flag[b]) {
@@ -371,12 +507,14 @@ void amr_smooth(const AmrMesh& m, std::vector<signed char>& flag, int max_level)
     for (int a = 0; a < nc; ++a) {
       if (flag[a] == 1) continue;
       int refined = 0, unrefined = 0;
-      for (int f = 0; f < 2 * m.dim; ++f) {
-        const auto& nb = faces[a][f];
-        if (nb.empty()) continue;  // domain boundary
+      for (int f = 0; f < nf; ++f) {
+        const int e0 = f_ptr[(size_t)a * nf + f], e1 = f_ptr[(size_t)a * nf + f + 1];
+        if (e0 == e1) continue;  // domain boundary
         bool fine = false;
-        for (int b : nb)
+        for (int e = e0; e < e1; ++e) {
+          const int b = fnb[e];
           fine |= m.cells[b].lev > m.cells[a].lev || (m.cells[b].lev == m.cells[a].lev && flag[b] == 1);
+        }
         if (fine) ++refined;
         else ++unrefined;
       }
@@ -416,9 +554,9 @@ void amr_transfer_plan(const AmrMesh& old, const AmrMesh& m, std::vector<int>& p
   w.clear();
   const int nq = m.nq, n = m.n;
   for (long long p = 0; p < m.N; ++p) {
-    auto it = old.node_of.find(old.pos_key(m.pos[p]));
-    if (it != old.node_of.end()) {
-      idx.push_back(it->second);
+    const int same = old.node_of.find(old.pos_key(m.pos[p]));
+    if (same >= 0) {
+      idx.push_back(same);
       w.push_back(1.0);
       ptr.push_back((int)idx.size());
       continue;

@@ -24,7 +24,6 @@
 #include <array>
 #include <cstdint>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 namespace ppf {
@@ -34,6 +33,24 @@ struct AmrCell {
   int x[3];
 };
 
+// 64-bit key -> int table with open addressing (linear probing, power-of-two capacity at most
+// half full); keys are cell and position keys, which never use the all-ones pattern.
+class KeyTable {
+ public:
+  void reset(size_t expected);  // empties the table, sized for `expected` keys
+  int find(uint64_t key) const;  // value or -1
+  // the value stored for `key`, or `value` after inserting it (inserted tells which)
+  int insert(uint64_t key, int value, bool& inserted);
+
+ private:
+  static constexpr uint64_t EMPTY = ~0ULL;
+  void grow();
+  std::vector<uint64_t> keys_;
+  std::vector<int> vals_;
+  uint64_t mask_ = 0;
+  size_t count_ = 0;
+};
+
 struct AmrMesh {
   int dim = 2, k = 1, n = 2, nq = 4;
   int sub[3] = {1, 1, 1};
@@ -41,11 +58,11 @@ struct AmrMesh {
   int maxlev = 0;
   long long E[3] = {1, 1, 1};                 // extent in node units at level maxlev
   std::vector<AmrCell> cells;                 // active cells in tree order
-  std::unordered_map<uint64_t, int> index;    // cell key -> active cell index
+  KeyTable index;                             // cell key -> active cell index
   long long N = 0;                            // DoFs (nodes)
   std::vector<int> cell_dofs;                 // ncells * nq, lexicographic cell nodes
   std::vector<std::array<long long, 3>> pos;  // node position of every DoF
-  std::unordered_map<uint64_t, int> node_of;  // position key -> DoF
+  KeyTable node_of;                           // position key -> DoF
   // closed hanging-node lines: row r constrains DoF h_dof[r] to
   // sum_{e in [h_ptr[r], h_ptr[r+1])} h_w[e] * u[h_idx[e]] (masters ascending, none hanging)
   std::vector<int> hang_row;                  // per DoF: its row or -1

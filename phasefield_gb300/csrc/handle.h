@@ -165,6 +165,7 @@ struct ppf_handle_s {
   ppf::AdjointState* adj = nullptr;  // adjoint / tangent-linear state (created on first use)
   ppf::AmrState* amr = nullptr;      // adaptive mesh (ppf_set_adaptivity), else null
   long long mesh_version = 0;
+  long long graph_mesh_version = -1;  // mesh the increment graph was captured on
   // CUDA graph of the explicit increment loop
   prismspf::SimulationTimer* d_timer = nullptr;
   cudaGraphExec_t run_graph = nullptr;
@@ -211,6 +212,7 @@ void free_adjoint(AdjointState* A);
 int amr_launch_cell(ppf_handle h, int b, int which, const CellLaunch& L);
 int amr_finalize_explicit(ppf_handle h, FieldState& F);
 int amr_remesh_if_due(ppf_handle h);
+unsigned amr_next_remesh(ppf_handle h, unsigned inc);
 int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
                    bool upload);
 int amr_apply_constraints(ppf_handle h, FieldState& F, double* v);

@@ -1078,9 +1078,9 @@ int ppf_solve_block(ppf_handle h, int b) {
 // were), each followed by a device-side timer advance; callbacks read the timer from device
 // memory during replays, so time-dependent operators see the right time.
 static bool graph_eligible(ppf_handle h, int output_every) {
-  // per-launch event timing needs plain launches; postprocess increments are not periodic;
-  // adaptive meshes change their vectors when they remesh
-  if (!h->use_graph || h->timing || output_every > 0 || h->amr) return false;
+  // per-launch event timing needs plain launches; postprocess increments are not periodic
+  // (adaptive meshes replay only between remeshing increments, see ppf_run)
+  if (!h->use_graph || h->timing || output_every > 0) return false;
   for (auto& B : h->blocks) {
     const int t = B.desc.solve_type;
     if (t != PPF_EXPLICIT && t != PPF_CONSTANT) return false;
@@ -1137,6 +1137,7 @@ static int capture_graph(ppf_handle h) {
   h->graph_launches = h->all_launches - launches0;
   h->all_launches = launches0;
   h->graph_stream = h->stream;
+  h->graph_mesh_version = h->mesh_version;
   return PPF_OK;
 }
 
@@ -1148,9 +1149,17 @@ int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
     // so every kernel has been configured before a capture
     if (inc >= 2 && graph_eligible(h, output_every)) {
       const int period = rotation_period(h);
-      const unsigned remaining = n_increments - inc + 1;
+      // on adaptive meshes a replay stops before the next remeshing increment, which changes
+      // the vectors the graph holds
+      unsigned last = n_increments;
+      if (h->amr) {
+        const unsigned nr = amr_next_remesh(h, inc);
+        if (nr != ~0u && nr - 1 < last) last = nr - 1;
+      }
+      const unsigned remaining = last >= inc ? last - inc + 1 : 0;
       if (remaining >= (unsigned)period) {
-        if (!h->run_graph || h->graph_stream != h->stream || h->graph_phase != h->rot_count % period) {
+        if (!h->run_graph || h->graph_stream != h->stream || h->graph_phase != h->rot_count % period ||
+            h->graph_mesh_version != h->mesh_version) {
           int rc = capture_graph(h);
           if (rc) return rc;
         }
