@@ -255,8 +255,7 @@ int ppf_lhs_diagonal(ppf_handle h, int b, double* out);
 
 /* ---- Adaptive meshes ----------------------------------------------------------------------
  * Mesh adaptivity of RefinementManager (src/core/refinement_manager.cc:42-439) with deal.II's
- * refinement smoothing, hanging-node constraints and solution transfer, for degrees 1 and 2 and
- * Explicit, Constant and PostProcess blocks.
+ * refinement smoothing, hanging-node constraints and solution transfer, for degrees 1 and 2.
  *
  * The mesh is a forest of quadtrees / octrees over the coarse subdivided rectangle. It starts
  * uniform at the global refinement (the initial condition is uploaded on that mesh, in lattice
@@ -293,8 +292,10 @@ typedef struct {
 } ppf_adaptivity;
 
 /* Makes the handle's mesh adaptive; call right after ppf_create / ppf_create_custom (field
- * states are reset). Fails with PPF_ERR_UNSUPPORTED for degree > 2, Linear or Newton blocks,
- * or meshes too fine for the position encoding. */
+ * states are reset). Fails with PPF_ERR_UNSUPPORTED for degree > 2 or meshes too fine for the
+ * position encoding. Linear and Newton blocks solve without a preconditioner on adaptive meshes
+ * (the reference refuses multigrid with adaptivity); their warm starts restart from zero after
+ * a remesh. */
 int ppf_set_adaptivity(ppf_handle h, const ppf_adaptivity* a);
 
 /* One remeshing pass now (RefinementManager::do_adaptive_refinement). */

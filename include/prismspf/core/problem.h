@@ -22,8 +22,8 @@
 //   * a non-finite solution writes the output of that increment and throws ExcNaN;
 //   * "mesh adaptivity = true": the engine's adaptive mesh (ppf_set_adaptivity) with the
 //     parameter file's min/max refinement, remeshing period and refinement criteria, for
-//     degrees 1 and 2 and Explicit, Constant and PostProcess blocks (other configurations run
-//     on the uniform mesh with a note); the initial condition is set on the initial uniform
+//     degrees 1 and 2 (other degrees run on the uniform mesh with a note; Linear and Newton
+//     blocks without a preconditioner); the initial condition is set on the initial uniform
 //     mesh and carried through the refinement passes as the reference's solution transfer does,
 //     Dirichlet values come from set_dirichlet at the nodes of every mesh, and the output
 //     writes the active cells of the current mesh.
@@ -230,15 +230,18 @@ class Problem {
     if (handle) return;
     const auto& sd = user_inputs->spatial_discretization;
     const auto& mesh = sd.rectangular_mesh;
-    // adaptive meshes (refinement_manager.cc) for degrees 1 and 2 with Explicit, Constant and
-    // PostProcess blocks; other configurations run on the uniform mesh with a note
+    // adaptive meshes (refinement_manager.cc) for degrees 1 and 2; other configurations run on
+    // the uniform mesh with a note. Linear and Newton blocks solve without a preconditioner there
+    // (problem.cc:356-359 refuses multigrid with adaptivity).
     adaptive = false;
     if (sd.has_adaptivity) {
+      for (const auto& sb : solve_blocks)
+        if ((sb.solve_type == SolveType::Linear || sb.solve_type == SolveType::Newton) &&
+            sb.linear_solver_parameters.preconditioner != PreconditionerType::None)
+          throw std::invalid_argument("AMR cannot be enabled when using multigrid preconditioners currently.");
       std::string why;
       if (dim < 2) why = "one-dimensional meshes";
       else if (degree > 2) why = "degree > 2";
-      for (const auto& sb : solve_blocks)
-        if (sb.solve_type == SolveType::Linear || sb.solve_type == SolveType::Newton) why = "Linear or Newton blocks";
       if (why.empty()) {
         if (sd.max_refinement < sd.global_refinement)
           throw std::invalid_argument("The maximum refinement level must be greater than or equal to the global refinement level.");

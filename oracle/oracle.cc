@@ -2073,6 +2073,15 @@ static void remesh(Problem& P) {
     move(F.cur);
     for (int a = 0; a < F.n_old; ++a) move(F.old[a]);
   }
+  // linear and Newton solvers start over on the new mesh (warm starts from zero)
+  for (auto& B : P.blocks) {
+    for (auto& L : B.levels)
+      if (L.owned) delete L.P;
+    B.levels.clear();
+    B.lin_init = false;
+    B.x_hom.clear();
+    B.newton_update.clear();
+  }
 }
 
 static int enable_adaptivity(Problem& P, int min_level, int max_level, int period) {

@@ -367,6 +367,16 @@ int amr_finalize_explicit(ppf_handle h, FieldState& F) {
   return PPF_OK;
 }
 
+void amr_fill_hanging(ppf_handle h, int ncomp, double* v) {
+  const AmrMesh& m = h->amr->mesh;
+  for (int c = 0; c < ncomp; ++c)
+    for (size_t r = 0; r < m.h_dof.size(); ++r) {
+      double s = 0.0;
+      for (int e = m.h_ptr[r]; e < m.h_ptr[r + 1]; ++e) s += m.h_w[e] * v[c * m.N + m.h_idx[e]];
+      v[c * m.N + m.h_dof[r]] = s;
+    }
+}
+
 // the first increment at or after `inc` whose remeshing step runs (UINT_MAX: none)
 unsigned amr_next_remesh(ppf_handle h, unsigned inc) {
   const AmrState& S = *h->amr;
@@ -596,9 +606,6 @@ int ppf_set_adaptivity(ppf_handle h, const ppf_adaptivity* a) {
       a->max_refinement - a->min_refinement + 1 > AMR_MAX_LEVELS)
     return fail(h, PPF_ERR_ARG, "refinement levels: need min <= global refinement <= max");
   if (a->n_criteria < 0 || a->n_criteria > PPF_MAX_FIELDS) return PPF_ERR_ARG;
-  for (auto& B : h->blocks)
-    if (B.desc.solve_type == PPF_LINEAR || B.desc.solve_type == PPF_NEWTON)
-      return fail(h, PPF_ERR_UNSUPPORTED, "Linear and Newton blocks on adaptive meshes");
   for (int d = 0; d < h->dim; ++d)
     if (h->mesh.periodic[d] && ((long long)h->mesh.subdivisions[d] << a->min_refinement) < 2)
       return fail(h, PPF_ERR_UNSUPPORTED, "a periodic direction needs two cells at the minimum refinement");

@@ -124,6 +124,7 @@ struct LinearState {
   int last_newton_iterations = 0;
   int last_newton_linear_iterations = 0;
   double last_newton_residual = 0.0;
+  long long mesh_version = -1;      // mesh the work vectors were sized for (adaptive meshes)
 };
 
 struct BlockState {
@@ -201,7 +202,8 @@ int check_err(ppf_handle h);
 double* state_ptr(ppf_handle h, int f, int age);
 // records a kernel launch for the statistics; brackets cell launches with events when timing
 int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L, const void* obj, size_t smem);
-int launch_cell(ppf_handle h, int b, int which, const double* const* src);
+// plain_src: the LHS reads src without the homogeneous constraints (the inhomogeneous lift)
+int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool plain_src = false);
 int linear_solve(ppf_handle h, int b);
 int newton_solve(ppf_handle h, int b);
 void free_linear(LinearState& L);
@@ -216,6 +218,8 @@ unsigned amr_next_remesh(ppf_handle h, unsigned inc);
 int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, double* dev_dst, int ordering,
                    bool upload);
 int amr_apply_constraints(ppf_handle h, FieldState& F, double* v);
+// hanging entries of a host vector (ncomp components) from their masters
+void amr_fill_hanging(ppf_handle h, int ncomp, double* v);
 void free_amr(AmrState* A);
 
 }  // namespace ppf

@@ -891,7 +891,31 @@ int linear_solve(ppf_handle h, int b) {
   BlockState& B = h->blocks[b];
   LinearState& L = B.lin;
   L.last_init_ms = 0.0;
-  if (!L.initialized) {
+  if (h->amr) {
+    // adaptive meshes: CG without a preconditioner on the current mesh's vectors, which are
+    // re-made (warm start from zero) whenever the mesh changes
+    if (!L.params_set) {
+      ppf_default_linear_params(&L.params);
+      L.params_set = true;
+    }
+    if (L.params.preconditioner != 0)
+      return fail(h, PPF_ERR_UNSUPPORTED, "adaptive meshes: linear solves run without a preconditioner");
+    if (B.desc.n_fields != 1) return fail(h, PPF_ERR_UNSUPPORTED, "linear blocks with more than one field");
+    if (!B.plan[1].valid) return fail(h, PPF_ERR_ARG, "linear block has no LHS dependencies or no compiled LHS");
+    if (L.mesh_version != h->mesh_version || !L.initialized) {
+      const long long len = h->fields[B.desc.field_indices[0]].len;
+      double** vecs[] = {&L.rhs, &L.g, &L.x_hom, &L.r, &L.p, &L.q, &L.z};
+      for (double** v : vecs) {
+        cudaFree(*v);
+        *v = nullptr;
+        PPF_CUDA(h, cudaMalloc(v, sizeof(double) * len));
+      }
+      PPF_CUDA(h, cudaMemsetAsync(L.x_hom, 0, sizeof(double) * len, h->stream));
+      if (!L.partial) PPF_CUDA(h, cudaMalloc(&L.partial, sizeof(double) * 1100));
+      L.mesh_version = h->mesh_version;
+      L.initialized = true;
+    }
+  } else if (!L.initialized) {
     const auto t0 = std::chrono::steady_clock::now();
     int rc = init_linear(h, b);
     if (rc) return rc;
@@ -905,6 +929,16 @@ int linear_solve(ppf_handle h, int b) {
   auto outer_apply = [&](const double* src, double* dst, bool plain) -> int {
     const double* srcs[PPF_MAX_FIELDS] = {src};
     PPF_CUDA(h, cudaMemsetAsync(F.acc, 0, sizeof(double) * n, h->stream));
+    if (h->amr) {
+      int rc = launch_cell(h, b, 1, srcs, plain);
+      if (rc) return rc;
+      dim3 grid(grid_for(h->N), F.ncomp);
+      level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>(dst, F.acc, scaled(L) ? h->d_invm_sqrt : nullptr,
+                                                                 F.constrained ? F.cmap : nullptr, h->N);
+      h->all_launches++;
+      PPF_CUDA(h, cudaGetLastError());
+      return PPF_OK;
+    }
     CellLaunch Lc;
     std::memset(&Lc, 0, sizeof(Lc));
     for (int d = 0; d < 3; ++d) {
@@ -989,6 +1023,7 @@ int linear_solve(ppf_handle h, int b) {
     std::vector<double> gh(n, 0.0);
     for (long long i = 0; i < n; ++i)
       if (F.h_cmap[i] < 0) gh[i] = F.h_dvals[-1 - F.h_cmap[i]];
+    if (h->amr) amr_fill_hanging(h, F.ncomp, gh.data());  // hanging nodes on Dirichlet faces
     PPF_CUDA(h, cudaMemcpyAsync(L.g, gh.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
     PPF_CUDA(h, cudaStreamSynchronize(h->stream));
     int rc = outer_apply(L.g, L.q, true);
@@ -1207,6 +1242,8 @@ int newton_solve(ppf_handle h, int b) {
     return fail(h, PPF_ERR_ARG, "Newton block needs compute_rhs and compute_lhs dependencies");
   if (L.params.preconditioner == 2)
     return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks: GMG levels would need the current solution on every level");
+  if (h->amr && L.params.preconditioner != 0)
+    return fail(h, PPF_ERR_UNSUPPORTED, "adaptive meshes: Newton blocks run without a preconditioner");
   if (L.params.preconditioner == 1 && nbf != 1)
     return fail(h, PPF_ERR_UNSUPPORTED, "Newton blocks: the Chebyshev preconditioner needs a single-field block");
   if (L.params.preconditioner == 1 && !L.initialized) {
@@ -1216,7 +1253,8 @@ int newton_solve(ppf_handle h, int b) {
   long long off[PPF_MAX_FIELDS + 1] = {0};
   for (int i = 0; i < nbf; ++i) off[i + 1] = off[i] + h->fields[B.desc.field_indices[i]].len;
   const long long n = off[nbf];
-  if (L.block_len != n) {
+  if (L.block_len != n || L.mesh_version != h->mesh_version) {
+    L.mesh_version = h->mesh_version;
     cudaFree(L.newton_update);
     for (double*& p : L.kv) cudaFree(p);
     PPF_CUDA(h, cudaMalloc(&L.newton_update, sizeof(double) * n));

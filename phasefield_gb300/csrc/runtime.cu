@@ -533,7 +533,7 @@ double* state_ptr(ppf_handle h, int f, int age) {
 
 // Launches the cell kernel of block b (which: 0 rhs, 1 lhs) accumulating into each block
 // field's acc. `src` supplies the SRC dependency per block field (may be null).
-int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
+int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool plain_src) {
   BlockState& B = h->blocks[b];
   BlockPlan& P = B.plan[which];
   if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
@@ -557,7 +557,7 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src) {
         if (B.desc.field_indices[i] == f) pos = i;
       if (pos < 0 || !src || !src[pos]) return fail(h, PPF_ERR_ARG, "src dependency without a src vector");
       sd.ptr = src[pos];
-      sd.constrained_read = which == 1 && F.constrained;
+      sd.constrained_read = which == 1 && F.constrained && !plain_src;
       sd.cmap = F.cmap;
     } else {
       sd.ptr = state_ptr(h, f, a);

@@ -105,3 +105,63 @@ def test_apply_constraints_interpolates_hanging_nodes():
     p.upload(1, noisy, 0, NATIVE)
     p.apply_constraints(1)
     assert np.abs(p.download(1, 0, NATIVE) - q).max() < 1e-13
+
+
+def _solver_pair(wl, lin, newton=None):
+    p = wl.make_problem()
+    o = po.Oracle(wl, adaptivity=wl.adaptivity)
+    for b, blk in enumerate(wl.blocks):
+        if blk.solve_type in (2, 3):  # Linear, Newton
+            p.set_linear_params(b, **lin)
+            o.set_linear_params(b, **lin)
+            if newton:
+                p.set_newton_params(b, **newton)
+                o.set_newton_params(b, **newton)
+    return p, o
+
+
+def _rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_newton_allen_cahn_on_an_adaptive_mesh_matches_the_oracle():
+    wl = W.allen_cahn_implicit_2d(refine=4, dt=1.0)
+    wl.adaptivity = dict(min_level=3, max_level=6, period=2, criteria=[(0, 1, 0.01, 0.99, 0.0)])
+    p, o = _solver_pair(wl, dict(tolerance_type=1, tolerance=1e-12, max_iterations=3000),
+                        dict(max_iterations=50, tolerance=1e-10))
+    n = 5
+    p.solve(n, output_every=n)
+    assert o.run(n, n) == 0
+    _same_mesh(p, o)
+    assert len(np.unique(p.cells()[:, 0])) > 1
+    for f, age in ((0, 1), (1, 0), (2, 0)):
+        assert _rel_l2(p.download(f, age, NATIVE), o.get_native(f, age)) < 1e-8, f
+
+
+def test_newton_cahn_hilliard_bicgstab_on_an_adaptive_mesh_matches_the_oracle():
+    wl = W.cahn_hilliard_implicit_2d(refine=3, dt=0.05)
+    wl.adaptivity = dict(min_level=2, max_level=4, period=2, criteria=[(0, 2, 0.0, 0.0, 0.025)])
+    p, o = _solver_pair(wl, dict(tolerance_type=1, tolerance=1e-13, max_iterations=4000, solver_type=1),
+                        dict(max_iterations=50, tolerance=1e-11))
+    n = 4
+    p.solve(n)
+    assert o.run(n) == 0
+    _same_mesh(p, o)
+    assert len(np.unique(p.cells()[:, 0])) > 1
+    assert _rel_l2(p.download(0, 1, NATIVE), o.get_native(0, 1)) < 1e-8
+    assert _rel_l2(p.download(1, 0, NATIVE), o.get_native(1, 0)) < 1e-8
+
+
+def test_linear_elasticity_on_an_adaptive_mesh_matches_the_oracle():
+    """A Linear block (vector field, CG without preconditioner) on a graded mesh with an
+    inhomogeneous Dirichlet face, so hanging nodes meet Dirichlet nodes in the lift."""
+    wl = W.eshelby_3d(refine=2, degree=2, size=16.0, n_incl=5, dim=3)
+    wl.fields[0].dirichlet = {(0, 0): 0.01, (1, 0): 0.0, (2, 0): 0.0}
+    wl.adaptivity = dict(min_level=1, max_level=3, period=1, criteria=[(0, 2, 0.02, 1e9, 0.0)])
+    p, o = _solver_pair(wl, dict(tolerance_type=1, tolerance=1e-11, max_iterations=5000))
+    p.solve(1)
+    assert o.run(1, 0) == 0
+    _same_mesh(p, o)
+    assert len(np.unique(p.cells()[:, 0])) > 1
+    assert (p.hanging()[0] > 0).any()
+    assert _rel_l2(p.download(0, 0, NATIVE), o.get_native(0, 0)) < 1e-8
