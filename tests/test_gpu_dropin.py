@@ -315,15 +315,85 @@ end
     assert o.run(n, n) == 0
     assert len(np.unique(o.cells()[:, 0])) > 1
     v = read_vtu(ada / "solutions" / f"solution_{n}.vtu")
-    # one Q1 patch (4 points) per active cell of the oracle's mesh
-    assert len(v["Points"]) == 4 * o.n_cells()
-    h_min = wl.mesh.size[0] / (wl.mesh.subdivisions[0] << wl.adaptivity["max_level"])
-    key = lambda x: tuple(np.rint(x[:, :2] / h_min).astype(np.int64).T)
-    where = {k: i for i, k in enumerate(zip(*key(o.node_points())))}
-    idx = np.array([where[k] for k in zip(*key(v["Points"]))])
+    idx = oracle_points(v, o, wl)
     assert rel_l2(v["n"], o.get_native(0, 1)[idx]) < 1e-9
     for f, name in ((1, "mg_n"), (2, "f_tot")):
         assert rel_l2(v[name], o.get_native(f, 0)[idx]) < 1e-9, name
     norms = logged_norms(out, n)
     assert norms["n"] == pytest.approx(np.linalg.norm(o.get_native(0, 1)), rel=1e-5)
+
+
+def oracle_points(v: dict, o, wl) -> np.ndarray:
+    """For the points of an adaptive run's Q1 output patches (one 4-point patch per active cell
+    of the oracle's mesh), the oracle DoF at the same position."""
+    assert len(v["Points"]) == 4 * o.n_cells()
+    h_min = wl.mesh.size[0] / (wl.mesh.subdivisions[0] << wl.adaptivity["max_level"])
+    key = lambda x: tuple(np.rint(x[:, :2] / h_min).astype(np.int64).T)
+    where = {k: i for i, k in enumerate(zip(*key(o.node_points())))}
+    return np.array([where[k] for k in zip(*key(v["Points"]))])
+
+
+def test_implicit_allen_cahn_application_on_an_adaptive_mesh_matches_oracle(gpu_lib, tmp_path):
+    """Newton blocks on an adaptive mesh through the drop-in (no preconditioner, remeshing every
+    2 increments), against the oracle started from the same initial condition."""
+    common = """
+subsection Rectangular mesh
+  set x size = 100.0
+  set y size = 100.0
+end
+set time step = 1.0
+subsection linear solver parameters: 0
+  set solver_ids = 1
+  set tolerance type = RMSEPerField
+  set tolerance value = 1e-13
+  set max iterations = 3000
+end
+subsection newton solver parameters: 0
+  set solver_ids = 1
+  set max iterations = 50
+  set tolerance value = 1e-12
+end
+subsection miscellaneous
+  set random seed = 7
+end
+set Model constant mobility = 1.0, DOUBLE
+set Model constant kappa = 2.0, DOUBLE
+set Model constant n_grains = 12, INT
+"""
+    n = 6
+    uni = tmp_path / "uniform"
+    uni.mkdir()
+    build_and_run("allen_cahn_implicit", "set global refinement = 4\nset number steps = 0\n" + common, uni)
+    wl = W.allen_cahn_implicit_2d(refine=4, dt=1.0)
+    wl.adaptivity = dict(min_level=3, max_level=6, period=2, criteria=[(0, 1, 0.01, 0.99, 0.0)])
+    wl.initial = {0: to_lattice(read_vtu(uni / "solutions" / "solution_0.vtu"), wl.mesh, "n")}
+    ada = tmp_path / "adaptive"
+    ada.mkdir()
+    out = build_and_run("allen_cahn_implicit", f"""
+set global refinement = 4
+set max refinement = 6
+set min refinement = 3
+set mesh adaptivity = true
+set remeshing period = 2
+subsection refinement criterion: 0
+  set type = value
+  set value lower bound = 0.01
+  set value upper bound = 0.99
+  set variables = n
+end
+set number steps = {n}
+subsection output
+  set number = 1
+end
+""" + common, ada)
+    assert "not applied" not in out
+    o = po.Oracle(wl, adaptivity=wl.adaptivity)
+    o.set_linear_params(0, tolerance_type=1, tolerance=1e-13, max_iterations=3000)
+    o.set_newton_params(0, max_iterations=50, tolerance=1e-12)
+    assert o.run(n, n) == 0
+    assert len(np.unique(o.cells()[:, 0])) > 1
+    v = read_vtu(ada / "solutions" / f"solution_{n}.vtu")
+    idx = oracle_points(v, o, wl)
+    assert rel_l2(v["n"], o.get_native(0, 1)[idx]) < 1e-8
+    assert rel_l2(v["f_tot"], o.get_native(2, 0)[idx]) < 1e-8
 
