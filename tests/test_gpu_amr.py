@@ -165,3 +165,57 @@ def test_linear_elasticity_on_an_adaptive_mesh_matches_the_oracle():
     assert len(np.unique(p.cells()[:, 0])) > 1
     assert (p.hanging()[0] > 0).any()
     assert _rel_l2(p.download(0, 0, NATIVE), o.get_native(0, 0)) < 1e-8
+
+
+def test_dirichlet_function_values_on_every_mesh():
+    """ppf_set_dirichlet_function: the engine evaluates the callback at the Dirichlet nodes of
+    every mesh it builds. A callback returning the per-face constants reproduces the constant
+    run; a position-dependent one leaves its values on the Dirichlet nodes after
+    remeshing increments."""
+    import ctypes as C
+
+    def make():
+        wl = _ac(2)
+        wl.fields[0].dirichlet = {(0, 0): 1.0, (0, 3): 0.25}
+        return wl
+
+    ref = make().make_problem()
+    ref.solve(6)
+    consts = {0: 1.0, 3: 0.25}
+    calls = []
+
+    @capi.DIRICHLET_FN
+    def const_fn(user, field, comp, bid, x, t):
+        calls.append(bid)
+        return consts[bid]
+
+    p = make().make_problem()
+    assert p.lib.ppf_set_dirichlet_function(p.h, 0, const_fn, None) == capi.PPF_OK
+    p.solve(6)
+    assert calls and set(calls) <= {0, 3}
+    assert np.array_equal(p.cells(), ref.cells())
+    # the same run up to the summation order of the scatter's atomics
+    assert np.abs(p.download(0, 1, NATIVE) - ref.download(0, 1, NATIVE)).max() < 1e-13
+
+    @capi.DIRICHLET_FN
+    def ramp(user, field, comp, bid, x, t):
+        return 0.5 + 0.004 * x[1] if bid == 0 else 0.1 + 0.002 * x[0]
+
+    q = make().make_problem()
+    assert q.lib.ppf_set_dirichlet_function(q.h, 0, ramp, None) == capi.PPF_OK
+    q.solve(6)
+    assert q.mesh_version > 0
+    x = q.node_points()
+    cmap = q.constraint_map(0)
+    cnt, _, _ = q.hanging()
+    u = q.download(0, 1, NATIVE)
+    L = 100.0
+    on0 = np.isclose(x[:, 0], 0.0) & (cmap < 0)
+    on3 = np.isclose(x[:, 1], L) & (cmap < 0) & ~np.isclose(x[:, 0], 0.0)
+    assert on0.sum() > 0 and on3.sum() > 0
+    assert np.abs(u[on0] - (0.5 + 0.004 * x[on0, 1])).max() < 1e-15
+    assert np.abs(u[on3] - (0.1 + 0.002 * x[on3, 0])).max() < 1e-15
+    # hanging boundary nodes interpolate the (linear) boundary values of their coarse face
+    hb = (cnt > 0) & np.isclose(x[:, 0], 0.0)
+    if hb.any():
+        assert np.abs(u[hb] - (0.5 + 0.004 * x[hb, 1])).max() < 1e-14
