@@ -308,6 +308,12 @@ int ppf_remesh_if_due(ppf_handle h);
 /* Counts mesh changes (0 before the first); callers that cache geometry compare it. */
 long long ppf_mesh_version(ppf_handle h);
 
+/* Wall-clock phases of the last remeshing pass in ms, 5 values: refinement criteria, flag
+ * smoothing, the new mesh (refine/coarsen, numbering, hanging lines, transfer plan), transfer of
+ * the stored vectors, set-up of the new mesh (device arrays, inverse mass, constraints). The
+ * reference's "Refine Grid" timer section (refinement_manager.cc:53). */
+int ppf_remesh_stats(ppf_handle h, double* phases_ms);
+
 /* Active cells in tree order, 4 ints each: level, x, y, z (integer coordinates at that level;
  * the cell spans lower + size * [x, x+1] / (subdivisions * 2^level) per axis). Uniform handles
  * report their lattice cells at the global refinement. */

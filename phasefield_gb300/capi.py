@@ -50,7 +50,7 @@ EXPORTED = [
     "ppf_create_custom", "ppf_set_dirichlet_values", "ppf_dealii_cell_nodes", "ppf_download_solution",
     # adaptive meshes
     "ppf_set_adaptivity", "ppf_adapt", "ppf_remesh_if_due", "ppf_mesh_version", "ppf_cells", "ppf_cell_dofs",
-    "ppf_node_points", "ppf_hanging", "ppf_set_dirichlet_function",
+    "ppf_node_points", "ppf_hanging", "ppf_set_dirichlet_function", "ppf_remesh_stats",
 ]
 
 
@@ -182,6 +182,7 @@ def load() -> C.CDLL:
     lib.ppf_hanging.argtypes = [H, P(C.c_int), P(C.c_int), dp]
     lib.ppf_hanging.restype = C.c_longlong
     lib.ppf_set_dirichlet_function.argtypes = [H, C.c_int, DIRICHLET_FN, C.c_void_p]
+    lib.ppf_remesh_stats.argtypes = [H, dp]
     _lib = lib
     return lib
 

@@ -3,6 +3,7 @@
 // the transfer plan when the mesh changes; the device does the per-step work (cell kernel on the
 // cell list, finalize with hanging-node distribution) and the per-remesh work (criteria on every
 // cell, transfer of every stored age, constraint distribution).
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -39,6 +40,10 @@ struct AmrState {
   signed char* d_flags = nullptr;
   std::vector<ppf_dirichlet_fn> dfn;  // per field
   std::vector<void*> duser;
+  // wall-clock phases of the last remeshing pass (ms): criteria, smoothing, new mesh
+  // (refine, numbering, hanging lines, transfer plan), transfer (device vectors), set-up of the
+  // new mesh (mesh arrays, invM, constraints, distribution)
+  double phase_ms[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -441,6 +446,14 @@ int amr_permute_io(ppf_handle h, int f, double* host, const double* dev_src, dou
 static int adapt(ppf_handle h) {
   AmrState& S = *h->amr;
   AmrMesh& m = S.mesh;
+  using clock = std::chrono::steady_clock;
+  auto t_last = clock::now();
+  auto lap = [&](int i) {
+    const auto t = clock::now();
+    S.phase_ms[i] = std::chrono::duration<double, std::milli>(t - t_last).count();
+    t_last = t;
+  };
+  for (double& v : S.phase_ms) v = 0.0;
   // criteria on every cell
   MarkArgs M;
   std::memset(&M, 0, sizeof(M));
@@ -472,7 +485,9 @@ static int adapt(ppf_handle h) {
   std::vector<signed char> flags(m.ncells());
   PPF_CUDA(h, cudaMemcpyAsync(flags.data(), S.d_flags, flags.size(), cudaMemcpyDeviceToHost, h->stream));
   PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  lap(0);
   amr_smooth(m, flags, S.max_level);
+  lap(1);
   bool change = false;
   for (signed char f : flags) change |= f != 0;
   if (!change) {
@@ -500,6 +515,7 @@ static int adapt(ppf_handle h) {
   std::vector<int> tptr, tidx;
   std::vector<double> tw;
   amr_transfer_plan(m, nm, tptr, tidx, tw);
+  lap(2);
   int* d_ptr = nullptr;
   int* d_idx = nullptr;
   double* d_w = nullptr;
@@ -537,6 +553,7 @@ static int adapt(ppf_handle h) {
   cudaFree(d_idx);
   cudaFree(d_w);
   if (rc) return rc;
+  lap(3);
   m = std::move(nm);
   if ((rc = upload_mesh(h))) return rc;
   if ((rc = build_invm(h))) return rc;
@@ -554,6 +571,7 @@ static int adapt(ppf_handle h) {
   h->scratch_len = 0;
   h->mesh_version++;
   PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  lap(4);
   return PPF_OK;
 }
 
@@ -699,6 +717,13 @@ int ppf_remesh_if_due(ppf_handle h) {
 }
 
 long long ppf_mesh_version(ppf_handle h) { return h ? h->mesh_version : -1; }
+
+int ppf_remesh_stats(ppf_handle h, double* phases_ms) {
+  if (!h || !phases_ms) return PPF_ERR_ARG;
+  if (!h->amr) return fail(h, PPF_ERR_ARG, "the mesh is not adaptive");
+  for (int i = 0; i < 5; ++i) phases_ms[i] = h->amr->phase_ms[i];
+  return PPF_OK;
+}
 
 int ppf_cells(ppf_handle h, int* out) {
   if (!h || !out) return PPF_ERR_ARG;

@@ -237,6 +237,12 @@ class Problem:
     def remesh_if_due(self):
         self._check(self.lib.ppf_remesh_if_due(self.h))
 
+    def remesh_stats(self) -> dict:
+        """Phases of the last remeshing pass in ms (ppf_remesh_stats)."""
+        v = np.zeros(5)
+        self._check(self.lib.ppf_remesh_stats(self.h, capi.dptr(v)))
+        return dict(zip(("criteria_ms", "smoothing_ms", "new_mesh_ms", "transfer_ms", "setup_ms"), v.tolist()))
+
     @property
     def mesh_version(self) -> int:
         return int(self.lib.ppf_mesh_version(self.h))
