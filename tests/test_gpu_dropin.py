@@ -324,11 +324,20 @@ end
 
 
 def oracle_points(v: dict, o, wl) -> np.ndarray:
-    """For the points of an adaptive run's Q1 output patches (one 4-point patch per active cell
-    of the oracle's mesh), the oracle DoF at the same position."""
-    assert len(v["Points"]) == 4 * o.n_cells()
-    h_min = wl.mesh.size[0] / (wl.mesh.subdivisions[0] << wl.adaptivity["max_level"])
-    key = lambda x: tuple(np.rint(x[:, :2] / h_min).astype(np.int64).T)
+    """For the points of an adaptive run's output patches (one patch of (degree+1)^dim points
+    per active cell of the oracle's mesh, on the Gauss-Lobatto nodes for degrees 1 and 2), the
+    oracle DoF at the same position."""
+    dim, k = wl.mesh.dim, wl.mesh.degree
+    assert len(v["Points"]) == (k + 1) ** dim * o.n_cells()
+    h_min = wl.mesh.size[0] / (wl.mesh.subdivisions[0] << wl.adaptivity["max_level"]) / k
+    ext = np.array([int(round(wl.mesh.size[d] / h_min)) for d in range(dim)])
+    per = np.array([bool(wl.mesh.periodic[d]) for d in range(dim)])
+
+    def key(x):  # node units; periodic images wrap onto their master, as the DoFs do
+        i = np.rint(x[:, :dim] / h_min).astype(np.int64)
+        i = np.where(per, i % ext, i)
+        return tuple(i.T)
+
     where = {k: i for i, k in enumerate(zip(*key(o.node_points())))}
     return np.array([where[k] for k in zip(*key(v["Points"]))])
 
@@ -396,4 +405,58 @@ end
     idx = oracle_points(v, o, wl)
     assert rel_l2(v["n"], o.get_native(0, 1)[idx]) < 1e-8
     assert rel_l2(v["f_tot"], o.get_native(2, 0)[idx]) < 1e-8
+
+
+def test_cahn_hilliard_application_on_a_3d_adaptive_mesh_matches_oracle(gpu_lib, tmp_path):
+    """The periodic 3-D Cahn-Hilliard application (Q2) with a gradient criterion: hanging nodes
+    on faces and edges, periodic images, and the 3-D output of an adaptive mesh."""
+    common = """
+subsection Rectangular mesh
+  set x size = 4.0
+  set y size = 4.0
+  set z size = 4.0
+  set x periodic = true
+  set y periodic = true
+  set z periodic = true
+end
+set time step = 2.0e-5
+set Model constant mobility = 1.0, DOUBLE
+set Model constant kappa = 1.5, DOUBLE
+set Model constant well_height = 4.0, DOUBLE
+set Model constant c0 = 0.5, DOUBLE
+set Model constant amplitude = 0.05, DOUBLE
+"""
+    n = 10
+    uni = tmp_path / "uniform"
+    uni.mkdir()
+    build_and_run("cahn_hilliard_explicit", "set global refinement = 2\nset number steps = 0\n" + common, uni)
+    wl = W.cahn_hilliard_3d(refine=2, degree=2, size=4.0, dt=2e-5)
+    wl.adaptivity = dict(min_level=1, max_level=3, period=5, criteria=[(0, 2, 0.0, 0.0, 0.18)])
+    wl.initial = {0: to_lattice(read_vtu(uni / "solutions" / "solution_0.vtu"), wl.mesh, "c")}
+    ada = tmp_path / "adaptive"
+    ada.mkdir()
+    out = build_and_run("cahn_hilliard_explicit", f"""
+set global refinement = 2
+set max refinement = 3
+set min refinement = 1
+set mesh adaptivity = true
+set remeshing period = 5
+subsection refinement criterion: 0
+  set type = gradient
+  set gradient magnitude lower bound = 0.18
+  set variables = c
+end
+set number steps = {n}
+subsection output
+  set number = 1
+end
+""" + common, ada)
+    assert "not applied" not in out
+    o = po.Oracle(wl, adaptivity=wl.adaptivity)
+    assert o.run(n, n) == 0
+    assert len(np.unique(o.cells()[:, 0])) > 1
+    v = read_vtu(ada / "solutions" / f"solution_{n}.vtu")
+    idx = oracle_points(v, o, wl)
+    for f, name, age in ((0, "c", 1), (1, "mu", 1), (2, "f_tot", 0)):
+        assert rel_l2(v[name], o.get_native(f, age)[idx]) < 1e-9, name
 
