@@ -164,6 +164,18 @@ uint64_t path_key(const AmrMesh& m, const AmrCell& c) {
   return key;
 }
 
+// fn(begin, end, chunk) over [0, n) in contiguous chunks on host threads (one chunk for small n)
+template <class Fn>
+int parallel_chunks(long long n, Fn fn) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int nchunk = (int)std::min<long long>(hw, std::max<long long>(1, n / 2048));
+  std::vector<std::thread> pool;
+  for (int k = 1; k < nchunk; ++k) pool.emplace_back(fn, n * k / nchunk, n * (k + 1) / nchunk, k);
+  fn(0, n / nchunk, 0);
+  for (auto& t : pool) t.join();
+  return nchunk;
+}
+
 // level-`lev` cells whose closure holds position p (up to 2 per axis), active ones only; the
 // smallest active index, or -1
 int first_containing(const AmrMesh& m, int lev, const std::array<long long, 3>& p) {
@@ -273,9 +285,10 @@ void amr_set_cells(AmrMesh& m, std::vector<AmrCell> cells) {
     const long long coarse = q[0] + (long long)m.sub[0] * (q[1] + (long long)m.sub[1] * q[2]);
     items.push_back({coarse, path_key(m, c), c});
   }
-  std::sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
-    return a.coarse != b.coarse ? a.coarse < b.coarse : a.path < b.path;
-  });
+  // refining in place keeps tree order (children replace their parent in child order, a
+  // coarsened family's parent takes its first child's place): sort only when that fails
+  auto before = [](const Item& a, const Item& b) { return a.coarse != b.coarse ? a.coarse < b.coarse : a.path < b.path; };
+  if (!std::is_sorted(items.begin(), items.end(), before)) std::sort(items.begin(), items.end(), before);
   m.cells.resize(items.size());
   m.index.reset(items.size());
   for (size_t i = 0; i < items.size(); ++i) {
@@ -356,22 +369,24 @@ void amr_build(AmrMesh& m) {
   // hanging lines before closure: each DoF against the active cells one level coarser than its
   // coarsest incident cell (2:1 balance leaves no other candidates); the first in cell order
   std::vector<std::vector<std::pair<int, double>>> raw(m.N);
-  for (long long p = 0; p < m.N; ++p) {
-    const int lev = minlev[p] - 1;
-    if (lev < 0) continue;
-    const int best = first_containing(m, lev, m.pos[p]);
-    if (best < 0) continue;
-    const AmrCell& C = m.cells[best];
-    long long off[3] = {0, 0, 0};
-    if (!local_offset(m, C.lev, C.x, m.pos[p], off)) continue;
-    const double W = (double)((long long)k << (m.maxlev - lev));
-    for (int l = 0; l < nq; ++l) {
-      const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
-      double wl = 1.0;
-      for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(k, idx[d], (double)off[d] / W);
-      if (wl != 0.0) raw[p].push_back({m.cell_dofs[(size_t)best * nq + l], wl});
+  parallel_chunks(m.N, [&](long long p0, long long p1, int) {
+    for (long long p = p0; p < p1; ++p) {
+      const int lev = minlev[p] - 1;
+      if (lev < 0) continue;
+      const int best = first_containing(m, lev, m.pos[p]);
+      if (best < 0) continue;
+      const AmrCell& C = m.cells[best];
+      long long off[3] = {0, 0, 0};
+      if (!local_offset(m, C.lev, C.x, m.pos[p], off)) continue;
+      const double W = (double)((long long)k << (m.maxlev - lev));
+      for (int l = 0; l < nq; ++l) {
+        const int idx[3] = {l % n, (l / n) % n, l / (n * n)};
+        double wl = 1.0;
+        for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(k, idx[d], (double)off[d] / W);
+        if (wl != 0.0) raw[p].push_back({m.cell_dofs[(size_t)best * nq + l], wl});
+      }
     }
-  }
+  });
   // closure over hanging masters (AffineConstraints::close)
   std::vector<std::vector<std::pair<int, double>>> closed(m.N);
   std::vector<char> done(m.N, 0);
@@ -549,40 +564,57 @@ std::vector<AmrCell> amr_refine(const AmrMesh& m, const std::vector<signed char>
 
 void amr_transfer_plan(const AmrMesh& old, const AmrMesh& m, std::vector<int>& ptr, std::vector<int>& idx,
                        std::vector<double>& w) {
-  ptr.assign(1, 0);
-  idx.clear();
-  w.clear();
   const int nq = m.nq, n = m.n;
-  for (long long p = 0; p < m.N; ++p) {
-    const int same = old.node_of.find(old.pos_key(m.pos[p]));
-    if (same >= 0) {
-      idx.push_back(same);
-      w.push_back(1.0);
-      ptr.push_back((int)idx.size());
-      continue;
-    }
-    // first old cell (in old order) whose closure holds the new node
-    int best = -1;
-    for (int lev = 0; lev <= old.maxlev; ++lev) {
-      const int i = first_containing(old, lev, m.pos[p]);
-      if (i >= 0 && (best < 0 || i < best)) best = i;
-    }
-    if (best >= 0) {
-      const AmrCell& C = old.cells[best];
-      long long off[3] = {0, 0, 0};
-      local_offset(old, C.lev, C.x, m.pos[p], off);
-      const double W = (double)((long long)old.k << (old.maxlev - C.lev));
-      for (int l = 0; l < nq; ++l) {
-        const int id[3] = {l % n, (l / n) % n, l / (n * n)};
-        double wl = 1.0;
-        for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(m.k, id[d], (double)off[d] / W);
-        if (wl != 0.0) {
-          idx.push_back(old.cell_dofs[(size_t)best * nq + l]);
-          w.push_back(wl);
+  // rows built per chunk of new DoFs on host threads, then joined in DoF order
+  struct Part {
+    std::vector<int> cnt, idx;
+    std::vector<double> w;
+  };
+  std::vector<Part> parts(16);
+  const int nchunk = parallel_chunks(m.N, [&](long long p0, long long p1, int k) {
+    Part& P = parts[k];
+    for (long long p = p0; p < p1; ++p) {
+      const size_t e0 = P.idx.size();
+      const int same = old.node_of.find(old.pos_key(m.pos[p]));
+      if (same >= 0) {
+        P.idx.push_back(same);
+        P.w.push_back(1.0);
+        P.cnt.push_back(1);
+        continue;
+      }
+      // first old cell (in old order) whose closure holds the new node
+      int best = -1;
+      for (int lev = 0; lev <= old.maxlev; ++lev) {
+        const int i = first_containing(old, lev, m.pos[p]);
+        if (i >= 0 && (best < 0 || i < best)) best = i;
+      }
+      if (best >= 0) {
+        const AmrCell& C = old.cells[best];
+        long long off[3] = {0, 0, 0};
+        local_offset(old, C.lev, C.x, m.pos[p], off);
+        const double W = (double)((long long)old.k << (old.maxlev - C.lev));
+        for (int l = 0; l < nq; ++l) {
+          const int id[3] = {l % n, (l / n) % n, l / (n * n)};
+          double wl = 1.0;
+          for (int d = 0; d < m.dim; ++d) wl *= lagrange_exact(m.k, id[d], (double)off[d] / W);
+          if (wl != 0.0) {
+            P.idx.push_back(old.cell_dofs[(size_t)best * nq + l]);
+            P.w.push_back(wl);
+          }
         }
       }
+      P.cnt.push_back((int)(P.idx.size() - e0));
     }
-    ptr.push_back((int)idx.size());
+  });
+  ptr.assign(1, 0);
+  ptr.reserve(m.N + 1);
+  idx.clear();
+  w.clear();
+  for (int k = 0; k < nchunk; ++k) {
+    const Part& P = parts[k];
+    for (int c : P.cnt) ptr.push_back(ptr.back() + c);
+    idx.insert(idx.end(), P.idx.begin(), P.idx.end());
+    w.insert(w.end(), P.w.begin(), P.w.end());
   }
 }
 
