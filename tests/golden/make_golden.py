@@ -5,7 +5,8 @@
 The reference's own tests hold no vectors for the operator-evaluation path, so these are
 seeded oracle dumps at small instances of the benchmark configurations: deal.II DoF maps,
 constraint maps, the lumped inverse mass, one operator apply, fields after N explicit steps,
-the operator diagonal and a preconditioned CG solution with its iteration count. The CPU tests
+the operator diagonal and a preconditioned CG solution with its iteration count; and an
+adaptive mesh's cells, DoF table, hanging-node lines and fields after remeshing increments. The CPU tests
 check that the oracle still reproduces them; the GPU tests check the CUDA path against them.
 """
 from __future__ import annotations
@@ -47,6 +48,10 @@ def wl_coupled():
 
 def wl_elasticity():
     return W.eshelby_3d(refine=1, degree=2, size=8.0, n_incl=3, seed=14)
+
+
+def wl_allen_cahn_amr():
+    return W.allen_cahn_amr_2d(refine=3, degree=2, min_level=2, max_level=5, period=5, seed=16, n_grains=6)
 
 
 ELASTICITY_SOLVER = dict(tolerance_type=0, tolerance=1e-11, max_iterations=500, preconditioner=2, mg_depth=2,
@@ -97,7 +102,19 @@ def elasticity():
     return d
 
 
-FIXTURES = {"allen_cahn_2d_q2": allen_cahn, "cahn_hilliard_3d_q2": cahn_hilliard, "coupled_acch_2d_q2": coupled,
+def allen_cahn_amr():
+    """Adaptive mesh: the active cells, DoF table, hanging-node lines, lumped mass and fields
+    after 12 increments with the initial refinement and remeshing every 5 increments."""
+    wl = wl_allen_cahn_amr()
+    o = po.Oracle(wl, adaptivity=wl.adaptivity)
+    assert o.run(12, 12) == 0
+    cnt, mas, w = o.hanging()
+    return dict(n0=wl.initial[0], cells=o.cells().astype(np.int64), cell_dofs=o.cell_dofs(0),
+                hang_count=cnt.astype(np.int64), hang_master=mas, hang_weight=w, invm=o.invm_native(0),
+                n_12=o.get_native(0, 1), mg_n_12=o.get_native(1, 0), f_tot_12=o.get_native(2, 0))
+
+
+FIXTURES = {"allen_cahn_2d_q2": allen_cahn, "allen_cahn_amr_2d_q2": allen_cahn_amr, "cahn_hilliard_3d_q2": cahn_hilliard, "coupled_acch_2d_q2": coupled,
             "elasticity_3d_q2": elasticity}
 
 

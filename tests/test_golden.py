@@ -12,7 +12,8 @@ sys.path.insert(0, str(GOLDEN))
 
 import make_golden as G  # noqa: E402
 
-INDEX_KEYS = {"dof_map", "vector_dof_map", "cmap", "iterations"}
+INDEX_KEYS = {"dof_map", "vector_dof_map", "cmap", "iterations", "cells", "cell_dofs", "hang_count", "hang_master",
+              "hang_weight"}
 
 
 @pytest.mark.parametrize("name", sorted(G.FIXTURES))

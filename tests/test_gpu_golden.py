@@ -78,3 +78,21 @@ def test_elasticity_golden(gpu_lib):
     assert res < 1e-11
     assert abs(its - int(g["iterations"])) <= max(2, 0.1 * int(g["iterations"]))
     assert rel_l2(p.download(0), g["u"]) < 1e-8
+
+
+def test_allen_cahn_adaptive_golden(gpu_lib):
+    g = load("allen_cahn_amr_2d_q2")
+    wl = G.wl_allen_cahn_amr()
+    assert np.array_equal(wl.initial[0], g["n0"])
+    p = wl.make_problem()
+    p.solve(12, output_every=12)
+    assert np.array_equal(p.cells().astype(np.int64), g["cells"])
+    assert np.array_equal(p.cell_dofs().astype(np.int64), g["cell_dofs"])
+    cnt, mas, w = p.hanging()
+    assert np.array_equal(cnt, g["hang_count"]) and np.array_equal(mas, g["hang_master"])
+    assert np.array_equal(w, g["hang_weight"])
+    assert rel_l2(p.invm(), g["invm"]) < 1e-14
+    assert rel_l2(p.download(0, 1, 2), g["n_12"]) < 1e-9
+    assert rel_l2(p.download(1, 0, 2), g["mg_n_12"]) < 1e-9
+    assert rel_l2(p.download(2, 0, 2), g["f_tot_12"]) < 1e-9
+
