@@ -2010,9 +2010,14 @@ static void rebuild_mesh(Problem& P) {
 
 // one remesh pass (RefinementManager::do_adaptive_refinement): mark, smooth, refine/coarsen,
 // renumber, transfer every stored age, distribute the new constraints
-static void remesh(Problem& P) {
+static void remesh_with_flags(Problem& P, std::vector<int> flag);
+
+static void remesh(Problem& P) { remesh_with_flags(P, mark_cells(P)); }
+
+// the pass from given marks (1 refine, -1 coarsen, 0 keep) on: smoothing, refine/coarsen,
+// renumbering, transfer
+static void remesh_with_flags(Problem& P, std::vector<int> flag) {
   Mesh& m = P.m;
-  std::vector<int> flag = mark_cells(P);
   smooth_flags(P, flag);
   std::vector<CellKey> nxt;
   std::map<CellKey, int> parents_done;
@@ -2327,6 +2332,15 @@ int orc_adapt(void* h) {
   auto* P = (Problem*)h;
   if (!P->m.adaptive) return -1;
   remesh(*P);
+  return 0;
+}
+
+// one remesh pass from given per-cell marks (tree order; 1 refine, -1 coarsen, 0 keep) in
+// place of the refinement criteria
+int orc_adapt_with_flags(void* h, const int* flags) {
+  auto* P = (Problem*)h;
+  if (!P->m.adaptive) return -1;
+  remesh_with_flags(*P, std::vector<int>(flags, flags + P->m.ncells));
   return 0;
 }
 

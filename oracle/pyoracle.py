@@ -82,6 +82,7 @@ def load() -> C.CDLL:
         lib.orc_set_adaptivity.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int),
                                            dp, dp, dp]
         lib.orc_adapt.argtypes = [C.c_void_p]
+        lib.orc_adapt_with_flags.argtypes = [C.c_void_p, P(C.c_int)]
         lib.orc_remesh_if_due.argtypes = [C.c_void_p]
         lib.orc_n_nodes.argtypes = [C.c_void_p]
         lib.orc_n_nodes.restype = C.c_long
@@ -288,6 +289,12 @@ class Oracle:
     def adapt(self):
         """One remesh pass (mark, smooth, refine/coarsen, transfer)."""
         if self.lib.orc_adapt(self.h) != 0:
+            raise RuntimeError("oracle: mesh is not adaptive")
+
+    def adapt_with_flags(self, flags):
+        """One remesh pass from given marks per cell (1 refine, -1 coarsen, 0 keep)."""
+        f = np.ascontiguousarray(np.asarray(flags, dtype=np.int32))
+        if self.lib.orc_adapt_with_flags(self.h, f.ctypes.data_as(C.POINTER(C.c_int))) != 0:
             raise RuntimeError("oracle: mesh is not adaptive")
 
     def remesh_if_due(self):
