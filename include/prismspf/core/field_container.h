@@ -49,7 +49,9 @@ struct CellTables {
   number D2h[dim][n][n];  // (D D)[q][j] / h_d^2
   number Dt[n][n];        // Dt[i][j] = D[j][i] (integration uses the transposed derivative)
   number jxw[nq];         // JxW per quadrature point
-  number jxw_ih[dim][nq]; // JxW/h_d per quadrature point
+  // jdt[d][q][j] = D[j][q_d] JxW(q_j) / h_d: the weight, in node q's integral, of the gradient
+  // component d submitted (unscaled) at the j-th point q_j of q's line along d
+  number jdt[dim][nq][n];
   number lo[3], h[3], gl_x[n];
   number vol;
   signed char slot_of[MAX_FIELDS][NAGE];  // dependency slot of (field, age), -1 if undeclared
@@ -293,7 +295,8 @@ class FieldContainer {
   PPF_HD void set_gradient_term(unsigned int field_index, const dealii::Tensor<1, dim, ScalarValue>& g) {
     const int o = out_row(field_index);
     if (o < 0) return;
-    for (int d = 0; d < int(dim); ++d) ctx.outs[(o + 1 + d) * ctx.stride + slot()] = g[d].v * ctx.tab->jxw_ih[d][ctx.q];
+    // gradients are stored unscaled: the integration weights (jdt) carry JxW / h_d
+    for (int d = 0; d < int(dim); ++d) ctx.outs[(o + 1 + d) * ctx.stride + slot()] = g[d].v;
     ctx.submitted |= 2 << (2 * ctx.tab->out_of[field_index]);
   }
 
@@ -302,7 +305,7 @@ class FieldContainer {
     if (o < 0) return;
     for (int c = 0; c < int(dim); ++c)
       for (int d = 0; d < int(dim); ++d)
-        ctx.outs[(o + c * (1 + dim) + 1 + d) * ctx.stride + slot()] = g[c][d].v * ctx.tab->jxw_ih[d][ctx.q];
+        ctx.outs[(o + c * (1 + dim) + 1 + d) * ctx.stride + slot()] = g[c][d].v;
     ctx.submitted |= 2 << (2 * ctx.tab->out_of[field_index]);
   }
 

@@ -154,8 +154,9 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, 1)
           const bool has_g = flags & (2 << (2 * o));
           const int row0 = tab0->out_row0[o];
           for (int c = 0; c < od.ncomp; ++c) {
-            const number r = integrate_row<dim, degree, number>(tab0, outs, row0 + c * (1 + dim), has_v, has_g, t,
-                                                                lc, q, qa, qb, qc);
+            // the integration weights are the cell's level's
+            const number r = integrate_row<dim, degree, number>(ctx.tab, outs, row0 + c * (1 + dim), has_v, has_g,
+                                                                t, lc, q, qa, qb, qc);
             if (!(has_v || has_g)) continue;
             const long long base = c * P.N;
             const long long idx = dof + base;

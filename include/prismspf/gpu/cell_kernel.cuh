@@ -122,9 +122,9 @@ __device__ __forceinline__ number integrate_row(const pg::CellTables<dim, degree
       const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
       const int id = d == 0 ? qa : (d == 1 ? qb : qc);
       const number* g = outs + (rv + 1 + d) * S::threads + lc * nq + (q - id * sd);
-      const number* Dt = tab->Dt[id];
+      const number* w = tab->jdt[d][q];
 #pragma unroll
-      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j * sd], r);
+      for (int j = 0; j < n; ++j) r = fma(w[j], g[j * sd], r);
     }
   }
   return r;

@@ -39,13 +39,6 @@ struct EnsInstance {
   double m_well, kappa;
 };
 
-struct EnsTables {  // per degree, staged per tile
-  double Dh[2][3][3];
-  double Dt[3][3];
-  double jxw[9];
-  double jxw_ih[2][9];
-};
-
 struct EnsLaunch {
   const EnsInstance* inst;
   const int* tile_inst;         // instance of each tile
@@ -75,8 +68,13 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
     const double detJ = I.h[0] * I.h[1];
     const double w = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][b];
     tab->jxw[t] = w;
-    tab->jxw_ih[0][t] = w / I.h[0];
-    tab->jxw_ih[1][t] = w / I.h[1];
+    // integration weights of the unscaled gradients submitted along q's lines (jdt)
+    for (int j = 0; j < n; ++j) {
+      const double wx = detJ * P.gl_w[degree - 1][j] * P.gl_w[degree - 1][b];  // JxW at (j, b)
+      const double wy = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][j];  // JxW at (a, j)
+      tab->jdt[0][t][j] = P.gl_D[degree - 1][j][a] * (wx / I.h[0]);
+      tab->jdt[1][t][j] = P.gl_D[degree - 1][j][b] * (wy / I.h[1]);
+    }
   }
   if (t < n * n) {
     const int i = t / n, j = t % n;
@@ -138,15 +136,15 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
     double r = outs[lc * nq + q];
     {
       const double* g = outs + 1 * CPB * nq + lc * nq + (q - qa);
-      const double* Dt = tab->Dt[qa];
+      const double* w = tab->jdt[0][q];
 #pragma unroll
-      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j], r);
+      for (int j = 0; j < n; ++j) r = fma(w[j], g[j], r);
     }
     {
       const double* g = outs + 2 * CPB * nq + lc * nq + (q - qb * n);
-      const double* Dt = tab->Dt[qb];
+      const double* w = tab->jdt[1][q];
 #pragma unroll
-      for (int j = 0; j < n; ++j) r = fma(Dt[j], g[j * n], r);
+      for (int j = 0; j < n; ++j) r = fma(w[j], g[j * n], r);
     }
     atomicAdd(P.acc_out + I.off + node, r);
   }

@@ -12,7 +12,7 @@
 // the inverse lumped mass. The accumulator, the per-call cell tables and the error word live
 // in one file-scope __device__ array (g_noalloc_scratch) of fixed size, so the largest mesh
 // is NOALLOC_MAX_NODES lattice nodes; larger meshes are rejected with PPF_ERR_UNSUPPORTED.
-// Every GPU that loads this library holds that array (8 MiB + 16 KiB) until the process
+// Every GPU that loads this library holds that array (8 MiB + 32 KiB) until the process
 // exits.
 //
 // Sharing: all calls on a device share the one array and it keeps the last call's contents;
@@ -35,7 +35,7 @@ namespace ppf {
 namespace {
 
 constexpr long long NOALLOC_MAX_NODES = 1LL << 20;  // 1,048,576 lattice nodes (8 MiB of FP64)
-constexpr size_t NOALLOC_TABLE_BYTES = 16384;
+constexpr size_t NOALLOC_TABLE_BYTES = 32768;  // CellTables of any dim/degree (Q4 3-D: about 19 KB)
 constexpr size_t NOALLOC_ACC_BYTES = (size_t)NOALLOC_MAX_NODES * sizeof(double);
 constexpr size_t NOALLOC_BYTES = NOALLOC_ACC_BYTES + NOALLOC_TABLE_BYTES + 256;
 constexpr int NOALLOC_MAX_DEVICES = 64;
@@ -111,7 +111,13 @@ size_t fill_tables(const ppf_mesh_desc& m, const double* h, unsigned char* out) 
       r /= n;
     }
     t.jxw[q] = wq;
-    for (int d = 0; d < dim; ++d) t.jxw_ih[d][q] = wq / h[d];
+  }
+  for (int d = 0; d < dim; ++d) {
+    const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+    for (int q = 0; q < nq; ++q) {
+      const int id = (q / sd) % n;
+      for (int j = 0; j < n; ++j) t.jdt[d][q][j] = D[j][id] * (t.jxw[q + (j - id) * sd] / h[d]);
+    }
   }
   for (int d = 0; d < 3; ++d) {
     t.lo[d] = d < dim ? m.lower[d] : 0.0;

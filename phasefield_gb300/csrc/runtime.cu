@@ -148,7 +148,13 @@ static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
       r /= n;
     }
     t.jxw[q] = w;
-    for (int d = 0; d < dim; ++d) t.jxw_ih[d][q] = w / h[d];
+  }
+  for (int d = 0; d < dim; ++d) {
+    const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+    for (int q = 0; q < nq; ++q) {
+      const int id = (q / sd) % n;
+      for (int j = 0; j < n; ++j) t.jdt[d][q][j] = g.D[j][id] * (t.jxw[q + (j - id) * sd] / h[d]);
+    }
   }
   for (int d = 0; d < 3; ++d) {
     t.lo[d] = d < dim ? lo[d] : 0.0;
@@ -184,7 +190,7 @@ static std::vector<unsigned char> tables_impl_f32(const double* lo, const double
   cvt(&a.D2h[0][0][0], &t.D2h[0][0][0], sizeof(a.D2h) / sizeof(double));
   cvt(&a.Dt[0][0], &t.Dt[0][0], sizeof(a.Dt) / sizeof(double));
   cvt(a.jxw, t.jxw, sizeof(a.jxw) / sizeof(double));
-  cvt(&a.jxw_ih[0][0], &t.jxw_ih[0][0], sizeof(a.jxw_ih) / sizeof(double));
+  cvt(&a.jdt[0][0][0], &t.jdt[0][0][0], sizeof(a.jdt) / sizeof(double));
   cvt(a.lo, t.lo, 3);
   cvt(a.h, t.h, 3);
   cvt(a.gl_x, t.gl_x, sizeof(a.gl_x) / sizeof(double));
