@@ -52,6 +52,9 @@ struct EnsLaunch {
   double dt;
   double gl_w[2][3];   // GL weights per degree (index degree-1)
   double gl_D[2][3][3];
+  // reference-cell integration weights per degree: jbase[deg-1][d][q][j] = D[j][q_d] w_j w_e
+  // (e the other direction); times the instance's other cell size they are the cell's jdt
+  double jbase[2][2][9][3];
 };
 
 template <int degree, int CPB>
@@ -68,12 +71,11 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
     const double detJ = I.h[0] * I.h[1];
     const double w = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][b];
     tab->jxw[t] = w;
-    // integration weights of the unscaled gradients submitted along q's lines (jdt)
+    // integration weights of the unscaled gradients submitted along q's lines (jdt): in 2-D
+    // JxW(q_j) / h_0 = w_j w_b h_1, so the instance contributes one factor
     for (int j = 0; j < n; ++j) {
-      const double wx = detJ * P.gl_w[degree - 1][j] * P.gl_w[degree - 1][b];  // JxW at (j, b)
-      const double wy = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][j];  // JxW at (a, j)
-      tab->jdt[0][t][j] = P.gl_D[degree - 1][j][a] * (wx / I.h[0]);
-      tab->jdt[1][t][j] = P.gl_D[degree - 1][j][b] * (wy / I.h[1]);
+      tab->jdt[0][t][j] = P.jbase[degree - 1][0][t][j] * I.h[1];
+      tab->jdt[1][t][j] = P.jbase[degree - 1][1][t][j] * I.h[0];
     }
   }
   if (t < n * n) {
@@ -303,6 +305,15 @@ EnsLaunch make_launch(ppf_ensemble e, long long step) {
   L.dt = e->dt;
   std::memcpy(L.gl_w, e->gl_w, sizeof(L.gl_w));
   std::memcpy(L.gl_D, e->gl_D, sizeof(L.gl_D));
+  for (int deg = 1; deg <= 2; ++deg) {
+    const int n = deg + 1;
+    for (int q = 0; q < n * n; ++q)
+      for (int j = 0; j < n; ++j) {
+        const int a = q % n, b = q / n;
+        L.jbase[deg - 1][0][q][j] = e->gl_D[deg - 1][j][a] * e->gl_w[deg - 1][j] * e->gl_w[deg - 1][b];
+        L.jbase[deg - 1][1][q][j] = e->gl_D[deg - 1][j][b] * e->gl_w[deg - 1][a] * e->gl_w[deg - 1][j];
+      }
+  }
   return L;
 }
 
