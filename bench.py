@@ -439,6 +439,8 @@ def run_ours(args):
     cell_n, all_n = C.c_longlong(), C.c_longlong()
     lib.ppf_kernel_stats(p.h, C.byref(cell_ms), C.byref(cell_n), C.byref(all_n))
     lib.ppf_kernel_timing(p.h, 0)
+    # 0 FP64 contractions, 1 fixed-point derivatives + FP64 integration, 2 both fixed point
+    modes = {"c_block": p.contraction_mode(0, 0), "mu_block": p.contraction_mode(1, 0)}
     from phasefield_gb300 import replicas
     max_ms, dof_updates = replicas.aggregate(total_ms, 2 * N * args.steps, dist if ws > 1 else None, dev)
     value = dof_updates / (max_ms * 1e-3)
@@ -489,9 +491,12 @@ def run_ours(args):
                              "traffic_unit": "bytes/launch", "peak_source": peak_src,
                              "kernel": "cell_kernel<CahnHilliard<3,2>>", "bytes_per_launch": bytes_per_launch,
                              "avg_launch_ms": avg_launch_s * 1e3},
-                "roofline_fp64": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
-                                  "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
-                                  "flops_per_launch": flops_per_launch, "peak_source": "measured in this run"},
+                "fp64_equivalent": {"achieved": fp64_achieved, "peak": fp64_peak.value, "unit": "TFLOP/s",
+                                    "frac": fp64_achieved / fp64_peak.value if fp64_peak.value else None,
+                                    "flops_per_launch": flops_per_launch, "peak_source": "measured in this run",
+                                    "note": "FP64 flops of the same launch with FP64 contractions; the kernel "
+                                            "contracts exactly in 64-bit integers"},
+                "contraction_modes": modes,
                 "cpu_baseline": cpu, "gmg_cg": gmg, "ensemble": ens, "adjoint": adj, "amr": amr}
         print(json.dumps(line), flush=True)
     p.close()

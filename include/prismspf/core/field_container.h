@@ -16,6 +16,7 @@
 #include <prismspf/core/simulation_timer.h>
 #include <prismspf/core/type_enums.h>
 #include <prismspf/dealii_shim.h>
+#include <prismspf/gpu/fixed_point.cuh>
 
 #include <type_traits>
 
@@ -58,6 +59,16 @@ struct CellTables {
   signed char slot_comp0[MAX_SLOTS];      // first value row of a slot
   signed char out_of[MAX_FIELDS];         // output index of a block field, -1 if not in block
   signed char out_row0[MAX_OUTS];         // first output row (per comp: value, then dim grads)
+  // integer contractions (FP64 Q1/Q2, prismspf/gpu/fixed_point.cuh); fx = 1 when they apply
+  int fx;
+  int fx_cubic;                   // the integration scales c_d agree in every direction
+  unsigned int fx_rows;           // value rows with a fixed-point copy (those read as gradients)
+  signed char wo_sh[dim][nq];     // log2 of the product of w_int(q_e) over the directions e != d,
+                                  // w_int = 2w (Q1) or 6w (Q2)
+  unsigned long long dsig[3];     // 1/h_d = dsig / 2^63 * 2^dk
+  int dk[3];
+  unsigned long long isig[3];     // c_d = detJ / (h_d W^dim), W = 2 (Q1) or 6 (Q2): isig / 2^63 * 2^ik
+  int ik[3];
 };
 
 template <int dim, int degree, typename number = double>
@@ -73,6 +84,11 @@ struct CellCtx {
   int cell[3];         // global cell coordinates
   int* err;
   int submitted;       // bit 2*o: value of output o submitted, bit 2*o+1: gradient
+  // integer contractions: fixed-point nodal values [row][stride] and their per-cell block
+  // exponents [row][cells per block]; null when the kernel contracts in the arithmetic type
+  const long long* vals_fx = nullptr;
+  const int* ex_in = nullptr;
+  int cpb = 0;
 };
 
 }  // namespace gpu
@@ -349,7 +365,22 @@ class FieldContainer {
     int stride_d = 1;
     for (int e = 0; e < d; ++e) stride_d *= n;
     const int qd = (ctx.q / stride_d) % n;
-    const number* u = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
+    const int base = row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
+    if constexpr (std::is_same<number, double>::value && degree <= 2) {
+      if (ctx.vals_fx) {
+        // exact integer sum of the line's fixed-point values, rounded once (1/h_d folded in)
+        const int E = ctx.ex_in[row * ctx.cpb + ctx.lc];
+        if (E == gpu::fx::EXP_NONFINITE) return gpu::fx::quiet_nan();
+        if (E >= 0) {
+        const long long* u = ctx.vals_fx + base;
+        const long long s =
+            gpu::fx::line_derivative<n>(qd, u[0], u[stride_d], n > 2 ? u[2 * stride_d] : 0ll);
+        return gpu::fx::to_double(s, E - 1023 - gpu::fx::TOP_VALUES + ctx.tab->dk[d], ctx.tab->dsig[d]);
+        }
+        // a row declared without gradients has no fixed-point copy (exponent -1)
+      }
+    }
+    const number* u = ctx.vals + base;
     const number* Dr = ctx.tab->Dh[d][qd];
     number s = Dr[0] * u[0];
 #pragma unroll

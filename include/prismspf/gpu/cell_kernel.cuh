@@ -28,6 +28,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <prismspf/core/field_container.h>
 
 // prismspf/core/pde_operator_base.h re-declares the callback names as macros for user
@@ -92,6 +94,7 @@ struct CellLaunch {
   const SimulationTimer* timer_dev;  // when set (graph replays), the timer is read from here
   unsigned int block_id;
   int* err;
+  int fx_int;  // with integer contractions on: integrate in fixed point too (else FP64, jdt)
 };
 
 template <int dim, int degree>
@@ -102,11 +105,22 @@ struct CellShape {
   static constexpr int threads = cpb * nq;
 };
 
+// FP64 Q1/Q2 kernels contract in 64-bit fixed point (prismspf/gpu/fixed_point.cuh) when the
+// launch's tables enable it; their shared memory then also holds the fixed-point nodal values
+// and the per-cell block exponents of the value rows and of the output components.
+template <int dim, int degree, typename number>
+__host__ __device__ constexpr bool cell_fx_capable() {
+  return std::is_same<number, double>::value && degree <= 2;
+}
+
 template <int dim, int degree, typename number>
 __host__ __device__ inline size_t cell_smem_bytes(int nrows_in, int nrows_out) {
   using S = CellShape<dim, degree>;
   size_t tab = (sizeof(pg::CellTables<dim, degree, number>) + 15) / 16 * 16;
-  return tab + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
+  size_t b = tab + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
+  if (cell_fx_capable<dim, degree, number>())
+    b += sizeof(long long) * (size_t)nrows_in * S::threads + sizeof(int) * (size_t)(nrows_in + nrows_out) * S::cpb;
+  return b;
 }
 
 template <int dim, int degree, typename number>
@@ -130,6 +144,40 @@ __device__ __forceinline__ number integrate_row(const pg::CellTables<dim, degree
   return r;
 }
 
+// integrate_row with the submitted gradient terms already converted in place to fixed point
+// (block exponent E of the output component): per direction the exact integer line sum with
+// the weights iint, times the other directions' weights (a shift), rounded once with the
+// scale c_d = JxW / (h_d w_int...) of the integer weights.
+template <int dim, int degree>
+__device__ __forceinline__ double integrate_row_fx(const pg::CellTables<dim, degree, double>* tab, const double* outs,
+                                                   int rv, bool has_v, bool has_g, int t, int lc, int q, int qa, int qb,
+                                                   int qc, int E) {
+  using S = CellShape<dim, degree>;
+  constexpr int n = S::n, nq = S::nq;
+  namespace fx = pg::fx;
+  double r = has_v ? outs[rv * S::threads + t] : 0.0;
+  if (has_g) {
+    if (E == fx::EXP_NONFINITE) return fx::quiet_nan();
+    const long long* gx = reinterpret_cast<const long long*>(outs);
+    const int lsb = E - 1023 - fx::TOP_TERMS;
+    long long sum = 0;
+    double rg = 0.0;
+#pragma unroll
+    for (int d = 0; d < dim; ++d) {
+      const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+      const int id = d == 0 ? qa : (d == 1 ? qb : qc);
+      const long long* g = gx + (rv + 1 + d) * S::threads + lc * nq + (q - id * sd);
+      long long p = fx::line_integral<n>(id, g[0], g[sd], n > 2 ? g[2 * sd] : 0ll);
+      p = (long long)((unsigned long long)p << tab->wo_sh[d][q]);
+      if (tab->fx_cubic) sum += p;
+      else rg += fx::to_double(p, lsb + tab->ik[d], tab->isig[d]);
+    }
+    if (tab->fx_cubic) rg = fx::to_double(sum, lsb + tab->ik[0], tab->isig[0]);
+    r += rg;
+  }
+  return r;
+}
+
 template <class PDE, int dim, int degree, int MODE, typename number>
 __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks<PDE>::value)
     cell_kernel(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde) {
@@ -141,6 +189,25 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
   number* vals = reinterpret_cast<number*>(smem_raw + (sizeof(Tab) + 15) / 16 * 16);
   number* outs = vals + P.nrows_in * S::threads;
   __shared__ int sflags;
+  // integer contractions: enabled by the launch's tables, and only with the shared memory for them
+  constexpr bool FXC = cell_fx_capable<dim, degree, number>() && MODE != MODE_DIAG;
+  long long* vals_fx = reinterpret_cast<long long*>(outs + P.nrows_out * S::threads);
+  int* ex_in = reinterpret_cast<int*>(vals_fx + P.nrows_in * S::threads);
+  int* ex_out = ex_in + P.nrows_in * cpb;
+  bool fx_on = false, fx_int = false;
+  unsigned int tab_fx_rows = 0;
+  if constexpr (FXC) {
+    unsigned int dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const Tab* gtab = reinterpret_cast<const Tab*>(P.tables);
+    fx_on = gtab->fx != 0 && dyn >= (unsigned int)cell_smem_bytes<dim, degree, number>(P.nrows_in, P.nrows_out);
+    tab_fx_rows = gtab->fx_rows;
+    fx_int = fx_on && P.fx_int != 0;
+  }
+  // cell coordinates by multiply-high division (cell indices stay below 2^31: DoF indices are int)
+  pg::fx::FastDiv div0, div1;
+  div0.init((unsigned int)P.nc[0]);
+  div1.init((unsigned int)P.nc[1]);
 
   // stage the tables once per resident block
   {
@@ -164,10 +231,22 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
     int cx = 0, cy = 0, cz = 0;
     long long node = 0;
     if (active) {
-      cx = (int)(cell % P.nc[0]);
-      if (dim > 1) cy = (int)((cell / P.nc[0]) % P.nc[1]);
-      if (dim > 2) cz = (int)(cell / ((long long)P.nc[0] * P.nc[1]));
+      const unsigned int cl = (unsigned int)cell;
+      const unsigned int q0 = div0.div(cl);
+      cx = (int)(cl - q0 * div0.d);
+      if (dim == 2) cy = (int)q0;
+      if (dim > 2) {
+        const unsigned int q1 = div1.div(q0);
+        cy = (int)(q0 - q1 * div1.d);
+        cz = (int)q1;
+      }
       node = ((long long)(k * cz + qc) * P.nn[1] + (k * cy + qb)) * P.nn[0] + (k * cx + qa);
+    }
+    if constexpr (FXC) {
+      // the value-row exponents were last read by the previous tile's callbacks; rows without a
+      // fixed-point copy keep -1
+      if (fx_on)
+        for (int i = t; i < P.nrows_in * cpb; i += S::threads) ex_in[i] = ((tab_fx_rows >> (i / cpb)) & 1u) ? 0 : -1;
     }
     __syncthreads();  // tables staged; previous tile finished with vals/outs/sflags
 
@@ -196,6 +275,9 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
                 }
               }
               vals[(row + c) * S::threads + t] = v;
+              if constexpr (FXC) {
+                if (fx_on && ((tab_fx_rows >> (row + c)) & 1u)) atomicMax(&ex_in[(row + c) * cpb + lc], pg::fx::exponent(v));
+              }
             }
           }
           row += sd.ncomp;
@@ -204,6 +286,17 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
     }
 
     if constexpr (MODE != MODE_DIAG) {
+      if constexpr (FXC) {
+        if (fx_on) {
+          __syncthreads();  // block exponents of the value rows complete
+          for (int r = 0; r < P.nrows_in; ++r) {
+            const int E = ex_in[r * cpb + lc];
+            if (E >= 0 && E != pg::fx::EXP_NONFINITE)
+              vals_fx[r * S::threads + t] = pg::fx::to_fixed(vals[r * S::threads + t], E, pg::fx::TOP_VALUES);
+          }
+          for (int i = t; i < P.nrows_out * cpb; i += S::threads) ex_out[i] = 0;
+        }
+      }
       if (t == 0) sflags = 0;
       for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = number(0);
       __syncthreads();
@@ -220,6 +313,13 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
       ctx.cell[2] = cz;
       ctx.err = P.err;
       ctx.submitted = 0;
+      if constexpr (FXC) {
+        if (fx_on) {
+          ctx.vals_fx = vals_fx;
+          ctx.ex_in = ex_in;
+          ctx.cpb = cpb;
+        }
+      }
       if (active) {
         FieldContainer<dim, degree, number> fc(ctx);
         const SimulationTimer timer = P.timer_dev ? *P.timer_dev : P.timer;
@@ -230,6 +330,36 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
       __syncthreads();
       const int flags = sflags;
 
+      if constexpr (FXC) {
+        if (fx_int) {
+          // submitted gradient terms -> fixed point in place, one block exponent per cell and
+          // output component (rows of component c of output o: value, then dim gradient rows)
+          for (int o = 0; o < P.nout; ++o)
+            if (flags & (2 << (2 * o)))
+              for (int c = 0; c < P.outs[o].ncomp; ++c) {
+                const int rv = tab->out_row0[o] + c * (1 + dim);
+                int e = 0;
+#pragma unroll
+                for (int d = 0; d < dim; ++d) e = max(e, pg::fx::exponent(outs[(rv + 1 + d) * S::threads + t]));
+                atomicMax(&ex_out[rv * cpb + lc], e);
+              }
+          __syncthreads();
+          for (int o = 0; o < P.nout; ++o)
+            if (flags & (2 << (2 * o)))
+              for (int c = 0; c < P.outs[o].ncomp; ++c) {
+                const int rv = tab->out_row0[o] + c * (1 + dim);
+                const int E = ex_out[rv * cpb + lc];
+#pragma unroll
+                for (int d = 0; d < dim; ++d) {
+                  double* gp = outs + (rv + 1 + d) * S::threads + t;
+                  const long long x = E == pg::fx::EXP_NONFINITE ? 0 : pg::fx::to_fixed(*gp, E, pg::fx::TOP_TERMS);
+                  *reinterpret_cast<long long*>(gp) = x;
+                }
+              }
+          __syncthreads();
+        }
+      }
+
       if (active) {
 #pragma unroll
         for (int o = 0; o < pg::MAX_OUTS; ++o) {
@@ -239,8 +369,18 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
             const bool has_g = flags & (2 << (2 * o));
             const int row0 = tab->out_row0[o];
             for (int c = 0; c < od.ncomp; ++c) {
-              const number r = integrate_row<dim, degree, number>(tab, outs, row0 + c * (1 + dim), has_v, has_g, t,
-                                                                  lc, q, qa, qb, qc);
+              number r;
+              if constexpr (FXC) {
+                const int rv = row0 + c * (1 + dim);
+                if (fx_int)
+                  r = integrate_row_fx<dim, degree>(tab, outs, rv, has_v, has_g, t, lc, q, qa, qb, qc,
+                                                    ex_out[rv * cpb + lc]);
+                else
+                  r = integrate_row<dim, degree, number>(tab, outs, rv, has_v, has_g, t, lc, q, qa, qb, qc);
+              } else {
+                r = integrate_row<dim, degree, number>(tab, outs, row0 + c * (1 + dim), has_v, has_g, t, lc, q, qa,
+                                                       qb, qc);
+              }
               if (has_v || has_g) {
                 const long long idx = node + c * P.N;
                 const int target = od.cmap ? od.cmap[idx] : (int)idx;

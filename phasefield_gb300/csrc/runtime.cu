@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <memory>
 #include <string>
 #include <vector>
@@ -118,11 +119,69 @@ GLRule gauss_lobatto(int n) {
 // ------------------------------------------------------------------------------------------
 // cell tables
 // ------------------------------------------------------------------------------------------
+
+// The integer contractions of the FP64 cell kernels (prismspf/gpu/fixed_point.cuh): for Q1 and
+// Q2 the unit-interval derivative matrix and the quadrature weights times W = 2 (Q1) or 6 (Q2)
+// are integers and the weights powers of two. Left off (fx = 0) for other degrees, or when
+// PPF_FP64_CONTRACTIONS=1 asks for the FP64 contractions.
+template <int dim, int degree>
+static void fixed_point_tables(pg::CellTables<dim, degree, double>& t, const GLRule& g, const double* h, double detJ,
+                               unsigned int fx_rows) {
+  constexpr int n = degree + 1, nq = pg::CellTables<dim, degree, double>::nq;
+  t.fx = 0;
+  t.fx_rows = fx_rows;
+  if (degree > 2) return;
+  const char* env = std::getenv("PPF_FP64_CONTRACTIONS");
+  if (env && env[0] == '1') return;
+  const double W = degree == 1 ? 2.0 : 6.0;
+  int wint[pg::MAX_N], wsh[pg::MAX_N];
+  for (int q = 0; q < n; ++q) {
+    wint[q] = (int)std::lround(g.w[q] * W);
+    if (std::fabs(g.w[q] * W - wint[q]) > 1e-12 || (wint[q] & (wint[q] - 1))) return;
+    wsh[q] = 0;
+    while ((1 << wsh[q]) < wint[q]) ++wsh[q];
+  }
+  // the kernels contract with the closed forms of fixed_point.cuh (line_derivative,
+  // line_integral): check that the rule's derivative matrix is theirs
+  static const int dq1[2][2] = {{-1, 1}, {-1, 1}};
+  static const int dq2[3][3] = {{-3, 4, -1}, {-1, 0, 1}, {1, -4, 3}};
+  for (int q = 0; q < n; ++q)
+    for (int j = 0; j < n; ++j) {
+      const int want = degree == 1 ? dq1[q][j] : dq2[q][j];
+      if (std::fabs(g.D[q][j] - want) > 1e-12) return;
+    }
+  if (degree == 2 && (wint[0] != 1 || wint[1] != 4 || wint[2] != 1)) return;
+  if (degree == 1 && (wint[0] != 1 || wint[1] != 1)) return;
+  for (int d = 0; d < dim; ++d)
+    for (int q = 0; q < nq; ++q) {
+      int sh = 0, r = q;
+      for (int e = 0; e < dim; ++e) {
+        if (e != d) sh += wsh[r % n];
+        r /= n;
+      }
+      t.wo_sh[d][q] = (signed char)sh;
+    }
+  double Wd = 1.0;
+  for (int d = 0; d < dim; ++d) Wd *= W;
+  for (int d = 0; d < 3; ++d) {
+    const double hd = d < dim ? h[d] : h[0];
+    const pg::fx::Scale ds = pg::fx::make_scale(1.0 / hd);
+    const pg::fx::Scale is = pg::fx::make_scale(detJ / hd / Wd);
+    t.dsig[d] = ds.sig;
+    t.dk[d] = ds.k;
+    t.isig[d] = is.sig;
+    t.ik[d] = is.k;
+  }
+  t.fx_cubic = 1;
+  for (int d = 1; d < dim; ++d)
+    if (t.isig[d] != t.isig[0] || t.ik[d] != t.ik[0]) t.fx_cubic = 0;
+  t.fx = 1;
+}
 template <int dim, int degree>
 static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
                                               const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                               const signed char* slot_comp0, const signed char* out_of,
-                                              const signed char* out_row0) {
+                                              const signed char* out_row0, unsigned int fx_rows) {
   using Tab = pg::CellTables<dim, degree>;
   constexpr int n = degree + 1, nq = Tab::nq;
   Tab t;
@@ -162,6 +221,7 @@ static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
   }
   for (int i = 0; i < n; ++i) t.gl_x[i] = g.x[i];
   t.vol = detJ;
+  fixed_point_tables<dim, degree>(t, g, h, detJ, fx_rows);
   std::memcpy(t.slot_of, slot_of, sizeof(t.slot_of));
   std::memcpy(t.slot_comp0, slot_comp0, sizeof(t.slot_comp0));
   std::memcpy(t.out_of, out_of, sizeof(t.out_of));
@@ -176,10 +236,10 @@ template <int dim, int degree>
 static std::vector<unsigned char> tables_impl_f32(const double* lo, const double* h,
                                                   const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                                   const signed char* slot_comp0, const signed char* out_of,
-                                                  const signed char* out_row0) {
+                                                  const signed char* out_row0, unsigned int) {
   using T64 = pg::CellTables<dim, degree, double>;
   using T32 = pg::CellTables<dim, degree, float>;
-  auto b = tables_impl<dim, degree>(lo, h, slot_of, slot_comp0, out_of, out_row0);
+  auto b = tables_impl<dim, degree>(lo, h, slot_of, slot_comp0, out_of, out_row0, 0u);
   const T64& a = *reinterpret_cast<const T64*>(b.data());
   T32 t;
   std::memset(&t, 0, sizeof(t));
@@ -217,15 +277,27 @@ static std::vector<unsigned char> tables_impl_f32(const double* lo, const double
     default: break;                                            \
   }
 
+template <int dim, int degree>
+static bool tables_fx_impl(const unsigned char* tab) {
+  return reinterpret_cast<const pg::CellTables<dim, degree, double>*>(tab)->fx != 0;
+}
+// whether FP64 tables built by build_cell_tables turn the integer contractions on
+static bool tables_fx(const std::vector<unsigned char>& tab, int dim, int degree) {
+  if (tab.empty()) return false;
+  const unsigned char* t = tab.data();
+  PPF_DD_SWITCH(tables_fx_impl, t)
+  return false;
+}
+
 std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
-                                             const signed char* out_row0) {
+                                             const signed char* out_row0, unsigned int fx_rows) {
   if (precision == 1) {
-    PPF_DD_SWITCH(tables_impl_f32, lo, h, slot_of, slot_comp0, out_of, out_row0)
+    PPF_DD_SWITCH(tables_impl_f32, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows)
     return {};
   }
-  PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0)
+  PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows)
   return {};
 }
 
@@ -494,6 +566,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memset(out_of, -1, sizeof(out_of));
   std::memset(out_row0, 0, sizeof(out_row0));
   const int nf = (int)h->fields.size();
+  unsigned int fx_rows = 0;  // value rows read as gradients (fixed-point copies in the kernel)
   P.nslots = 0;
   P.nrows_in = 0;
   for (int f = 0; f < nf; ++f)
@@ -505,6 +578,8 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
       slot_comp0[P.nslots] = (signed char)P.nrows_in;
       P.slot_field[P.nslots] = f;
       P.slot_age[P.nslots] = a;
+      if (fl & PPF_DEP_GRADIENT)
+        for (int c = 0; c < h->fields[f].ncomp && P.nrows_in + c < 32; ++c) fx_rows |= 1u << (P.nrows_in + c);
       P.nrows_in += h->fields[f].ncomp;
       P.nslots++;
     }
@@ -518,12 +593,14 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   }
   if (P.nrows_in + P.nrows_out > 127) return fail(h, PPF_ERR_UNSUPPORTED, "block too large");
   double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
-  auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0);
+  auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0, fx_rows);
   if (tab.empty()) return fail(h, PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
   std::memcpy(P.slot_of, slot_of, sizeof(slot_of));
   std::memcpy(P.slot_comp0, slot_comp0, sizeof(slot_comp0));
   std::memcpy(P.out_of, out_of, sizeof(out_of));
   std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
+  P.fx = tables_fx(tab, h->dim, h->k);
+  P.fx_int = -1;
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
   P.valid = true;
@@ -539,6 +616,8 @@ double* state_ptr(ppf_handle h, int f, int age) {
 
 // Launches the cell kernel of block b (which: 0 rhs, 1 lhs) accumulating into each block
 // field's acc. `src` supplies the SRC dependency per block field (may be null).
+static int choose_fx_integration(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem);
+
 int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool plain_src) {
   BlockState& B = h->blocks[b];
   BlockPlan& P = B.plan[which];
@@ -588,7 +667,66 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   L.err = h->d_err;
   if (h->amr) return amr_launch_cell(h, b, which, L);
   const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
-  return timed_cell_launch(h, 0, which == 1 ? MODE_LHS : MODE_RHS, L, h->model_obj.data(), smem);
+  const int mode = which == 1 ? MODE_LHS : MODE_RHS;
+  if (P.fx) {
+    if (P.fx_int < 0) {
+      // timing both integrations pays off for plans launched every increment or iteration; the
+      // right-hand side of a linear or Newton block (once per solve) integrates in FP64
+      if (which == 0 && B.desc.solve_type != PPF_EXPLICIT) {
+        P.fx_int = 0;
+      } else {
+        const int rc = choose_fx_integration(h, P, mode, L, smem);
+        if (rc) return rc;
+      }
+    }
+    L.fx_int = P.fx_int;
+  }
+  return timed_cell_launch(h, 0, mode, L, h->model_obj.data(), smem);
+}
+
+// The integer-contraction kernels (FP64 Q1/Q2) take their derivatives in fixed point; their
+// integration can run in fixed point too (issue slots) or in FP64 (the FP64 pipe). Which is
+// cheaper depends on how much FP64 work the callback itself does, so the first plain launch of
+// a plan times both, twice each, back to back into the block's accumulators (which every
+// caller has just zeroed, and which are zeroed again afterwards), and keeps the faster.
+// PPF_FX_INTEGRATION=0 or 1 fixes the choice; a plan first launched inside a graph capture
+// integrates in FP64.
+static int choose_fx_integration(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem) {
+  const char* env = std::getenv("PPF_FX_INTEGRATION");
+  if (env && (env[0] == '0' || env[0] == '1')) {
+    P.fx_int = env[0] - '0';
+    return PPF_OK;
+  }
+  if (h->capturing) {
+    P.fx_int = 0;
+    return PPF_OK;
+  }
+  cudaEvent_t ev[5] = {};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
+  CellLaunch T = L;
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
+  for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+    T.fx_int = r & 1;
+    e = h->custom_launch ? (cudaError_t)h->custom_launch(h->dim, h->k, mode, 0, &T, h->model_obj.data(), smem,
+                                                         (void*)h->stream)
+                         : h->model->launch(h->dim, h->k, mode, 0, T, h->model_obj.data(), smem, h->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[r + 1], h->stream);
+  }
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+  float best[2] = {1e30f, 1e30f};
+  for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ev[r], ev[r + 1]);
+    if (e == cudaSuccess && ms < best[r & 1]) best[r & 1] = ms;
+  }
+  for (int i = 0; i < L.nout && e == cudaSuccess; ++i)
+    e = cudaMemsetAsync(L.outs[i].acc, 0, sizeof(double) * (size_t)L.outs[i].ncomp * (size_t)L.N, h->stream);
+  for (int i = 0; i < 5; ++i)
+    if (ev[i]) cudaEventDestroy(ev[i]);
+  if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("integration timing: ") + cudaGetErrorString(e));
+  P.fx_int = best[1] < best[0] ? 1 : 0;
+  return PPF_OK;
 }
 
 int timed_cell_launch(ppf_handle h, int precision, int mode, const CellLaunch& L, const void* obj, size_t smem) {
@@ -1279,6 +1417,14 @@ int ppf_set_stream(ppf_handle h, void* stream) {
   if (!h) return PPF_ERR_ARG;
   PPF_CUDA(h, cudaStreamSynchronize(h->stream));
   h->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : h->own_stream;
+  return PPF_OK;
+}
+
+int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode) {
+  if (!h || !mode || b < 0 || b >= (int)h->blocks.size() || which < 0 || which > 1) return PPF_ERR_ARG;
+  const BlockPlan& P = h->blocks[b].plan[which];
+  if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
+  *mode = !P.fx || h->amr ? 0 : (P.fx_int < 0 ? -1 : 1 + P.fx_int);
   return PPF_OK;
 }
 
