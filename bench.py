@@ -39,8 +39,8 @@ METRIC = "DoF-updates/s (explicit Cahn-Hilliard Q2 3-D step, FP64)"
 UNIT = "DoF-updates/s"
 WORKLOAD = dict(refine=6, degree=2, size=64.0, dt=1e-4)
 # dram__bytes_read.sum + dram__bytes_write.sum of the cell kernel from one ncu capture of
-# this workload, mean of the c-block (59.94 MB) and mu-block (42.73 MB) launches
-TRAFFIC_PER_LAUNCH = 51.34e6
+# this workload, mean of the c-block (60.39 + 0.75 MB) and mu-block (43.07 + 0.04 MB) launches
+TRAFFIC_PER_LAUNCH = 52.13e6
 
 
 def workload_config(extra=None):
