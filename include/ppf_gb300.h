@@ -410,11 +410,11 @@ int ppf_kernel_stats_reset(ppf_handle h);
 
 /* Contraction arithmetic of block b's operator (which: 0 rhs, 1 lhs) on a uniform mesh:
  * *mode = 0 FP64 contractions (degrees 3-4, or PPF_FP64_CONTRACTIONS=1), 1 exact fixed-point
- * derivatives with FP64 integration, 2 fixed-point derivatives and integration, -1 not chosen
- * yet (the first plain launch of an explicit right-hand side or of a left-hand side times 1 and
- * 2 and keeps the faster; a linear or Newton right-hand side takes 1; PPF_FX_INTEGRATION=0/1
- * fixes it). Engine-side only: the reference contracts in FP64 (fe_evaluation sum
- * factorisation). */
+ * derivatives with FP64 integration, 2 fixed-point derivatives and integration, 3 FP64
+ * derivatives with fixed-point integration, -1 not chosen yet (the first plain launch of an
+ * explicit right-hand side or of a left-hand side times 1, 2 and 3 and keeps the fastest; a
+ * linear or Newton right-hand side takes 1; PPF_CONTRACTION_MODE=1/2/3 fixes the mode).
+ * Engine-side only: the reference contracts in FP64 (fe_evaluation sum factorisation). */
 int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode);
 
 /* Measures the current GPU's FP64 FMA throughput (TFLOP/s, FMA = 2 flops) with a

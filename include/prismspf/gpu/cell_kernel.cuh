@@ -94,7 +94,10 @@ struct CellLaunch {
   const SimulationTimer* timer_dev;  // when set (graph replays), the timer is read from here
   unsigned int block_id;
   int* err;
-  int fx_int;  // with integer contractions on: integrate in fixed point too (else FP64, jdt)
+  // with integer contractions on in the tables: fx_deriv takes the derivatives in fixed point
+  // (else FP64 from the nodal values), fx_int integrates in fixed point (else FP64 with jdt)
+  int fx_deriv;
+  int fx_int;
 };
 
 template <int dim, int degree>
@@ -194,15 +197,17 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
   long long* vals_fx = reinterpret_cast<long long*>(outs + P.nrows_out * S::threads);
   int* ex_in = reinterpret_cast<int*>(vals_fx + P.nrows_in * S::threads);
   int* ex_out = ex_in + P.nrows_in * cpb;
-  bool fx_on = false, fx_int = false;
+  bool fx_on = false, fx_int = false;  // fx_on: fixed-point derivatives
   unsigned int tab_fx_rows = 0;
   if constexpr (FXC) {
     unsigned int dyn;
     asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
     const Tab* gtab = reinterpret_cast<const Tab*>(P.tables);
-    fx_on = gtab->fx != 0 && dyn >= (unsigned int)cell_smem_bytes<dim, degree, number>(P.nrows_in, P.nrows_out);
+    const bool fx_ok =
+        gtab->fx != 0 && dyn >= (unsigned int)cell_smem_bytes<dim, degree, number>(P.nrows_in, P.nrows_out);
     tab_fx_rows = gtab->fx_rows;
-    fx_int = fx_on && P.fx_int != 0;
+    fx_on = fx_ok && P.fx_deriv != 0;
+    fx_int = fx_ok && P.fx_int != 0;
   }
   // cell coordinates by multiply-high division (cell indices stay below 2^31: DoF indices are int)
   pg::fx::FastDiv div0, div1;
@@ -294,8 +299,9 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
             if (E >= 0 && E != pg::fx::EXP_NONFINITE)
               vals_fx[r * S::threads + t] = pg::fx::to_fixed(vals[r * S::threads + t], E, pg::fx::TOP_VALUES);
           }
-          for (int i = t; i < P.nrows_out * cpb; i += S::threads) ex_out[i] = 0;
         }
+        if (fx_int)
+          for (int i = t; i < P.nrows_out * cpb; i += S::threads) ex_out[i] = 0;
       }
       if (t == 0) sflags = 0;
       for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = number(0);

@@ -152,6 +152,7 @@ int linearised_launch(ppf_handle h, AdjointState& A, const char* model, const vo
   L.timer = h->timer;
   L.block_id = 0;
   L.err = h->d_err;
+  L.fx_deriv = 1;  // integer derivatives where the tables allow them (FP64 Q1/Q2)
   const size_t smem = cell_smem(h->dim, h->k, 0, L.nrows_in, L.nrows_out);
   cudaError_t e = ops->launch(h->dim, h->k, MODE_RHS, 0, L, obj, smem, h->stream);
   if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("linearised kernel: ") + cudaGetErrorString(e));

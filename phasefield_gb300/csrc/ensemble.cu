@@ -11,8 +11,10 @@
 //     accumulators rotate; a launch depends only on the previous launch having finished.
 //   * one persistent launch for every instance and both degrees: a global list of cell tiles
 //     (instance, first cell) is walked grid-stride; a tile of a Q1 instance runs the Q1 body,
-//     of a Q2 instance the Q2 body (block-uniform branch), with the instance's own mesh
-//     spacing and parameters (m_well, kappa) staged per tile.
+//     of a Q2 instance the Q2 body (block-uniform branch), with the instance's parameters
+//     (m_well, kappa) and its cell tables, built once on the host with the engine's table
+//     builder for the instance's mesh spacing, copied into shared memory per tile (an integer
+//     copy: GB300's FP64 pipe is too narrow to recompute them per tile).
 //   * tile shapes (cells per tile for Q1 and for Q2) and the grid size are chosen by a
 //     project-written autotuner that times candidate shapes on the ensemble itself.
 // Natural boundary conditions (the ensemble workload has no constraints).
@@ -34,7 +36,8 @@ struct EnsInstance {
   int nc[2];
   int nn[2];
   long long N;
-  long long off;  // offset of the instance's vectors in the packed arrays
+  long long off;      // offset of the instance's vectors in the packed arrays
+  long long tab_off;  // offset (bytes, 16-aligned) of its CellTables in the packed tables
   double h[2];
   double m_well, kappa;
 };
@@ -50,11 +53,8 @@ struct EnsLaunch {
   double* acc_zero;
   long long total_len;
   double dt;
-  double gl_w[2][3];   // GL weights per degree (index degree-1)
-  double gl_D[2][3][3];
-  // reference-cell integration weights per degree: jbase[deg-1][d][q][j] = D[j][q_d] w_j w_e
-  // (e the other direction); times the instance's other cell size they are the cell's jdt
-  double jbase[2][2][9][3];
+  const unsigned char* tables;  // per-instance CellTables<2, degree, double>
+  int fx;                       // integer derivatives (the tables enable them for Q1/Q2)
 };
 
 template <int degree, int CPB>
@@ -64,39 +64,15 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
   Tab* tab = reinterpret_cast<Tab*>(smem);
   double* vals = smem + (sizeof(Tab) + 7) / 8;
   double* outs = vals + CPB * nq;
+  long long* vals_fx = reinterpret_cast<long long*>(outs + 3 * CPB * nq);  // integer derivatives
+  int* ex_in = reinterpret_cast<int*>(vals_fx + CPB * nq);                 // per-cell block exponent
   const int t = threadIdx.x;
-  // stage the instance's tables (mesh spacing differs per instance)
-  if (t < nq) {
-    const int a = t % n, b = t / n;
-    const double detJ = I.h[0] * I.h[1];
-    const double w = detJ * P.gl_w[degree - 1][a] * P.gl_w[degree - 1][b];
-    tab->jxw[t] = w;
-    // integration weights of the unscaled gradients submitted along q's lines (jdt): in 2-D
-    // JxW(q_j) / h_0 = w_j w_b h_1, so the instance contributes one factor
-    for (int j = 0; j < n; ++j) {
-      tab->jdt[0][t][j] = P.jbase[degree - 1][0][t][j] * I.h[1];
-      tab->jdt[1][t][j] = P.jbase[degree - 1][1][t][j] * I.h[0];
-    }
-  }
-  if (t < n * n) {
-    const int i = t / n, j = t % n;
-    tab->Dh[0][i][j] = P.gl_D[degree - 1][i][j] / I.h[0];
-    tab->Dh[1][i][j] = P.gl_D[degree - 1][i][j] / I.h[1];
-    tab->Dt[i][j] = P.gl_D[degree - 1][j][i];
-  }
-  if (t < 8) {
-    reinterpret_cast<signed char*>(tab->out_of)[t] = (t == 0) ? 0 : -1;
-    for (int a = 0; a < pg::NAGE; ++a) tab->slot_of[t][a] = (t == 0 && a == 1) ? 0 : -1;
-  }
-  if (t == 0) {
-    tab->slot_comp0[0] = 0;
-    tab->out_row0[0] = 0;
-    tab->vol = I.h[0] * I.h[1];
-    for (int d = 0; d < 3; ++d) {
-      tab->lo[d] = 0.0;
-      tab->h[d] = d < 2 ? I.h[d] : 1.0;
-    }
-    for (int a = 0; a < n; ++a) tab->gl_x[a] = 0.0;
+  if (P.fx && t < CPB) ex_in[t] = 0;  // last read before the previous tile's closing barrier
+  // stage the instance's tables (built on the host for its mesh spacing)
+  {
+    const unsigned int* src = reinterpret_cast<const unsigned int*>(P.tables + I.tab_off);
+    unsigned int* dst = reinterpret_cast<unsigned int*>(tab);
+    for (int k = t; k < (int)(sizeof(Tab) / 4); k += blockDim.x) dst[k] = src[k];
   }
   const int lc = t / nq, q = t - lc * nq;
   const bool in_tile = lc < CPB;
@@ -107,15 +83,27 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
   long long node = 0;
   int cx = 0, cy = 0;
   if (active) {
-    cx = (int)(cell % I.nc[0]);
-    cy = (int)(cell / I.nc[0]);
+    // instances hold fewer than 2^31 cells (int32 DoF indices): 32-bit division
+    const unsigned int cl = (unsigned int)cell, n0 = (unsigned int)I.nc[0];
+    cy = (int)(cl / n0);
+    cx = (int)(cl - (unsigned int)cy * n0);
     node = (long long)(degree * cy + qb) * I.nn[0] + (degree * cx + qa);
     // gather: n = invM (.) acc of the previous step
-    vals[lc * nq + q] = P.invm[I.off + node] * P.acc_in[I.off + node];
+    const double v = P.invm[I.off + node] * P.acc_in[I.off + node];
+    vals[lc * nq + q] = v;
+    if (P.fx) atomicMax(&ex_in[lc], pg::fx::exponent(v));
   }
   if (in_tile)
     for (int r = 0; r < 3; ++r) outs[r * CPB * nq + lc * nq + q] = 0.0;
   __syncthreads();
+  if (P.fx) {
+    // fixed-point copy of the nodal values for exact integer derivatives (fixed_point.cuh)
+    if (active) {
+      const int E = ex_in[lc];
+      if (E != pg::fx::EXP_NONFINITE) vals_fx[lc * nq + q] = pg::fx::to_fixed(vals[lc * nq + q], E, pg::fx::TOP_VALUES);
+    }
+    __syncthreads();
+  }
   pg::CellCtx<2, degree, double> ctx;
   ctx.tab = tab;
   ctx.vals = vals;
@@ -128,6 +116,11 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
   ctx.cell[2] = 0;
   ctx.err = nullptr;
   ctx.submitted = 0;
+  if (P.fx) {
+    ctx.vals_fx = vals_fx;
+    ctx.ex_in = ex_in;
+    ctx.cpb = CPB;
+  }
   if (active) {
     AllenCahn<2, degree, double> pde{I.m_well, I.kappa};
     FieldContainer<2, degree, double> fc(ctx);
@@ -170,8 +163,9 @@ __global__ void __launch_bounds__(THREADS) ensemble_step_kernel(const EnsLaunch 
 
 template <int CPB1, int CPB2>
 size_t ens_smem_bytes() {
-  const size_t t1 = (sizeof(pg::CellTables<2, 1, double>) + 7) / 8 * 8 + 8 * 4 * CPB1 * 4;
-  const size_t t2 = (sizeof(pg::CellTables<2, 2, double>) + 7) / 8 * 8 + 8 * 4 * CPB2 * 9;
+  // tables, values, three output rows, the fixed-point values and the per-cell exponents
+  const size_t t1 = (sizeof(pg::CellTables<2, 1, double>) + 7) / 8 * 8 + 8 * 5 * CPB1 * 4 + 4 * CPB1;
+  const size_t t2 = (sizeof(pg::CellTables<2, 2, double>) + 7) / 8 * 8 + 8 * 5 * CPB2 * 9 + 4 * CPB2;
   return std::max(t1, t2) + 64;
 }
 
@@ -231,6 +225,8 @@ struct ppf_ensemble_s {
   std::string err;
   double gl_w[2][3];
   double gl_D[2][3][3];
+  unsigned char* d_tables = nullptr;  // per-instance CellTables, 16-byte aligned
+  int fx = 0;                         // the instance tables enable integer derivatives
 };
 
 namespace ppf {
@@ -303,17 +299,8 @@ EnsLaunch make_launch(ppf_ensemble e, long long step) {
   L.acc_zero = e->acc[(step + 2) % 3];
   L.total_len = e->total;
   L.dt = e->dt;
-  std::memcpy(L.gl_w, e->gl_w, sizeof(L.gl_w));
-  std::memcpy(L.gl_D, e->gl_D, sizeof(L.gl_D));
-  for (int deg = 1; deg <= 2; ++deg) {
-    const int n = deg + 1;
-    for (int q = 0; q < n * n; ++q)
-      for (int j = 0; j < n; ++j) {
-        const int a = q % n, b = q / n;
-        L.jbase[deg - 1][0][q][j] = e->gl_D[deg - 1][j][a] * e->gl_w[deg - 1][j] * e->gl_w[deg - 1][b];
-        L.jbase[deg - 1][1][q][j] = e->gl_D[deg - 1][j][b] * e->gl_w[deg - 1][a] * e->gl_w[deg - 1][j];
-      }
-  }
+  L.tables = e->d_tables;
+  L.fx = e->fx;
   return L;
 }
 
@@ -349,6 +336,17 @@ int ppf_ensemble_create(int n_instances, const ppf_mesh_desc* meshes, const doub
   }
   long long off = 0;
   std::vector<double> invm;
+  std::vector<unsigned char> tables;
+  // the instance tables: block 1 of the Allen-Cahn application reads old n (value and gradient)
+  // and submits n's value and gradient terms
+  signed char slot_of[pg::MAX_FIELDS][pg::NAGE], slot_comp0[pg::MAX_SLOTS], out_of[pg::MAX_FIELDS],
+      out_row0[pg::MAX_OUTS];
+  std::memset(slot_of, -1, sizeof(slot_of));
+  std::memset(slot_comp0, 0, sizeof(slot_comp0));
+  std::memset(out_of, -1, sizeof(out_of));
+  std::memset(out_row0, 0, sizeof(out_row0));
+  slot_of[0][1] = 0;
+  out_of[0] = 0;
   for (int i = 0; i < n_instances; ++i) {
     const ppf_mesh_desc& m = meshes[i];
     if (m.dim != 2 || m.degree < 1 || m.degree > 2 || m.periodic[0] || m.periodic[1]) {
@@ -364,6 +362,20 @@ int ppf_ensemble_create(int n_instances, const ppf_mesh_desc* meshes, const doub
     }
     I.N = (long long)I.nn[0] * I.nn[1];
     I.off = off;
+    {
+      const double lo[3] = {0.0, 0.0, 0.0}, hh[3] = {I.h[0], I.h[1], 1.0};
+      auto tb = build_cell_tables(2, I.degree, 0, lo, hh, slot_of, slot_comp0, out_of, out_row0, 1u);
+      if (tb.empty()) {
+        delete e;
+        return PPF_ERR_UNSUPPORTED;
+      }
+      I.tab_off = (long long)tables.size();
+      const int tfx = I.degree == 1 ? reinterpret_cast<const pg::CellTables<2, 1, double>*>(tb.data())->fx
+                                    : reinterpret_cast<const pg::CellTables<2, 2, double>*>(tb.data())->fx;
+      e->fx = (i == 0 ? 1 : e->fx) & (tfx != 0 ? 1 : 0);
+      tables.insert(tables.end(), tb.begin(), tb.end());
+      tables.resize((tables.size() + 15) / 16 * 16, 0);
+    }
     I.m_well = m_well[i];
     I.kappa = kappa[i];
     off += I.N;
@@ -390,6 +402,8 @@ int ppf_ensemble_create(int n_instances, const ppf_mesh_desc* meshes, const doub
   e->stream = e->own_stream;
   if (cudaMalloc(&e->d_inst, sizeof(EnsInstance) * n_instances) != cudaSuccess) return bail(PPF_ERR_CUDA);
   cudaMemcpy(e->d_inst, e->h_inst.data(), sizeof(EnsInstance) * n_instances, cudaMemcpyHostToDevice);
+  if (cudaMalloc(&e->d_tables, tables.size()) != cudaSuccess) return bail(PPF_ERR_CUDA);
+  cudaMemcpy(e->d_tables, tables.data(), tables.size(), cudaMemcpyHostToDevice);
   if (cudaMalloc(&e->invm, sizeof(double) * off) != cudaSuccess) return bail(PPF_ERR_CUDA);
   cudaMemcpy(e->invm, invm.data(), sizeof(double) * off, cudaMemcpyHostToDevice);
   for (int k = 0; k < 3; ++k) {
@@ -409,6 +423,7 @@ void ppf_ensemble_destroy(ppf_ensemble e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   cudaFree(e->d_inst);
+  cudaFree(e->d_tables);
   cudaFree(e->invm);
   for (int k = 0; k < 3; ++k) cudaFree(e->acc[k]);
   cudaFree(e->scratch);

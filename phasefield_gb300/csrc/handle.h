@@ -45,10 +45,11 @@ struct BlockPlan {
   signed char slot_comp0[pg::MAX_SLOTS];
   signed char out_of[pg::MAX_FIELDS];
   signed char out_row0[pg::MAX_OUTS];
-  // integer contractions (FP64 Q1/Q2): on in the tables; integration arithmetic chosen for this
-  // plan (-1 until the first plain launch times both, 0 FP64, 1 fixed point)
+  // integer contractions (FP64 Q1/Q2): on in the tables; arithmetic chosen for this plan
+  // (-1 until the first plain launch times the modes; 1 integer derivatives + FP64
+  // integration, 2 both in integers, 3 FP64 derivatives + integer integration)
   bool fx = false;
-  int fx_int = -1;
+  int fx_mode = -1;
 };
 
 // One mesh of a multigrid hierarchy for a single-field linear block (the finest level is the

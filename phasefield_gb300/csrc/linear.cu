@@ -389,6 +389,7 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   L.timer = h->timer;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
+  L.fx_deriv = 1;  // integer derivatives where the level's tables allow them (FP64 Q1/Q2)
   const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
   const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
   PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));
@@ -972,6 +973,11 @@ int linear_solve(ppf_handle h, int b) {
     Lc.timer = h->timer;
     Lc.block_id = (unsigned)B.desc.id;
     Lc.err = h->d_err;
+    {  // the plan's contraction mode if a plain launch chose one, else integer derivatives
+      const int m = P.fx_mode > 0 ? P.fx_mode : 1;
+      Lc.fx_deriv = m != 3;
+      Lc.fx_int = m >= 2;
+    }
     const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
     int rc = timed_cell_launch(h, 0, MODE_LHS, Lc, h->model_obj.data(), smem);
     if (rc) return rc;

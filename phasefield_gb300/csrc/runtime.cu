@@ -600,7 +600,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memcpy(P.out_of, out_of, sizeof(out_of));
   std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
   P.fx = tables_fx(tab, h->dim, h->k);
-  P.fx_int = -1;
+  P.fx_mode = -1;
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
   P.valid = true;
@@ -616,7 +616,7 @@ double* state_ptr(ppf_handle h, int f, int age) {
 
 // Launches the cell kernel of block b (which: 0 rhs, 1 lhs) accumulating into each block
 // field's acc. `src` supplies the SRC dependency per block field (may be null).
-static int choose_fx_integration(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem);
+static int choose_fx_mode(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem);
 
 int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool plain_src) {
   BlockState& B = h->blocks[b];
@@ -669,63 +669,72 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
   const int mode = which == 1 ? MODE_LHS : MODE_RHS;
   if (P.fx) {
-    if (P.fx_int < 0) {
-      // timing both integrations pays off for plans launched every increment or iteration; the
-      // right-hand side of a linear or Newton block (once per solve) integrates in FP64
-      if (which == 0 && B.desc.solve_type != PPF_EXPLICIT) {
-        P.fx_int = 0;
+    if (P.fx_mode < 0) {
+      // timing the modes pays off for plans launched every increment or iteration; the
+      // right-hand side of a linear or Newton block (once per solve) takes mode 1
+      const char* env = std::getenv("PPF_CONTRACTION_MODE");
+      if (which == 0 && B.desc.solve_type != PPF_EXPLICIT && !(env && env[0] >= '1' && env[0] <= '3')) {
+        P.fx_mode = 1;
       } else {
-        const int rc = choose_fx_integration(h, P, mode, L, smem);
+        const int rc = choose_fx_mode(h, P, mode, L, smem);
         if (rc) return rc;
       }
     }
-    L.fx_int = P.fx_int;
+    L.fx_deriv = P.fx_mode != 3;
+    L.fx_int = P.fx_mode >= 2;
   }
   return timed_cell_launch(h, 0, mode, L, h->model_obj.data(), smem);
 }
 
-// The integer-contraction kernels (FP64 Q1/Q2) take their derivatives in fixed point; their
-// integration can run in fixed point too (issue slots) or in FP64 (the FP64 pipe). Which is
-// cheaper depends on how much FP64 work the callback itself does, so the first plain launch of
-// a plan times both, twice each, back to back into the block's accumulators (which every
-// caller has just zeroed, and which are zeroed again afterwards), and keeps the faster.
-// PPF_FX_INTEGRATION=0 or 1 fixes the choice; a plan first launched inside a graph capture
-// integrates in FP64.
-static int choose_fx_integration(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem) {
-  const char* env = std::getenv("PPF_FX_INTEGRATION");
-  if (env && (env[0] == '0' || env[0] == '1')) {
-    P.fx_int = env[0] - '0';
+// The integer-contraction kernels (FP64 Q1/Q2) can take their derivatives and their integration
+// each in fixed point (issue slots) or in FP64 (the FP64 pipe). Which split is cheapest depends
+// on how much FP64 work the callback itself does, so the first plain launch of a plan times
+// modes 1 (integer derivatives, FP64 integration), 2 (both integer) and 3 (FP64 derivatives,
+// integer integration), twice each, back to back into the block's accumulators (which every
+// caller has just zeroed, and which are zeroed again afterwards), and keeps the fastest.
+// PPF_CONTRACTION_MODE=1, 2 or 3 fixes the mode; a plan first launched inside a graph capture
+// takes mode 1.
+static int choose_fx_mode(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem) {
+  const char* env = std::getenv("PPF_CONTRACTION_MODE");
+  if (env && env[0] >= '1' && env[0] <= '3') {
+    P.fx_mode = env[0] - '0';
     return PPF_OK;
   }
   if (h->capturing) {
-    P.fx_int = 0;
+    P.fx_mode = 1;
     return PPF_OK;
   }
-  cudaEvent_t ev[5] = {};
+  constexpr int NT = 6;  // modes 1, 2, 3, then again
+  cudaEvent_t ev[NT + 1] = {};
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
+  for (int i = 0; i <= NT && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
   CellLaunch T = L;
   if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
-  for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
-    T.fx_int = r & 1;
+  for (int r = 0; r < NT && e == cudaSuccess; ++r) {
+    const int m = 1 + r % 3;
+    T.fx_deriv = m != 3;
+    T.fx_int = m >= 2;
     e = h->custom_launch ? (cudaError_t)h->custom_launch(h->dim, h->k, mode, 0, &T, h->model_obj.data(), smem,
                                                          (void*)h->stream)
                          : h->model->launch(h->dim, h->k, mode, 0, T, h->model_obj.data(), smem, h->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[r + 1], h->stream);
   }
-  if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
-  float best[2] = {1e30f, 1e30f};
-  for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+  if (e == cudaSuccess) e = cudaEventSynchronize(ev[NT]);
+  float best[3] = {1e30f, 1e30f, 1e30f};
+  for (int r = 0; r < NT && e == cudaSuccess; ++r) {
     float ms = 0.f;
     e = cudaEventElapsedTime(&ms, ev[r], ev[r + 1]);
-    if (e == cudaSuccess && ms < best[r & 1]) best[r & 1] = ms;
+    if (e == cudaSuccess && ms < best[r % 3]) best[r % 3] = ms;
   }
   for (int i = 0; i < L.nout && e == cudaSuccess; ++i)
     e = cudaMemsetAsync(L.outs[i].acc, 0, sizeof(double) * (size_t)L.outs[i].ncomp * (size_t)L.N, h->stream);
-  for (int i = 0; i < 5; ++i)
+  for (int i = 0; i <= NT; ++i)
     if (ev[i]) cudaEventDestroy(ev[i]);
-  if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("integration timing: ") + cudaGetErrorString(e));
-  P.fx_int = best[1] < best[0] ? 1 : 0;
+  if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("contraction timing: ") + cudaGetErrorString(e));
+  int m = 0;
+  for (int i = 1; i < 3; ++i)
+    if (best[i] < best[m]) m = i;
+  P.fx_mode = 1 + m;
   return PPF_OK;
 }
 
@@ -1424,7 +1433,7 @@ int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode) {
   if (!h || !mode || b < 0 || b >= (int)h->blocks.size() || which < 0 || which > 1) return PPF_ERR_ARG;
   const BlockPlan& P = h->blocks[b].plan[which];
   if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
-  *mode = !P.fx || h->amr ? 0 : (P.fx_int < 0 ? -1 : 1 + P.fx_int);
+  *mode = !P.fx || h->amr ? 0 : P.fx_mode;
   return PPF_OK;
 }
 

@@ -2,8 +2,9 @@
 and integration sums with a per-cell block exponent, include/prismspf/gpu/fixed_point.cuh)
 against the oracle and against the same kernels contracting in FP64.
 
-Bars: one operator apply within 1e-12 relative L2 of the oracle (the FP64 apply bar), for both
-integration choices, non-cubic cells, fields scaled far from O(1) and values spanning many
+Bars: one operator apply within 1e-12 relative L2 of the oracle (the FP64 apply bar), in every
+mode (1 integer derivatives + FP64 integration, 2 both integer, 3 FP64 derivatives + integer
+integration), non-cubic cells, fields scaled far from O(1) and values spanning many
 binades inside a cell; fixed point against FP64 contractions within 1e-13 relative L2 (both
 are FP64-accurate; their difference is rounding)."""
 import contextlib
@@ -56,24 +57,27 @@ def ch_problem(dim, degree, size=None, scale_c=1.0, scale_mu=1.0, seed=3):
     return p, o
 
 
-@pytest.mark.parametrize("fx_int", ["0", "1"])
+MODES = ["1", "2", "3"]
+
+
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("dim,degree", [(2, 1), (2, 2), (3, 1), (3, 2)])
-def test_apply_matches_oracle_for_both_integrations(gpu_lib, dim, degree, fx_int):
-    with env(PPF_FX_INTEGRATION=fx_int):
+def test_apply_matches_oracle_in_every_mode(gpu_lib, dim, degree, mode):
+    with env(PPF_CONTRACTION_MODE=mode):
         p, o = ch_problem(dim, degree)
         for b in (0, 1):
             got = p.apply(b, 0, None, scale=1)
             ref = o.apply(b, 0, None, scale=1)
             assert rel_l2(got, ref) < APPLY_TOL, b
-            assert p.contraction_mode(b, 0) == 1 + int(fx_int)
+            assert p.contraction_mode(b, 0) == int(mode)
 
 
-@pytest.mark.parametrize("fx_int", ["0", "1"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("dim", [2, 3])
-def test_non_cubic_cells(gpu_lib, dim, fx_int):
+def test_non_cubic_cells(gpu_lib, dim, mode):
     """h_x != h_y (!= h_z): per-direction derivative scales, per-direction integration scales."""
     size = (8.0, 5.0, 3.0) if dim == 3 else (8.0, 3.0, 1.0)
-    with env(PPF_FX_INTEGRATION=fx_int):
+    with env(PPF_CONTRACTION_MODE=mode):
         p, o = ch_problem(dim, 2, size=size)
         for b in (0, 1):
             got = p.apply(b, 0, None, scale=1)
@@ -81,11 +85,11 @@ def test_non_cubic_cells(gpu_lib, dim, fx_int):
             assert rel_l2(got, ref) < APPLY_TOL, b
 
 
-@pytest.mark.parametrize("fx_int", ["0", "1"])
+@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("scale", [1e-150, 1e-20, 1e20, 1e150])
-def test_fields_far_from_unit_scale(gpu_lib, scale, fx_int):
+def test_fields_far_from_unit_scale(gpu_lib, scale, mode):
     """The c block is linear in (c, mu): scaling both moves every block exponent."""
-    with env(PPF_FX_INTEGRATION=fx_int):
+    with env(PPF_CONTRACTION_MODE=mode):
         p, o = ch_problem(3, 2, scale_c=scale, scale_mu=scale)
         got = p.apply(0, 0, None, scale=1)
         ref = o.apply(0, 0, None, scale=1)
@@ -93,11 +97,11 @@ def test_fields_far_from_unit_scale(gpu_lib, scale, fx_int):
         assert rel_l2(got, ref) < APPLY_TOL
 
 
-@pytest.mark.parametrize("fx_int", ["0", "1"])
-def test_values_spanning_many_binades_in_a_cell(gpu_lib, fx_int):
+@pytest.mark.parametrize("mode", MODES)
+def test_values_spanning_many_binades_in_a_cell(gpu_lib, mode):
     """mu = U(-1, 1) * 10^U(-30, 0) per node: small values share a cell with large ones."""
     wl = W.cahn_hilliard_3d(refine=2, degree=2, dim=3, size=8.0)
-    with env(PPF_FX_INTEGRATION=fx_int):
+    with env(PPF_CONTRACTION_MODE=mode):
         p = wl.make_problem()
         o = po.Oracle(wl)
         rng = np.random.default_rng(9)
@@ -112,31 +116,32 @@ def test_values_spanning_many_binades_in_a_cell(gpu_lib, fx_int):
         assert rel_l2(got, ref) < APPLY_TOL
 
 
-@pytest.mark.parametrize("fx_int", ["0", "1"])
-def test_vector_elasticity_lhs(gpu_lib, fx_int):
+@pytest.mark.parametrize("mode", MODES)
+def test_vector_elasticity_lhs(gpu_lib, mode):
     """Symmetric gradients of a vector field and a tensor gradient term (3 components)."""
     wl = W.eshelby_3d(refine=2, degree=2, size=16.0, n_incl=5, dim=3)
-    with env(PPF_FX_INTEGRATION=fx_int):
+    with env(PPF_CONTRACTION_MODE=mode):
         p = wl.make_problem()
         o = po.Oracle(wl)
         u = np.random.default_rng(11).uniform(-1, 1, p.field_length(0))
         got = p.apply(0, 1, u, scale=0)
         ref = o.apply(0, 1, u, scale=0)
         assert rel_l2(got, ref) < APPLY_TOL
-        assert p.contraction_mode(0, 1) == 1 + int(fx_int)
+        assert p.contraction_mode(0, 1) == int(mode)
 
 
 def test_fixed_point_against_fp64_contractions(gpu_lib):
+    """Every mode against FP64 contractions on the same inputs."""
     outs = {}
-    for key, kw in (("fp64", {"PPF_FP64_CONTRACTIONS": "1"}), ("fx1", {"PPF_FX_INTEGRATION": "0"}),
-                    ("fx2", {"PPF_FX_INTEGRATION": "1"})):
+    for key, kw in (("0", {"PPF_FP64_CONTRACTIONS": "1"}), ("1", {"PPF_CONTRACTION_MODE": "1"}),
+                    ("2", {"PPF_CONTRACTION_MODE": "2"}), ("3", {"PPF_CONTRACTION_MODE": "3"})):
         with env(**kw):
             p, _ = ch_problem(3, 2)
             outs[key] = [p.apply(b, 0, None, scale=1) for b in (0, 1)]
-            assert p.contraction_mode(0, 0) == {"fp64": 0, "fx1": 1, "fx2": 2}[key]
-    for key in ("fx1", "fx2"):
+            assert p.contraction_mode(0, 0) == int(key)
+    for key in ("1", "2", "3"):
         for b in (0, 1):
-            assert rel_l2(outs[key][b], outs["fp64"][b]) < 1e-13, (key, b)
+            assert rel_l2(outs[key][b], outs["0"][b]) < 1e-13, (key, b)
 
 
 def test_modes_outside_the_fixed_point_path(gpu_lib):
@@ -149,4 +154,4 @@ def test_modes_outside_the_fixed_point_path(gpu_lib):
     p = wl.make_problem()
     p.upload(0, wl.initial[0], age=1)
     p.apply(0, 0, None, scale=1)
-    assert p.contraction_mode(0, 0) in (1, 2)  # chosen by timing both on the first launch
+    assert p.contraction_mode(0, 0) in (1, 2, 3)  # chosen by timing the modes on the first launch
