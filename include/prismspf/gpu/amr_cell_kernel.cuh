@@ -40,7 +40,11 @@ template <int dim, int degree, typename number>
 __host__ __device__ inline size_t amr_cell_smem_bytes(int nlev, int nrows_in, int nrows_out) {
   using S = CellShape<dim, degree>;
   const size_t tab = (sizeof(pg::CellTables<dim, degree, number>) + 15) / 16 * 16;
-  return tab * (size_t)nlev + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
+  size_t b = tab * (size_t)nlev + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
+  // integer derivatives (FP64 Q1/Q2): fixed-point values and per-cell block exponents
+  if (cell_fx_capable<dim, degree, number>())
+    b += sizeof(long long) * (size_t)nrows_in * S::threads + sizeof(int) * (size_t)nrows_in * S::cpb;
+  return b;
 }
 
 template <class PDE, int dim, int degree, int MODE, typename number>
@@ -56,6 +60,20 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, 1)
   number* vals = reinterpret_cast<number*>(smem_raw + tab_stride * A.nlev);
   number* outs = vals + P.nrows_in * S::threads;
   __shared__ int sflags;
+  // integer derivatives (fixed_point.cuh) with every level's tables, FP64 integration
+  constexpr bool FXC = cell_fx_capable<dim, degree, number>();
+  long long* vals_fx = reinterpret_cast<long long*>(outs + P.nrows_out * S::threads);
+  int* ex_in = reinterpret_cast<int*>(vals_fx + P.nrows_in * S::threads);
+  bool fx_on = false;
+  unsigned int fx_rows = 0;
+  if constexpr (FXC) {
+    unsigned int dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const Tab* g0 = static_cast<const Tab*>(P.tables);
+    fx_on = P.fx_deriv != 0 && g0->fx != 0 &&
+            dyn >= (unsigned int)amr_cell_smem_bytes<dim, degree, number>(A.nlev, P.nrows_in, P.nrows_out);
+    fx_rows = g0->fx_rows;
+  }
 
   for (int l = 0; l < A.nlev; ++l) {
     const int nwords = (int)(sizeof(Tab) / 4);
@@ -82,6 +100,11 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, 1)
     if (active) {
       info = __ldg(A.cell_info + cell);
       dof = __ldg(A.cell_dofs + cell * nq + q);
+    }
+    if constexpr (FXC) {
+      // last read by the previous tile's callbacks; rows without a fixed-point copy keep -1
+      if (fx_on)
+        for (int i = t; i < P.nrows_in * cpb; i += S::threads) ex_in[i] = ((fx_rows >> (i / cpb)) & 1u) ? 0 : -1;
     }
     __syncthreads();  // tables staged; previous tile finished with vals/outs/sflags
 
@@ -113,18 +136,38 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, 1)
               }
             }
             vals[(row + c) * S::threads + t] = v;
+            if constexpr (FXC) {
+              if (fx_on && ((fx_rows >> (row + c)) & 1u)) atomicMax(&ex_in[(row + c) * cpb + lc], pg::fx::exponent(v));
+            }
           }
           row += sd.ncomp;
         }
       }
     }
 
+    if constexpr (FXC) {
+      if (fx_on) {
+        __syncthreads();  // block exponents of the value rows complete
+        for (int r = 0; r < P.nrows_in; ++r) {
+          const int E = ex_in[r * cpb + lc];
+          if (E >= 0 && E != pg::fx::EXP_NONFINITE)
+            vals_fx[r * S::threads + t] = pg::fx::to_fixed(vals[r * S::threads + t], E, pg::fx::TOP_VALUES);
+        }
+      }
+    }
     if (t == 0) sflags = 0;
     for (int r = 0; r < P.nrows_out; ++r) outs[r * S::threads + t] = number(0);
     __syncthreads();
 
     pg::CellCtx<dim, degree, number> ctx;
     ctx.tab = reinterpret_cast<const Tab*>(smem_raw + tab_stride * info.x);
+    if constexpr (FXC) {
+      if (fx_on) {
+        ctx.vals_fx = vals_fx;
+        ctx.ex_in = ex_in;
+        ctx.cpb = cpb;
+      }
+    }
     ctx.vals = vals;
     ctx.outs = outs;
     ctx.stride = S::threads;

@@ -665,6 +665,8 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   L.timer_dev = h->capturing ? h->d_timer : nullptr;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
+  // adaptive meshes: integer derivatives with every level's tables, FP64 integration
+  L.fx_deriv = 1;
   if (h->amr) return amr_launch_cell(h, b, which, L);
   const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
   const int mode = which == 1 ? MODE_LHS : MODE_RHS;
@@ -1433,7 +1435,7 @@ int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode) {
   if (!h || !mode || b < 0 || b >= (int)h->blocks.size() || which < 0 || which > 1) return PPF_ERR_ARG;
   const BlockPlan& P = h->blocks[b].plan[which];
   if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
-  *mode = !P.fx || h->amr ? 0 : P.fx_mode;
+  *mode = !P.fx ? 0 : (h->amr ? 1 : P.fx_mode);
   return PPF_OK;
 }
 
