@@ -221,6 +221,7 @@ def gmg_cg_measure(refine=6, depth=7):
         out[key + "_phases_ms"] = p.linear_stats(0)
         out[key + "_iterations"] = its
         out[key + "_rel_residual"] = res / bnorm
+        out[key + "_contraction_mode"] = p.contraction_mode(0, 1)
         sols[key] = p.download(0)
         p.close()
     out["speedup_mixed_vs_fp64"] = out["fp64_s"] / out["mixed_s"]

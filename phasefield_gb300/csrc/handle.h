@@ -85,6 +85,11 @@ struct MGLevel {
   void* t0 = nullptr;           // transfer work buffers (fine-sized)
   void* t1 = nullptr;
   void* cvt = nullptr;          // precision-conversion buffer (coarsest level of a mixed hierarchy)
+  // contraction mode of the level's FP64 operator (integer contractions, FP64 Q1/Q2): its first
+  // six plain LHS launches run modes 1, 2, 3 twice under CUDA events, then the fastest stays
+  int fx_mode = -1;
+  int fx_timed = 0;
+  cudaEvent_t fx_ev[12] = {};
 };
 
 struct AdjointState;

@@ -24,6 +24,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -352,6 +353,15 @@ static int upload_real(ppf_handle h, void** dst, const std::vector<double>& v, i
 // ------------------------------------------------------------------------------------------
 // level operators
 // ------------------------------------------------------------------------------------------
+// Contraction mode of the multigrid operators (levels and the outer FP64 operator):
+// PPF_CONTRACTION_MODE if set, else the LHS plan's timed choice if a plain launch made one,
+// else integer derivatives with FP64 integration.
+static int multigrid_fx_mode(const BlockPlan& P) {
+  const char* env = std::getenv("PPF_CONTRACTION_MODE");
+  if (env && env[0] >= '1' && env[0] <= '3') return env[0] - '0';
+  return P.fx_mode > 0 ? P.fx_mode : 1;
+}
+
 static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode, const void* src, bool plain_read) {
   const int f = B.desc.field_indices[0];
   FieldState& F = h->fields[f];
@@ -389,11 +399,56 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   L.timer = h->timer;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
-  L.fx_deriv = 1;  // integer derivatives where the level's tables allow them (FP64 Q1/Q2)
+  // integer contractions where the level's tables allow them (FP64 Q1/Q2); the mode is timed
+  // online over the level's first plain LHS launches, which are real work (the modes agree to
+  // rounding), so choosing costs no extra launches
+  int slot = -1;
+  int m = multigrid_fx_mode(P);
+  const char* env = std::getenv("PPF_CONTRACTION_MODE");
+  const bool fixed = env && env[0] >= '1' && env[0] <= '3';
+  if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed) {
+    // the V-cycle is captured into a graph: no timing (nor event waits) inside a capture
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PPF_CUDA(h, cudaStreamIsCapturing(h->stream, &cs));
+    if (lv.fx_mode > 0) {
+      m = lv.fx_mode;
+    } else if (h->capturing || cs != cudaStreamCaptureStatusNone) {
+      lv.fx_mode = m = 1;
+    } else {
+      slot = lv.fx_timed;
+      m = 1 + slot % 3;
+      for (int i = 2 * slot; i < 2 * slot + 2; ++i)
+        if (!lv.fx_ev[i]) PPF_CUDA(h, cudaEventCreate(&lv.fx_ev[i]));
+    }
+  }
+  L.fx_deriv = m != 3;
+  L.fx_int = m >= 2;
   const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
   const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
   PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));
-  return timed_cell_launch(h, lv.precision, mode, L, obj, smem);
+  if (slot < 0) return timed_cell_launch(h, lv.precision, mode, L, obj, smem);
+  PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot], h->stream));
+  const int rc = timed_cell_launch(h, lv.precision, mode, L, obj, smem);
+  if (rc) return rc;
+  PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot + 1], h->stream));
+  if (++lv.fx_timed == 6) {
+    PPF_CUDA(h, cudaEventSynchronize(lv.fx_ev[11]));
+    float best[3] = {1e30f, 1e30f, 1e30f};
+    for (int k = 0; k < 6; ++k) {
+      float ms = 0.f;
+      PPF_CUDA(h, cudaEventElapsedTime(&ms, lv.fx_ev[2 * k], lv.fx_ev[2 * k + 1]));
+      best[k % 3] = std::min(best[k % 3], ms);
+    }
+    int b = 0;
+    for (int k = 1; k < 3; ++k)
+      if (best[k] < best[b]) b = k;
+    lv.fx_mode = 1 + b;
+    for (auto& ev : lv.fx_ev) {
+      cudaEventDestroy(ev);
+      ev = nullptr;
+    }
+  }
+  return PPF_OK;
 }
 
 static bool scaled(const LinearState& L) { return L.params.tolerance_type != 0; }
@@ -973,8 +1028,10 @@ int linear_solve(ppf_handle h, int b) {
     Lc.timer = h->timer;
     Lc.block_id = (unsigned)B.desc.id;
     Lc.err = h->d_err;
-    {  // the plan's contraction mode if a plain launch chose one, else integer derivatives
-      const int m = P.fx_mode > 0 ? P.fx_mode : 1;
+    {  // the finest level is this operator on the same mesh: its timed mode if it has one
+      const int lm = L.levels.empty() ? -1 : L.levels.back().fx_mode;
+      const char* env = std::getenv("PPF_CONTRACTION_MODE");
+      const int m = (lm > 0 && !(env && env[0] >= '1' && env[0] <= '3')) ? lm : multigrid_fx_mode(P);
       Lc.fx_deriv = m != 3;
       Lc.fx_int = m >= 2;
     }
@@ -1330,6 +1387,8 @@ void free_linear(LinearState& L) {
   L.newton_update = nullptr;
   L.block_len = 0;
   for (auto& lv : L.levels) {
+    for (auto& ev : lv.fx_ev)
+      if (ev) cudaEventDestroy(ev);
     cudaFree(lv.cmap);
     for (void* p : {lv.invm_sqrt, lv.inv_diag, lv.tables, lv.acc, lv.x, lv.b, lv.r, lv.w0, lv.w1, lv.t0, lv.t1, lv.cvt})
       cudaFree(p);

@@ -1436,6 +1436,9 @@ int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode) {
   const BlockPlan& P = h->blocks[b].plan[which];
   if (!P.valid) return fail(h, PPF_ERR_ARG, "block has no plan for this operator");
   *mode = !P.fx ? 0 : (h->amr ? 1 : P.fx_mode);
+  // a multigrid-preconditioned block: the finest FP64 level's timed mode (its own operator)
+  const auto& lvs = h->blocks[b].lin.levels;
+  if (P.fx && !h->amr && which == 1 && *mode < 0 && !lvs.empty() && lvs.back().fx_mode > 0) *mode = lvs.back().fx_mode;
   return PPF_OK;
 }
 
