@@ -140,6 +140,16 @@ int ppf_set_dirichlet_values(ppf_handle h, int field, const double* values);
  * condition (solver_base.h:178-229). `out` receives lattice node indices, n_cells*(k+1)^dim. */
 int ppf_dealii_cell_nodes(ppf_handle h, long long first_cell, long long n_cells, long long* out);
 
+/* Streams field f to host memory after every increment: the device-to-host copy of an
+ * explicitly solved field is queued on a copy stream as soon as its block's finalize kernel has
+ * run, so it overlaps the blocks after it; fields no explicit block writes are copied at the end
+ * of the increment. ppf_run / ppf_end_increment return after the copies completed (host then
+ * holds the increment's solution, as ppf_download_solution would return it). host == NULL
+ * stops streaming the field. Lattice (= native) order only; not on adaptive meshes; increments
+ * with streamed outputs run as plain launches (no graph replay). Pinned host memory makes the
+ * copies asynchronous. Engine-side addition: the reference writes outputs from host vectors. */
+int ppf_set_output_stream(ppf_handle h, int f, double* host, int ordering);
+
 /* The solution of field f as it stood at the end of the last increment's solves, before the
  * age rotation (what SolutionOutput writes, problem.cc:505-552). */
 int ppf_download_solution(ppf_handle h, int field, double* host, int ordering);

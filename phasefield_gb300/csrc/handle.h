@@ -31,6 +31,9 @@ struct FieldState {
   std::vector<long long> h_drow;  // position (component-major lattice index) of Dirichlet row j
   bool constrained = false;
   ppf_field_desc desc;
+  // host destination the field is streamed to after every increment (ppf_set_output_stream)
+  double* stream_out = nullptr;
+  bool streamed = false;  // copied during the current increment
 };
 
 struct BlockPlan {
@@ -166,6 +169,9 @@ struct ppf_handle_s {
   int* d_err = nullptr;
   cudaStream_t stream = nullptr;      // stream all work is queued on
   cudaStream_t own_stream = nullptr;  // the handle's own stream
+  cudaStream_t copy_stream = nullptr; // device-to-host copies of streamed outputs
+  cudaEvent_t copy_ev = nullptr;
+  bool copies_pending = false;
   prismspf::SimulationTimer timer;
   double dt = 0.0;
   std::string err;

@@ -771,6 +771,8 @@ unsigned grid_for(long long n) {
 
 static int explicit_solve(ppf_handle h, int b);
 int explicit_solve_entry(ppf_handle h, int b) { return explicit_solve(h, b); }
+int stream_field_out(ppf_handle h, FieldState& F, const double* src);
+int finish_streamed_outputs(ppf_handle h);
 
 static int explicit_solve(ppf_handle h, int b) {
   BlockState& B = h->blocks[b];
@@ -792,7 +794,27 @@ static int explicit_solve(ppf_handle h, int b) {
                                                           F.dvals, h->N, h->d_err);
     PPF_CUDA(h, cudaGetLastError());
     h->all_launches++;
+    if (F.stream_out) {
+      // the field is final: copy it out on the copy stream while the later blocks compute
+      rc = stream_field_out(h, F, F.cur);
+      if (rc) return rc;
+    }
   }
+  return PPF_OK;
+}
+
+// Queues the device-to-host copy of a streamed output on the copy stream, ordered after the
+// work already queued on the handle's stream (ppf_set_output_stream).
+int stream_field_out(ppf_handle h, FieldState& F, const double* src) {
+  if (!h->copy_stream) {
+    PPF_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    PPF_CUDA(h, cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
+  }
+  PPF_CUDA(h, cudaEventRecord(h->copy_ev, h->stream));
+  PPF_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
+  PPF_CUDA(h, cudaMemcpyAsync(F.stream_out, src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->copy_stream));
+  F.streamed = true;
+  h->copies_pending = true;
   return PPF_OK;
 }
 
@@ -875,7 +897,25 @@ static int solve_increment(ppf_handle h, int output_every) {
     int rc = amr_remesh_if_due(h);
     if (rc) return rc;
   }
+  const int rc = finish_streamed_outputs(h);
+  if (rc) return rc;
   end_increment(h);
+  return PPF_OK;
+}
+
+// End of an increment for the streamed outputs: fields no explicit block wrote this increment
+// are copied from their current solution, then the copies are waited for.
+int finish_streamed_outputs(ppf_handle h) {
+  for (auto& F : h->fields)
+    if (F.stream_out && !F.streamed) {
+      int rc = stream_field_out(h, F, F.cur);
+      if (rc) return rc;
+    }
+  if (h->copies_pending) {
+    PPF_CUDA(h, cudaStreamSynchronize(h->copy_stream));
+    h->copies_pending = false;
+  }
+  for (auto& F : h->fields) F.streamed = false;
   return PPF_OK;
 }
 
@@ -1074,6 +1114,11 @@ void ppf_destroy(ppf_handle h) {
     return;
   }
   cudaStreamSynchronize(h->stream);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+    cudaEventDestroy(h->copy_ev);
+  }
   for (auto& F : h->fields) {
     cudaFree(F.cur);
     for (int a = 0; a < 4; ++a) cudaFree(F.old[a]);
@@ -1168,6 +1213,15 @@ int ppf_download_state(ppf_handle h, int f, int age, double* host, int ordering)
   return permute_io(h, f, host, p, nullptr, ordering, false);
 }
 
+int ppf_set_output_stream(ppf_handle h, int f, double* host, int ordering) {
+  if (!h || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "streamed outputs on an adaptive mesh (use ppf_download_solution)");
+  if (host && ordering != PPF_ORDER_LATTICE && ordering != PPF_ORDER_NATIVE)
+    return fail(h, PPF_ERR_UNSUPPORTED, "streamed outputs are copied in lattice order");
+  h->fields[f].stream_out = host;
+  return PPF_OK;
+}
+
 int ppf_download_solution(ppf_handle h, int f, double* host, int ordering) {
   if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
   FieldState& F = h->fields[f];
@@ -1234,8 +1288,11 @@ int ppf_solve_block(ppf_handle h, int b) {
 // memory during replays, so time-dependent operators see the right time.
 static bool graph_eligible(ppf_handle h, int output_every) {
   // per-launch event timing needs plain launches; postprocess increments are not periodic
-  // (adaptive meshes replay only between remeshing increments, see ppf_run)
+  // (adaptive meshes replay only between remeshing increments, see ppf_run); streamed outputs
+  // are copied out after every increment
   if (!h->use_graph || h->timing || output_every > 0) return false;
+  for (auto& F : h->fields)
+    if (F.stream_out) return false;
   for (auto& B : h->blocks) {
     const int t = B.desc.solve_type;
     if (t != PPF_EXPLICIT && t != PPF_CONSTANT) return false;
@@ -1342,6 +1399,8 @@ int ppf_increment_block(ppf_handle h, int b, int is_output) {
 
 int ppf_end_increment(ppf_handle h) {
   if (!h) return PPF_ERR_ARG;
+  const int rc = finish_streamed_outputs(h);
+  if (rc) return rc;
   end_increment(h);
   return check_err(h);
 }

@@ -171,6 +171,24 @@ class Problem:
         if rc != capi.PPF_OK:
             raise capi.PPFError(rc, self.lib.ppf_last_error(self.h).decode())
 
+    def set_output_stream(self, f: int, host=None):
+        """Stream field f into `host` (a float64 array of field_length(f), lattice order; pinned
+        memory makes the copy asynchronous) after every increment, overlapping the copy with the
+        blocks solved after f's (ppf_set_output_stream); None stops it."""
+        streams = getattr(self, "_streams", {})
+        if host is None:
+            self._check(self.lib.ppf_set_output_stream(self.h, f, None, capi.ORDER_LATTICE))
+            streams.pop(f, None)
+            self._streams = streams
+            return
+        ptr = host.data_ptr() if hasattr(host, "data_ptr") else host.ctypes.data
+        n = host.numel() if hasattr(host, "numel") else host.size
+        if n != self.field_length(f):
+            raise ValueError("host buffer length differs from the field length")
+        self._check(self.lib.ppf_set_output_stream(self.h, f, C.cast(ptr, C.POINTER(C.c_double)), capi.ORDER_LATTICE))
+        streams[f] = host  # the engine writes into it until streaming stops
+        self._streams = streams
+
     def contraction_mode(self, block: int, which: int = 0) -> int:
         """0 FP64 contractions, 1 fixed-point derivatives with FP64 integration, 2 both in fixed
         point, 3 FP64 derivatives with fixed-point integration, -1 not chosen yet
@@ -221,6 +239,12 @@ class Problem:
     def download(self, f: int, age: int = 0, ordering: int = capi.ORDER_LATTICE) -> np.ndarray:
         out = np.empty(self._io_length(f, ordering), dtype=np.float64)
         self._check(self.lib.ppf_download_state(self.h, f, age, capi.dptr(out), ordering))
+        return out
+
+    def download_solution(self, f: int, ordering: int = capi.ORDER_LATTICE) -> np.ndarray:
+        """The field's solution after the last increment (ppf_download_solution)."""
+        out = np.empty(self._io_length(f, ordering), dtype=np.float64)
+        self._check(self.lib.ppf_download_solution(self.h, f, capi.dptr(out), ordering))
         return out
 
     # --- adaptive meshes --------------------------------------------------------------------
