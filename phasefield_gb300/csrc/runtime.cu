@@ -702,7 +702,10 @@ static int choose_fx_mode(ppf_handle h, BlockPlan& P, int mode, const CellLaunch
     P.fx_mode = env[0] - '0';
     return PPF_OK;
   }
-  if (h->capturing) {
+  // no timing inside a graph capture (the engine's own, or one the caller runs on its stream)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  PPF_CUDA(h, cudaStreamIsCapturing(h->stream, &cs));
+  if (h->capturing || cs != cudaStreamCaptureStatusNone) {
     P.fx_mode = 1;
     return PPF_OK;
   }
