@@ -181,7 +181,9 @@ __device__ __forceinline__ double integrate_row_fx(const pg::CellTables<dim, deg
   return r;
 }
 
-template <class PDE, int dim, int degree, int MODE, typename number>
+// FXINT: compile the fixed-point integration path (modes 2 and 3); the mode-1 instantiation
+// leaves it out, which keeps its register budget for the derivative path
+template <class PDE, int dim, int degree, int MODE, typename number, bool FXINT = false>
 __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks<PDE>::value)
     cell_kernel(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde) {
   using S = CellShape<dim, degree>;
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
         gtab->fx != 0 && dyn >= (unsigned int)cell_smem_bytes<dim, degree, number>(P.nrows_in, P.nrows_out);
     tab_fx_rows = gtab->fx_rows;
     fx_on = fx_ok && P.fx_deriv != 0;
-    fx_int = fx_ok && P.fx_int != 0;
+    if constexpr (FXINT) fx_int = fx_ok && P.fx_int != 0;
   }
   // cell coordinates by multiply-high division (cell indices stay below 2^31: DoF indices are int)
   pg::fx::FastDiv div0, div1;

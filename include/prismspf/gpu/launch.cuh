@@ -14,10 +14,10 @@
 
 namespace ppf {
 
-template <class PDE, int dim, int degree, int mode, typename number>
-cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
+template <class PDE, int dim, int degree, int mode, typename number, bool FXINT>
+cudaError_t launch_cell_kernel_impl(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
   using S = CellShape<dim, degree>;
-  auto kern = cell_kernel<PDE, dim, degree, mode, number>;
+  auto kern = cell_kernel<PDE, dim, degree, mode, number, FXINT>;
   static size_t attr_smem = 0;
   static int occ = 0;
   static int sms = 0;
@@ -41,6 +41,16 @@ cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj));
   return cudaGetLastError();
+}
+
+// launches the instantiation with the fixed-point integration path only when the launch asks
+// for it (contraction modes 2 and 3 of FP64 Q1/Q2 operators)
+template <class PDE, int dim, int degree, int mode, typename number>
+cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
+  if constexpr (cell_fx_capable<dim, degree, number>() && mode != MODE_DIAG) {
+    if (P.fx_int) return launch_cell_kernel_impl<PDE, dim, degree, mode, number, true>(P, obj, smem, s);
+  }
+  return launch_cell_kernel_impl<PDE, dim, degree, mode, number, false>(P, obj, smem, s);
 }
 
 // The adaptive-mesh kernel for a mode without the MODE_AMR flag; `rec` is an AmrCellLaunch.
