@@ -53,6 +53,8 @@ struct BlockPlan {
   // integration, 2 both in integers, 3 FP64 derivatives + integer integration)
   bool fx = false;
   int fx_mode = -1;
+  int fx_timed = 0;                // online timing of the multigrid outer operator
+  cudaEvent_t fx_ev[12] = {};
 };
 
 // One mesh of a multigrid hierarchy for a single-field linear block (the finest level is the

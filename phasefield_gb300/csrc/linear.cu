@@ -362,6 +362,51 @@ static int multigrid_fx_mode(const BlockPlan& P) {
   return P.fx_mode > 0 ? P.fx_mode : 1;
 }
 
+// Online choice of a contraction mode: the first six plain launches of an operator run modes 1,
+// 2, 3 twice under CUDA events (real work: the modes agree to rounding), then the fastest
+// stays in `state`. begin returns the mode of this launch and the event slot (-1: not timed);
+// end records the closing event and decides after the sixth.
+static int online_mode_begin(ppf_handle h, int& state, int timed, cudaEvent_t* ev, int fallback, int* slot) {
+  *slot = -1;
+  if (state > 0) return state;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess || h->capturing || cs != cudaStreamCaptureStatusNone) {
+    state = fallback;  // no timing (nor event waits) inside a graph capture
+    return state;
+  }
+  *slot = timed;
+  for (int i = 2 * timed; i < 2 * timed + 2; ++i)
+    if (!ev[i] && cudaEventCreate(&ev[i]) != cudaSuccess) {
+      *slot = -1;
+      state = fallback;
+      return state;
+    }
+  cudaEventRecord(ev[2 * timed], h->stream);
+  return 1 + timed % 3;
+}
+
+static int online_mode_end(ppf_handle h, int& state, int& timed, cudaEvent_t* ev, int slot) {
+  if (slot < 0) return PPF_OK;
+  PPF_CUDA(h, cudaEventRecord(ev[2 * slot + 1], h->stream));
+  if (++timed < 6) return PPF_OK;
+  PPF_CUDA(h, cudaEventSynchronize(ev[11]));
+  float best[3] = {1e30f, 1e30f, 1e30f};
+  for (int k = 0; k < 6; ++k) {
+    float t = 0.f;
+    PPF_CUDA(h, cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]));
+    best[k % 3] = std::min(best[k % 3], t);
+  }
+  int b = 0;
+  for (int k = 1; k < 3; ++k)
+    if (best[k] < best[b]) b = k;
+  state = 1 + b;
+  for (int i = 0; i < 12; ++i) {
+    cudaEventDestroy(ev[i]);
+    ev[i] = nullptr;
+  }
+  return PPF_OK;
+}
+
 static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode, const void* src, bool plain_read) {
   const int f = B.desc.field_indices[0];
   FieldState& F = h->fields[f];
@@ -400,55 +445,21 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
   // integer contractions where the level's tables allow them (FP64 Q1/Q2); the mode is timed
-  // online over the level's first plain LHS launches, which are real work (the modes agree to
-  // rounding), so choosing costs no extra launches
+  // online over the level's first plain LHS launches, so choosing costs no extra launches
   int slot = -1;
   int m = multigrid_fx_mode(P);
   const char* env = std::getenv("PPF_CONTRACTION_MODE");
   const bool fixed = env && env[0] >= '1' && env[0] <= '3';
-  if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed) {
-    // the V-cycle is captured into a graph: no timing (nor event waits) inside a capture
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    PPF_CUDA(h, cudaStreamIsCapturing(h->stream, &cs));
-    if (lv.fx_mode > 0) {
-      m = lv.fx_mode;
-    } else if (h->capturing || cs != cudaStreamCaptureStatusNone) {
-      lv.fx_mode = m = 1;
-    } else {
-      slot = lv.fx_timed;
-      m = 1 + slot % 3;
-      for (int i = 2 * slot; i < 2 * slot + 2; ++i)
-        if (!lv.fx_ev[i]) PPF_CUDA(h, cudaEventCreate(&lv.fx_ev[i]));
-    }
-  }
+  if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed) m = online_mode_begin(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, 1, &slot);
   L.fx_deriv = m != 3;
   L.fx_int = m >= 2;
   const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
   const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
   PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));
-  if (slot < 0) return timed_cell_launch(h, lv.precision, mode, L, obj, smem);
-  PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot], h->stream));
+  if (slot >= 0) PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot], h->stream));  // after the memset
   const int rc = timed_cell_launch(h, lv.precision, mode, L, obj, smem);
   if (rc) return rc;
-  PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot + 1], h->stream));
-  if (++lv.fx_timed == 6) {
-    PPF_CUDA(h, cudaEventSynchronize(lv.fx_ev[11]));
-    float best[3] = {1e30f, 1e30f, 1e30f};
-    for (int k = 0; k < 6; ++k) {
-      float ms = 0.f;
-      PPF_CUDA(h, cudaEventElapsedTime(&ms, lv.fx_ev[2 * k], lv.fx_ev[2 * k + 1]));
-      best[k % 3] = std::min(best[k % 3], ms);
-    }
-    int b = 0;
-    for (int k = 1; k < 3; ++k)
-      if (best[k] < best[b]) b = k;
-    lv.fx_mode = 1 + b;
-    for (auto& ev : lv.fx_ev) {
-      cudaEventDestroy(ev);
-      ev = nullptr;
-    }
-  }
-  return PPF_OK;
+  return online_mode_end(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, slot);
 }
 
 static bool scaled(const LinearState& L) { return L.params.tolerance_type != 0; }
@@ -1003,7 +1014,7 @@ int linear_solve(ppf_handle h, int b) {
     }
     Lc.N = h->N;
     Lc.ncells = h->ncells;
-    const BlockPlan& P = B.plan[1];
+    BlockPlan& P = B.plan[1];
     Lc.nslots = P.nslots;
     for (int s = 0; s < P.nslots; ++s) {
       SlotDesc& sd = Lc.slots[s];
@@ -1028,15 +1039,23 @@ int linear_solve(ppf_handle h, int b) {
     Lc.timer = h->timer;
     Lc.block_id = (unsigned)B.desc.id;
     Lc.err = h->d_err;
-    {  // the finest level is this operator on the same mesh: its timed mode if it has one
+    // the finest level is this operator on the same mesh: its timed mode if it has one; else
+    // (an FP32 finest level) the plan's own mode, timed online over its first outer launches
+    int slot = -1;
+    {
       const int lm = L.levels.empty() ? -1 : L.levels.back().fx_mode;
       const char* env = std::getenv("PPF_CONTRACTION_MODE");
-      const int m = (lm > 0 && !(env && env[0] >= '1' && env[0] <= '3')) ? lm : multigrid_fx_mode(P);
+      const bool fixed = env && env[0] >= '1' && env[0] <= '3';
+      int m = multigrid_fx_mode(P);
+      if (!fixed && lm > 0) m = lm;
+      else if (!fixed && P.fx) m = online_mode_begin(h, P.fx_mode, P.fx_timed, P.fx_ev, 1, &slot);
       Lc.fx_deriv = m != 3;
       Lc.fx_int = m >= 2;
     }
     const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
     int rc = timed_cell_launch(h, 0, MODE_LHS, Lc, h->model_obj.data(), smem);
+    if (rc) return rc;
+    rc = online_mode_end(h, P.fx_mode, P.fx_timed, P.fx_ev, slot);
     if (rc) return rc;
     dim3 grid(grid_for(h->N), F.ncomp);
     level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>(dst, F.acc, scaled(L) ? h->d_invm_sqrt : nullptr,

@@ -601,6 +601,12 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
   P.fx = tables_fx(tab, h->dim, h->k);
   P.fx_mode = -1;
+  P.fx_timed = 0;
+  for (auto& ev : P.fx_ev)
+    if (ev) {
+      cudaEventDestroy(ev);
+      ev = nullptr;
+    }
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
   P.valid = true;
@@ -1130,7 +1136,11 @@ void ppf_destroy(ppf_handle h) {
     cudaFree(F.dvals);
   }
   for (auto& B : h->blocks) {
-    for (auto& P : B.plan) cudaFree(P.d_tables);
+    for (auto& P : B.plan) {
+      cudaFree(P.d_tables);
+      for (auto& ev : P.fx_ev)
+        if (ev) cudaEventDestroy(ev);
+    }
     free_linear(B.lin);
   }
   free_adjoint(h->adj);
