@@ -459,8 +459,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
-        for f in (0, 1):  # inputs of this step: old c and old mu
-            rc = lib.ppf_upload_state(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0)
+        for f in (0, 1):  # inputs of this step: old c and old mu (queued; the solve reads them)
+            rc = lib.ppf_upload_state_async(p.h, f, 1, C.cast(pin[f].data_ptr(), C.POINTER(C.c_double)), 0)
             assert rc == 0
         p.solve(inc)  # results of this step land in pin[2], pin[3]
         inc += 1

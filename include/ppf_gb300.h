@@ -172,6 +172,12 @@ int ppf_invm(ppf_handle h, double* out);
 
 /* Field state I/O (GroupSolutionHandler current/old vectors). age 0 = current, 1..4 = old_k. */
 int ppf_upload_state(ppf_handle h, int field, int age, const double* host, int ordering);
+
+/* ppf_upload_state without the wait: the copy is queued on the handle's stream (so the next
+ * solve reads it) and the call returns at once; `host` must stay unchanged until a call that
+ * waits for the stream (ppf_run, ppf_solve_block, a download) returned. Lattice (= native)
+ * order, uniform meshes. Engine-side addition for callers overlapping host work with copies. */
+int ppf_upload_state_async(ppf_handle h, int f, int age, const double* host, int ordering);
 int ppf_download_state(ppf_handle h, int field, int age, double* host, int ordering);
 
 /* Apply the constraints of field f to its current vector (AffineConstraints::distribute,

@@ -1219,6 +1219,17 @@ int ppf_upload_state(ppf_handle h, int f, int age, const double* host, int order
   return permute_io(h, f, const_cast<double*>(host), nullptr, p, ordering, true);
 }
 
+int ppf_upload_state_async(ppf_handle h, int f, int age, const double* host, int ordering) {
+  if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "asynchronous uploads on an adaptive mesh (use ppf_upload_state)");
+  if (ordering != PPF_ORDER_LATTICE && ordering != PPF_ORDER_NATIVE)
+    return fail(h, PPF_ERR_UNSUPPORTED, "asynchronous uploads are in lattice order");
+  double* p = state_ptr(h, f, age);
+  if (!p) return fail(h, PPF_ERR_ARG, "age not stored for this field");
+  PPF_CUDA(h, cudaMemcpyAsync(p, host, sizeof(double) * h->fields[f].len, cudaMemcpyHostToDevice, h->stream));
+  return PPF_OK;
+}
+
 int ppf_download_state(ppf_handle h, int f, int age, double* host, int ordering) {
   if (!h || !host || f < 0 || f >= (int)h->fields.size()) return PPF_ERR_ARG;
   double* p = state_ptr(h, f, age);

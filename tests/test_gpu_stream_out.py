@@ -57,3 +57,25 @@ def test_streamed_output_arguments(gpu_lib):
     rc = p.lib.ppf_set_output_stream(p.h, 0, capi.dptr(buf), capi.ORDER_DEALII)
     assert rc == capi.PPF_ERR_UNSUPPORTED
     assert p.lib.ppf_set_output_stream(p.h, 7, None, capi.ORDER_LATTICE) == capi.PPF_ERR_ARG
+
+
+def test_async_upload_is_read_by_the_next_solve(gpu_lib):
+    """ppf_upload_state_async queues the copy on the handle's stream: the increment after it
+    sees the uploaded state as after ppf_upload_state."""
+    import torch
+    outs = []
+    for use_async in (False, True):
+        wl = W.cahn_hilliard_3d(refine=2, degree=2, dim=3, size=8.0, dt=1e-4)
+        p = wl.make_problem()
+        p.solve(0)
+        rng = np.random.default_rng(4)
+        host = torch.from_numpy(0.5 + 0.05 * rng.uniform(-1, 1, p.field_length(0))).pin_memory()
+        ptr = capi.dptr(host.numpy())
+        if use_async:
+            assert p.lib.ppf_upload_state_async(p.h, 0, 1, ptr, capi.ORDER_LATTICE) == 0
+        else:
+            assert p.lib.ppf_upload_state(p.h, 0, 1, ptr, capi.ORDER_LATTICE) == 0
+        p.solve(1)
+        outs.append(p.download_solution(0))
+    # the scatter's FP64 atomics may add in another order from run to run
+    assert np.linalg.norm(outs[0] - outs[1]) <= 1e-13 * np.linalg.norm(outs[0])
