@@ -155,3 +155,20 @@ def test_modes_outside_the_fixed_point_path(gpu_lib):
     p.upload(0, wl.initial[0], age=1)
     p.apply(0, 0, None, scale=1)
     assert p.contraction_mode(0, 0) in (1, 2, 3)  # chosen by timing the modes on the first launch
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_nonfinite_value_reports_nan_in_every_mode(gpu_lib, mode):
+    """A NaN in a gradient row gives its cell block exponent 2047: the cell's derivatives (and
+    integer integration) return NaN and the finalize kernel reports PPF_ERR_NAN."""
+    from phasefield_gb300 import capi
+    wl = W.cahn_hilliard_3d(refine=2, degree=2, dim=3, size=8.0, dt=1e-4)
+    with env(PPF_CONTRACTION_MODE=mode):
+        p = wl.make_problem()
+        p.solve(0)
+        mu = p.download(1, age=1)
+        mu[len(mu) // 2] = np.nan
+        p.upload(1, mu, age=1)
+        with pytest.raises(capi.PPFError) as e:
+            p.solve(1)
+        assert e.value.code == capi.PPF_ERR_NAN
