@@ -22,6 +22,11 @@
 //   * MODE_DIAG replaces the SRC dependency of each block field by unit probes on one cell
 //     node at a time (identity in every component, as the reference submits
 //     identity<Rank>()) and keeps the integrated entry at the probed node.
+//   * FP64 Q1/Q2 launches contract exactly in 64-bit integers (prismspf/gpu/fixed_point.cuh):
+//     rows read as gradients get a fixed-point copy with a per-cell block exponent, the
+//     derivatives are integer line sums rounded once, and with fx_int the submitted gradient
+//     terms are integrated the same way (else in FP64 with jdt); the launch record selects the
+//     split, which the engine times per operator.
 // `number` is the arithmetic type (double for the drop-in, float for mixed-precision
 // multigrid smoothing).
 #pragma once
