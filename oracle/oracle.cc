@@ -1535,16 +1535,36 @@ static int block_krylov(Problem& P, Block& B, const std::vector<double>& b, std:
     // BiCGStab (van der Vorst), right-preconditioned, with the half-step convergence check
     std::vector<double> rbar = r, p(n, 0.0), v(n, 0.0), y(n), s(n), zz(n), t(n);
     double rho = 1.0, alpha = 1.0, omega = 1.0;
+    int restarts = 0;
+    // a breakdown (rho or omega zero, or |alpha| > 1e10) restarts from the current iterate with
+    // the exact residual, as deal.II's SolverBicgstab (solver_bicgstab.h, iterate/solve) does;
+    // at most 10 restarts
+    auto restart = [&]() {
+      A(x, q);
+      for (size_t i = 0; i < n; ++i) r[i] = b[i] - q[i];
+      rbar = r;
+      std::fill(p.begin(), p.end(), 0.0);
+      std::fill(v.begin(), v.end(), 0.0);
+      rho = alpha = omega = 1.0;
+    };
     while (it < B.lin.max_its) {
       const double rho_new = dotp(rbar, r);
-      if (rho_new == 0.0 || omega == 0.0) break;  // breakdown
+      if (rho_new == 0.0 || omega == 0.0) {  // breakdown
+        if (++restarts > 10) break;
+        restart();
+        continue;
+      }
       const double beta = (rho_new / rho) * (alpha / omega);
       rho = rho_new;
       for (size_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
       M(p, y);
       A(y, v);
       const double sigma = dotp(rbar, v);
-      if (sigma == 0.0) break;
+      if (sigma == 0.0 || !(std::fabs(rho / sigma) <= 1e10)) {  // breakdown
+        if (++restarts > 10) break;
+        restart();
+        continue;
+      }
       alpha = rho / sigma;
       for (size_t i = 0; i < n; ++i) s[i] = r[i] - alpha * v[i];
       ++it;

@@ -1264,10 +1264,27 @@ static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, doubl
     PPF_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * n, h->stream));
     PPF_CUDA(h, cudaMemsetAsync(vv, 0, sizeof(double) * n, h->stream));
     double rho = 1.0, alpha = 1.0, omega = 1.0;
+    int restarts = 0;
+    // a breakdown (rho or omega zero, or |alpha| > 1e10) restarts from the current iterate with
+    // the exact residual, as deal.II's SolverBicgstab does (at most 10 times)
+    auto restart = [&]() -> int {
+      if ((rc = A(x, q))) return rc;
+      PPF_CUDA(h, cudaMemcpyAsync(r, rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+      axpby(h, 0, n, -1.0, q, 1.0, r);
+      PPF_CUDA(h, cudaMemcpyAsync(rbar, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+      PPF_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * n, h->stream));
+      PPF_CUDA(h, cudaMemsetAsync(vv, 0, sizeof(double) * n, h->stream));
+      rho = alpha = omega = 1.0;
+      return PPF_OK;
+    };
     while (it < L.params.max_iterations) {
       double rho_new;
       if ((rc = dot(h, L, 0, n, rbar, r, &rho_new))) return rc;
-      if (rho_new == 0.0 || omega == 0.0) break;  // breakdown
+      if (rho_new == 0.0 || omega == 0.0) {  // breakdown
+        if (++restarts > 10) break;
+        if ((rc = restart())) return rc;
+        continue;
+      }
       const double beta = (rho_new / rho) * (alpha / omega);
       rho = rho_new;
       axpby(h, 0, n, -omega, vv, 1.0, p);  // p = p - omega v
@@ -1276,7 +1293,11 @@ static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, doubl
       if ((rc = A(y, vv))) return rc;
       double sigma;
       if ((rc = dot(h, L, 0, n, rbar, vv, &sigma))) return rc;
-      if (sigma == 0.0) break;
+      if (sigma == 0.0 || !(std::fabs(rho / sigma) <= 1e10)) {  // breakdown
+        if (++restarts > 10) break;
+        if ((rc = restart())) return rc;
+        continue;
+      }
       alpha = rho / sigma;
       PPF_CUDA(h, cudaMemcpyAsync(sv, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
       axpby(h, 0, n, -alpha, vv, 1.0, sv);  // s = r - alpha v
