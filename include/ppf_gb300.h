@@ -452,10 +452,19 @@ int ppf_device_fp64_peak(double* tflops);
  * static device array that every GPU loading this library holds until exit. All calls share
  * it: each call clears what must start at zero, and calls whose GPU work overlaps race, so
  * issue them on one stream. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture. Non-finite
- * results are not reported by this entry point. */
+ * (cudaGetSymbolAddress) and the device's SM count; make that first call before any stream
+ * capture. The step returns before its GPU work ends, so it cannot report a non-finite
+ * result itself: ppf_allen_cahn_step_noalloc_status does. */
 int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_well, double kappa, double dt,
                                 const double* d_n_old, double* d_n_new, void* stream);
+
+/* Status of the last ppf_allen_cahn_step_noalloc on the current device (no counterpart in the
+ * reference; the companion of the allocation-free step, and like it allocates nothing): waits
+ * for `stream` (the step's stream, NULL = default stream), reads the step's error word from the
+ * static scratch array into a host int and returns PPF_ERR_NAN when the step produced a
+ * non-finite value (the reference's NaN exit status, problem.cc:455-469), else PPF_OK. A later
+ * step overwrites the word; call this before the next step is issued. */
+int ppf_allen_cahn_step_noalloc_status(void* stream);
 
 #ifdef __cplusplus
 }

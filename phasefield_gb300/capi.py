@@ -38,7 +38,7 @@ EXPORTED = [
     "ppf_apply_constraints", "ppf_run", "ppf_solve_block", "ppf_apply", "ppf_apply_device",
     "ppf_set_time", "ppf_get_time", "ppf_set_use_graph", "ppf_state_device_ptr", "ppf_synchronize",
     "ppf_set_stream", "ppf_kernel_timing", "ppf_kernel_stats", "ppf_kernel_stats_reset", "ppf_contraction_mode", "ppf_set_output_stream", "ppf_upload_state_async",
-    "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc",
+    "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc", "ppf_allen_cahn_step_noalloc_status",
     "ppf_default_linear_params", "ppf_set_linear_params", "ppf_linear_solve", "ppf_lhs_diagonal",
     "ppf_set_newton_params", "ppf_newton_solve", "ppf_linear_stats", "ppf_increment_block", "ppf_end_increment",
     # ensembles (bound in phasefield_gb300/ensemble.py)
@@ -160,6 +160,7 @@ def load() -> C.CDLL:
     lib.ppf_device_fp64_peak.argtypes = [dp]
     lib.ppf_allen_cahn_step_noalloc.argtypes = [P(MeshDesc), C.c_double, C.c_double, C.c_double, C.c_void_p,
                                                 C.c_void_p, C.c_void_p]
+    lib.ppf_allen_cahn_step_noalloc_status.argtypes = [C.c_void_p]
     lib.ppf_default_linear_params.argtypes = [P(LinearParams)]
     lib.ppf_set_linear_params.argtypes = [H, C.c_int, P(LinearParams)]
     lib.ppf_linear_solve.argtypes = [H, C.c_int, P(C.c_int), dp]

@@ -21,8 +21,13 @@
 // serialise them, e.g. by issuing them on one stream.
 //
 // Set-up: the first call on a device, with that device current, looks up the device address
-// of the array with cudaGetSymbolAddress and caches it per device. Make that first call
-// before any stream capture begins.
+// of the array with cudaGetSymbolAddress and the device's SM count, and caches both per
+// device. Make that first call before any stream capture begins.
+//
+// Status: the finalize kernel sets a non-finite flag in the array's error word; the step
+// itself returns before its GPU work ends and so cannot report it.
+// ppf_allen_cahn_step_noalloc_status waits for a stream and reads that word (a copy into a
+// host int of the caller's stack, no allocation).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,8 +47,25 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 
-// device address of g_noalloc_scratch per device (host-side cache)
+constexpr size_t NOALLOC_ERR_OFFSET = NOALLOC_ACC_BYTES + NOALLOC_TABLE_BYTES;
+
+// device address of g_noalloc_scratch and the SM count, per device (host-side cache)
 static unsigned char* g_scratch_addr[NOALLOC_MAX_DEVICES] = {};
+static int g_sm_count[NOALLOC_MAX_DEVICES] = {};
+
+// the cell tables travel as a kernel argument (kernel parameters of up to 32 KB are
+// available from CUDA 12.1 on), so the call stages them without a host-to-device copy
+template <size_t B>
+struct alignas(16) TableBlob {
+  unsigned char b[B];
+};
+
+template <size_t B>
+__global__ void noalloc_stage_tables_kernel(const __grid_constant__ TableBlob<B> blob, unsigned char* dst,
+                                            int* err) {
+  for (int i = threadIdx.x; i < (int)B; i += blockDim.x) dst[i] = blob.b[i];
+  if (threadIdx.x == 0) *err = 0;
+}
 
 int noalloc_fail(int code, const char* msg) {
   std::fprintf(stderr, "ppf_allen_cahn_step_noalloc: %s\n", msg);
@@ -67,12 +89,16 @@ void gl_closed_form(int n, double* x, double* w) {
   }
 }
 
+// Builds the cell tables of block 1 and launches the kernel that writes them (and clears the
+// error word) into the scratch array; returns false when that launch fails.
 template <int dim, int degree>
-size_t fill_tables(const ppf_mesh_desc& m, const double* h, unsigned char* out) {
+bool stage_tables(const ppf_mesh_desc& m, const double* h, unsigned char* d_tables, int* d_err, cudaStream_t s) {
   using Tab = pg::CellTables<dim, degree>;
   static_assert(sizeof(Tab) <= NOALLOC_TABLE_BYTES, "cell tables exceed the scratch table region");
+  static_assert(sizeof(Tab) <= 32000, "cell tables exceed the kernel-parameter limit");
   constexpr int n = degree + 1, nq = Tab::nq;
-  Tab& t = *reinterpret_cast<Tab*>(out);
+  TableBlob<sizeof(Tab)> blob;
+  Tab& t = *reinterpret_cast<Tab*>(blob.b);
   std::memset(&t, 0, sizeof(Tab));
   double x[5], w[5], D[5][5], bw[5];
   gl_closed_form(n, x, w);
@@ -132,20 +158,22 @@ size_t fill_tables(const ppf_mesh_desc& m, const double* h, unsigned char* out) 
   t.slot_comp0[0] = 0;
   t.out_of[0] = 0;
   t.out_row0[0] = 0;
-  return sizeof(Tab);
+  noalloc_stage_tables_kernel<sizeof(Tab)><<<1, 256, 0, s>>>(blob, d_tables, d_err);
+  return cudaGetLastError() == cudaSuccess;
 }
 
-size_t fill_tables_dispatch(int dim, int degree, const ppf_mesh_desc& m, const double* h, unsigned char* out) {
+bool stage_tables_dispatch(int dim, int degree, const ppf_mesh_desc& m, const double* h, unsigned char* d_tables,
+                           int* d_err, cudaStream_t s) {
   switch (dim * 10 + degree) {
-    case 21: return fill_tables<2, 1>(m, h, out);
-    case 22: return fill_tables<2, 2>(m, h, out);
-    case 23: return fill_tables<2, 3>(m, h, out);
-    case 24: return fill_tables<2, 4>(m, h, out);
-    case 31: return fill_tables<3, 1>(m, h, out);
-    case 32: return fill_tables<3, 2>(m, h, out);
-    case 33: return fill_tables<3, 3>(m, h, out);
-    case 34: return fill_tables<3, 4>(m, h, out);
-    default: return 0;
+    case 21: return stage_tables<2, 1>(m, h, d_tables, d_err, s);
+    case 22: return stage_tables<2, 2>(m, h, d_tables, d_err, s);
+    case 23: return stage_tables<2, 3>(m, h, d_tables, d_err, s);
+    case 24: return stage_tables<2, 4>(m, h, d_tables, d_err, s);
+    case 31: return stage_tables<3, 1>(m, h, d_tables, d_err, s);
+    case 32: return stage_tables<3, 2>(m, h, d_tables, d_err, s);
+    case 33: return stage_tables<3, 3>(m, h, d_tables, d_err, s);
+    case 34: return stage_tables<3, 4>(m, h, d_tables, d_err, s);
+    default: return false;
   }
 }
 
@@ -191,8 +219,9 @@ extern "C" int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_w
                                            const double* d_n_old, double* d_n_new, void* stream) {
   if (!mesh || !d_n_old || !d_n_new) return noalloc_fail(PPF_ERR_ARG, "null argument");
   const int dim = mesh->dim, degree = mesh->degree;
-  if (dim < 2 || dim > 3 || degree < 1 || degree > 4 || mesh->global_refinement < 0)
-    return noalloc_fail(PPF_ERR_ARG, "mesh: dim must be 2 or 3, degree 1..4");
+  if (dim < 2 || dim > 3 || degree < 1 || degree > 4 || mesh->global_refinement < 0 ||
+      mesh->global_refinement > 30)
+    return noalloc_fail(PPF_ERR_ARG, "mesh: dim must be 2 or 3, degree 1..4, global refinement 0..30");
   for (int d = 0; d < dim; ++d) {
     if (mesh->periodic[d])
       return noalloc_fail(PPF_ERR_UNSUPPORTED, "allocation-free step: natural boundary conditions only");
@@ -202,11 +231,17 @@ extern "C" int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_w
   double h[3] = {1, 1, 1};
   long long N = 1, ncells = 1;
   for (int d = 0; d < dim; ++d) {
-    nc[d] = mesh->subdivisions[d] << mesh->global_refinement;
+    // counts in 64 bits: a large refinement must not wrap to a small mesh that passes the limit
+    const long long cells = (long long)mesh->subdivisions[d] << mesh->global_refinement;
+    if (cells > NOALLOC_MAX_NODES)
+      return noalloc_fail(PPF_ERR_UNSUPPORTED,
+                          "allocation-free step: mesh exceeds the 1048576-node limit of the static scratch array");
+    nc[d] = (int)cells;
     nn[d] = degree * nc[d] + 1;
     h[d] = mesh->size[d] / nc[d];
     N *= nn[d];
     ncells *= nc[d];
+    if (N > NOALLOC_MAX_NODES) break;
   }
   if (N > NOALLOC_MAX_NODES)
     return noalloc_fail(PPF_ERR_UNSUPPORTED,
@@ -222,23 +257,24 @@ extern "C" int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_w
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) return noalloc_fail(PPF_ERR_CUDA, "cudaGetSymbolAddress failed for the scratch array");
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+      return noalloc_fail(PPF_ERR_CUDA, "cudaDeviceGetAttribute failed for the SM count");
+    g_sm_count[dev] = sms;
     g_scratch_addr[dev] = static_cast<unsigned char*>(p);
   }
   unsigned char* base = g_scratch_addr[dev];
   double* acc = reinterpret_cast<double*>(base);
   unsigned char* d_tables = base + NOALLOC_ACC_BYTES;
-  int* d_err = reinterpret_cast<int*>(base + NOALLOC_ACC_BYTES + NOALLOC_TABLE_BYTES);
+  int* d_err = reinterpret_cast<int*>(base + NOALLOC_ERR_OFFSET);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
-  alignas(16) unsigned char tables[NOALLOC_TABLE_BYTES];
-  const size_t tab_bytes = fill_tables_dispatch(dim, degree, *mesh, h, tables);
-  if (!tab_bytes) return noalloc_fail(PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
   AllenCahn<2, 1, double> pde{m_well, kappa};  // same layout for every dim/degree
-
-  if (cudaMemcpyAsync(d_tables, tables, tab_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      cudaMemsetAsync(acc, 0, sizeof(double) * N, s) != cudaSuccess ||
-      cudaMemsetAsync(d_err, 0, sizeof(int), s) != cudaSuccess)
-    return noalloc_fail(PPF_ERR_CUDA, "staging the scratch array failed");
+  // tables and the cleared error word, then the cleared accumulator
+  if (!stage_tables_dispatch(dim, degree, *mesh, h, d_tables, d_err, s))
+    return noalloc_fail(PPF_ERR_CUDA, "staging the cell tables failed");
+  if (cudaMemsetAsync(acc, 0, sizeof(double) * N, s) != cudaSuccess)
+    return noalloc_fail(PPF_ERR_CUDA, "clearing the accumulator failed");
 
   CellLaunch L;
   std::memset(&L, 0, sizeof(L));
@@ -273,8 +309,22 @@ extern "C" int ppf_allen_cahn_step_noalloc(const ppf_mesh_desc* mesh, double m_w
     lm.h[d] = h[d];
   }
   long long grid = (N + 255) / 256;
-  if (grid > 152 * 16) grid = 152 * 16;
+  if (grid > (long long)g_sm_count[dev] * 16) grid = (long long)g_sm_count[dev] * 16;
   noalloc_finalize_kernel<<<(unsigned)grid, 256, 0, s>>>(d_n_new, acc, nn[0], nn[1], N, lm, dim, d_err);
   if (cudaGetLastError() != cudaSuccess) return noalloc_fail(PPF_ERR_CUDA, "finalize kernel launch failed");
   return PPF_OK;
+}
+
+extern "C" int ppf_allen_cahn_step_noalloc_status(void* stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+    return noalloc_fail(PPF_ERR_CUDA, "no usable current CUDA device");
+  if (!g_scratch_addr[dev]) return PPF_OK;  // no step has run on this device
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int flags = 0;
+  if (cudaStreamSynchronize(s) != cudaSuccess ||
+      cudaMemcpyFromSymbol(&flags, g_noalloc_scratch, sizeof(int), NOALLOC_ERR_OFFSET, cudaMemcpyDeviceToHost) !=
+          cudaSuccess)
+    return noalloc_fail(PPF_ERR_CUDA, "reading the error word failed");
+  return (flags & pg::ERR_NONFINITE) ? PPF_ERR_NAN : PPF_OK;
 }
