@@ -225,9 +225,16 @@ template <class PDE, int dim, int degree, int mode, typename number>
 cudaError_t launch_amr_cell_kernel(const AmrCellLaunch& A, const void* obj, size_t smem, cudaStream_t s) {
   using S = CellShape<dim, degree>;
   auto kern = amr_cell_kernel<PDE, dim, degree, mode, number>;
-  static size_t attr_smem = 0;
-  static int occ = 0;
-  static int sms = 0;
+  // the shared-memory opt-in and the occupancy hold per device: cached per device ordinal
+  constexpr int MAX_DEVICES = 64;
+  static size_t attr_smem_of[MAX_DEVICES] = {};
+  static int occ_of[MAX_DEVICES] = {};
+  static int sms_of[MAX_DEVICES] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  size_t& attr_smem = attr_smem_of[dev];
+  int& occ = occ_of[dev];
+  int& sms = sms_of[dev];
   if (smem > attr_smem) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -235,10 +242,9 @@ cudaError_t launch_amr_cell_kernel(const AmrCellLaunch& A, const void* obj, size
     occ = 0;
   }
   if (occ == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }

@@ -1539,19 +1539,21 @@ static int block_krylov(Problem& P, Block& B, const std::vector<double>& b, std:
     // a breakdown (rho or omega zero, or |alpha| > 1e10) restarts from the current iterate with
     // the exact residual, as deal.II's SolverBicgstab (solver_bicgstab.h, iterate/solve) does;
     // at most 10 restarts
-    auto restart = [&]() {
+    auto restart = [&]() -> bool {
       A(x, q);
       for (size_t i = 0; i < n; ++i) r[i] = b[i] - q[i];
       rbar = r;
       std::fill(p.begin(), p.end(), 0.0);
       std::fill(v.begin(), v.end(), 0.0);
       rho = alpha = omega = 1.0;
+      res = std::sqrt(dotp(r, r));  // a breakdown right at convergence ends the solve
+      return res < tol;
     };
     while (it < B.lin.max_its) {
       const double rho_new = dotp(rbar, r);
       if (rho_new == 0.0 || omega == 0.0) {  // breakdown
         if (++restarts > 10) break;
-        restart();
+        if (restart()) { *conv = true; break; }
         continue;
       }
       const double beta = (rho_new / rho) * (alpha / omega);
@@ -1562,7 +1564,7 @@ static int block_krylov(Problem& P, Block& B, const std::vector<double>& b, std:
       const double sigma = dotp(rbar, v);
       if (sigma == 0.0 || !(std::fabs(rho / sigma) <= 1e10)) {  // breakdown
         if (++restarts > 10) break;
-        restart();
+        if (restart()) { *conv = true; break; }
         continue;
       }
       alpha = rho / sigma;

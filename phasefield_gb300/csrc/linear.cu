@@ -1275,7 +1275,12 @@ static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, doubl
       PPF_CUDA(h, cudaMemsetAsync(p, 0, sizeof(double) * n, h->stream));
       PPF_CUDA(h, cudaMemsetAsync(vv, 0, sizeof(double) * n, h->stream));
       rho = alpha = omega = 1.0;
-      return PPF_OK;
+      return dot(h, L, 0, n, r, r, &rr);
+    };
+    // a breakdown right at convergence: the exact residual of the restart meets the tolerance
+    auto restarted_converged = [&]() -> bool {
+      res = std::sqrt(rr);
+      return res < tol;
     };
     while (it < L.params.max_iterations) {
       double rho_new;
@@ -1283,6 +1288,7 @@ static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, doubl
       if (rho_new == 0.0 || omega == 0.0) {  // breakdown
         if (++restarts > 10) break;
         if ((rc = restart())) return rc;
+        if (restarted_converged()) { *conv = true; break; }
         continue;
       }
       const double beta = (rho_new / rho) * (alpha / omega);
@@ -1296,6 +1302,7 @@ static int block_krylov(ppf_handle h, int b, const double* rhs, double* x, doubl
       if (sigma == 0.0 || !(std::fabs(rho / sigma) <= 1e10)) {  // breakdown
         if (++restarts > 10) break;
         if ((rc = restart())) return rc;
+        if (restarted_converged()) { *conv = true; break; }
         continue;
       }
       alpha = rho / sigma;

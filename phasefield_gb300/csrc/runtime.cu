@@ -953,8 +953,13 @@ static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, 
   h->N = 1;
   for (int d = 0; d < 3; ++d) {
     if (d < h->dim) {
-      if (mesh->subdivisions[d] < 1 || mesh->size[d] <= 0 || mesh->global_refinement < 0) return PPF_ERR_ARG;
-      h->nc[d] = mesh->subdivisions[d] << mesh->global_refinement;
+      if (mesh->subdivisions[d] < 1 || mesh->size[d] <= 0 || mesh->global_refinement < 0 ||
+          mesh->global_refinement > 30)
+        return PPF_ERR_ARG;
+      // cell counts in 64 bits: a large refinement must not wrap to a small mesh
+      const long long cells = (long long)mesh->subdivisions[d] << mesh->global_refinement;
+      if (cells * h->k + 1 >= (1LL << 31)) return PPF_ERR_UNSUPPORTED;
+      h->nc[d] = (int)cells;
       h->nn[d] = h->k * h->nc[d] + 1;
       h->h[d] = mesh->size[d] / h->nc[d];
     } else {
@@ -964,8 +969,8 @@ static int create_impl(const ppf_mesh_desc* mesh, const ppf_field_desc* fields, 
     }
     h->ncells *= h->nc[d];
     h->N *= h->nn[d];
+    if (h->N * 3 >= (1LL << 31)) return PPF_ERR_UNSUPPORTED;  // int32 constraint maps
   }
-  if (h->N * 3 >= (1LL << 31)) return PPF_ERR_UNSUPPORTED;  // int32 constraint maps
   h->dt = dt;
   h->timer = prismspf::SimulationTimer(dt, 0.0);
   if (custom) {
