@@ -13,8 +13,9 @@ engine's stream, L2 flushed between steps). `e2e` is the same metric through the
 ABI with the step's inputs uploaded from pinned host memory and its result downloaded every
 step. `--impl reference` times the CPU restatement of the reference algorithm (the oracle;
 the reference itself needs deal.II/MPI/p4est, which neither machine has) on all host cores.
-Under torchrun each rank runs an independent replica (replicas only: an explicit step of
-one simulation is not sharded); rank 0 prints one JSON line.
+Under torchrun (or with --sharded) one simulation is sharded over the ranks: z-slabs of
+64^3 cells per rank stacked along z (weak scaling), halo node planes exchanged after every
+block (phasefield_gb300/sharding.py); rank 0 prints one JSON line.
 """
 from __future__ import annotations
 

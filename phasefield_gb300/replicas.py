@@ -1,8 +1,9 @@
-"""Independent replicas across ranks (one process per GPU).
+"""Independent work across ranks (one process per GPU): ensemble slices and whole-simulation
+replicas.
 
-An explicit step of one simulation is not sharded in this build: ranks run independent
-simulations (or ensemble slices) and only their timings and work counts are combined. The
-job-wide rate is the total work of all ranks over the slowest rank's time.
+Ranks that run independent simulations (or slices of an ensemble, split by instance) combine
+only their timings and work counts: the job-wide rate is the total work of all ranks over the
+slowest rank's time. One simulation sharded over ranks is phasefield_gb300/sharding.py.
 """
 from __future__ import annotations
 

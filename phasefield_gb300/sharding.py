@@ -187,33 +187,6 @@ class EngineLocal:
         return self.p.download(f, age=age)
 
 
-class OracleLocal:
-    """The oracle on one rank's slab (test infrastructure for the CPU tests of this module)."""
-
-    device = "cpu"
-
-    def __init__(self, oracle):
-        import torch
-        self.o = oracle
-        self.torch = torch
-
-    def vector(self, f: int):
-        return self.torch.from_numpy(self.o.get(f, 0).copy())
-
-    def commit(self, f: int, v):
-        self.o.set(f, v.numpy(), 0)
-
-    def increment_block(self, b: int, is_output: bool):
-        rc = self.o.increment_block(b, is_output)
-        if rc:
-            raise RuntimeError(f"oracle block {b}: status {rc}")
-
-    def end_increment(self) -> bool:
-        return self.o.end_increment() == 2
-
-    def get(self, f: int, age: int) -> np.ndarray:
-        return self.o.get(f, age)
-
 
 # ---------------------------------------------------------------------------------------------
 # halo exchange and the increment loop

@@ -6,6 +6,7 @@ reference (include/prismspf/core/dependencies.h:134-213).
 Compile-only on this machine: nvcc cross-compiles the device code without a GPU.
 """
 import json
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -15,7 +16,8 @@ import pytest
 ROOT = Path(__file__).resolve().parents[1]
 INCLUDE = ROOT / "include"
 EXAMPLES = ROOT / "examples"
-REF_APPS = Path("/root/reference/applications")
+# the reference tree (read only by these CPU checks); PPF_REFERENCE_ROOT points elsewhere
+REF_APPS = Path(os.environ.get("PPF_REFERENCE_ROOT", "/root/reference")) / "applications"
 GXX = shutil.which("g++")
 NVCC = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if Path("/usr/local/cuda/bin/nvcc").exists() else None)
 

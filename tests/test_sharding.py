@@ -18,6 +18,34 @@ def rel_l2(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+class OracleLocal:
+    """The oracle on one rank's slab (the local engine of these CPU tests)."""
+
+    device = "cpu"
+
+    def __init__(self, oracle):
+        import torch
+        self.o = oracle
+        self.torch = torch
+
+    def vector(self, f: int):
+        return self.torch.from_numpy(self.o.get(f, 0).copy())
+
+    def commit(self, f: int, v):
+        self.o.set(f, v.numpy(), 0)
+
+    def increment_block(self, b: int, is_output: bool):
+        rc = self.o.increment_block(b, is_output)
+        if rc:
+            raise RuntimeError(f"oracle block {b}: status {rc}")
+
+    def end_increment(self) -> bool:
+        return self.o.end_increment() == 2
+
+    def get(self, f: int, age: int) -> np.ndarray:
+        return self.o.get(f, age)
+
+
 def _ch(periodic=True):
     wl = W.cahn_hilliard_3d(refine=3, degree=2, dim=2, size=8.0, dt=2e-5, periodic=periodic)
     if periodic:  # a periodic initial condition along the split axis (images = masters)
@@ -70,7 +98,7 @@ def _run_sharded(wl, rank, size, n, every, dist_=None):
     o = po.Oracle(S.local_workload(wl, slab))
     for f, v in S.local_workload(wl, slab).initial.items():
         o.set(f, v, 0)
-    run = S.ShardedExplicit(slab, S.OracleLocal(o), wl.fields, wl.blocks, dist_)
+    run = S.ShardedExplicit(slab, OracleLocal(o), wl.fields, wl.blocks, dist_)
     run.run(n, every)
     return slab, run
 
