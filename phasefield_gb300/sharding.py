@@ -12,8 +12,17 @@ component and travels without packing. The exchange is the only collective of th
 (NCCL on GPUs, gloo on CPUs), plus one logical-or of the non-finite flags per increment, as
 `Problem::solve_increment` does (problem.cc:459-477).
 
-Scope: explicit, constant and post-processing blocks (the explicit increment loop). Linear and
-Newton blocks need distributed inner products and are rejected.
+Linear blocks (ShardedLinear): deal.II's SolverCG as LinearSolver::do_linear_solve runs it
+(linear_solver.h:348-402), with every vector sharded like the fields. The operator apply of a
+rank is complete on the rows it owns (its ghost cells contribute locally), so an apply needs
+only the ghost planes of its input, refreshed by the same halo exchange; inner products sum
+the owned rows of every rank and meet in one all-reduce of a float64 scalar
+(linear_solver.h:357-379 reduces them over MPI the same way). No preconditioner: the
+multigrid hierarchy and the Chebyshev eigenvalue estimate stay per GPU.
+
+Scope: explicit, constant and post-processing blocks (the explicit increment loop), and single-
+field Linear blocks with homogeneous Dirichlet values through ShardedLinear. Newton blocks are
+rejected.
 """
 from __future__ import annotations
 
@@ -186,6 +195,22 @@ class EngineLocal:
     def get(self, f: int, age: int) -> np.ndarray:
         return self.p.download(f, age=age)
 
+    def zeros(self, n: int):
+        return self.torch.zeros(n, dtype=self.torch.float64, device="cuda")
+
+    def apply(self, b: int, which: int, src, scale: int):
+        """S op(src) of block b on device vectors (which 0: compute_rhs, 1: compute_lhs with
+        src read through the homogeneous constraints); rows this rank owns are complete."""
+        n = sum(self.p.field_length(f) for f in self.p.blocks[b].field_indices)
+        dst = self.torch.empty(n, dtype=self.torch.float64, device="cuda")
+        sp = ctypes.c_void_p(src.data_ptr()) if src is not None else None
+        self.p._check(self.p.lib.ppf_apply_device(self.p.h, b, which, sp, ctypes.c_void_p(dst.data_ptr()), scale))
+        return dst
+
+    def set_current(self, f: int, v):
+        self.p.device_view(f, 0).copy_(v)
+        self.p.apply_constraints(f)
+
 
 
 # ---------------------------------------------------------------------------------------------
@@ -294,10 +319,14 @@ class ShardedExplicit:
 
     def owned(self, f: int, age: int) -> np.ndarray:
         """This rank's owned planes of field f (all components, component-major)."""
-        v = self.local.get(f, age)
-        n, P = self.slab.n_nodes, self.slab.plane_size
-        lo, hi = self.slab.owned_planes()
-        return np.concatenate([v[c * n + lo * P:c * n + hi * P] for c in range(self._ncomp(f))])
+        return owned_part(self.slab, self.local.get(f, age), self._ncomp(f))
+
+
+def owned_part(slab: Slab, v: np.ndarray, ncomp: int) -> np.ndarray:
+    """The owned planes of a local lattice vector (all components, component-major)."""
+    n, P = slab.n_nodes, slab.plane_size
+    lo, hi = slab.owned_planes()
+    return np.concatenate([v[c * n + lo * P:c * n + hi * P] for c in range(ncomp)])
 
 
 def assemble(slabs: list[Slab], parts: list[np.ndarray], mesh: RectangularMesh, ncomp: int = 1) -> np.ndarray:
@@ -321,9 +350,110 @@ def assemble(slabs: list[Slab], parts: list[np.ndarray], mesh: RectangularMesh, 
 
 
 def local_workload(wl, slab: Slab):
-    """A copy of a workload restricted to a rank's slab (mesh and initial condition)."""
+    """A copy of a workload restricted to a rank's slab (mesh and initial condition). A face of
+    the split axis next to a ghost cell layer is interior to the global mesh: Dirichlet
+    conditions on its boundary id are dropped there (boundary ids 2 axis and 2 axis + 1)."""
     w = copy.copy(wl)
     w.mesh = slab.mesh
     w.initial = {f: local_from_global(slab, v, 1 if wl.fields[f].field_type == 0 else wl.mesh.dim)
                  for f, v in wl.initial.items()}
+    interior = set()
+    if slab.left is not None:
+        interior.add(2 * slab.axis)
+    if slab.right is not None:
+        interior.add(2 * slab.axis + 1)
+    fields = []
+    for fa in wl.fields:
+        fa = copy.copy(fa)
+        fa.dirichlet = {key: v for key, v in fa.dirichlet.items() if key[1] not in interior}
+        fields.append(fa)
+    w.fields = fields
     return w
+
+
+class ShardedLinear:
+    """The CG solve of a single-field Linear block over all ranks: deal.II's SolverCG as
+    LinearSolver::solve_impl / do_linear_solve run it (linear_solver.h:305-402), without a
+    preconditioner, from the previous solution of the block (zero at first), to
+    ||S (b - A x)|| < tolerance x normalization (S = invM^1/2 unless AbsoluteResidual;
+    linear_solver.h:414-427). Vectors are local lattice vectors (ghost planes included); each
+    operator apply first refreshes the ghost planes of its input; inner products sum the owned
+    rows and are all-reduced. The solution becomes the field's current vector (constraints
+    distributed, ghost planes refreshed)."""
+
+    def __init__(self, slab: Slab, local, fields, blocks, global_mesh: RectangularMesh, dist=None):
+        self.slab, self.local, self.fields, self.blocks, self.dist = slab, local, fields, blocks, dist
+        self.halo = HaloExchange(slab, dist)
+        self.volume = float(np.prod([global_mesh.size[d] for d in range(global_mesh.dim)]))
+        self.x = {}
+        self.iterations = {}
+        self.residual = {}
+
+    def _ncomp(self, f: int) -> int:
+        return 1 if self.fields[f].field_type == 0 else self.slab.mesh.dim
+
+    def _owned(self, ncomp: int):
+        n, P = self.slab.n_nodes, self.slab.plane_size
+        lo, hi = self.slab.owned_planes()
+        return [(c * n + lo * P, c * n + hi * P) for c in range(ncomp)]
+
+    def dot(self, u, v, owned) -> float:
+        torch = __import__("torch")
+        s = torch.zeros(1, dtype=torch.float64, device=u.device)
+        for a, b in owned:
+            s += torch.dot(u[a:b], v[a:b])
+        if self.dist is not None and self.slab.size > 1:
+            self.dist.all_reduce(s, op=self.dist.ReduceOp.SUM)
+        return float(s.item())
+
+    def solve(self, b: int, tolerance_type: int = 0, tolerance: float = 1e-10, max_iterations: int = 1000):
+        blk = self.blocks[b]
+        if len(blk.field_indices) != 1:
+            raise ValueError("the sharded linear solve covers single-field Linear blocks")
+        f = blk.field_indices[0]
+        if any(v != 0.0 for v in self.fields[f].dirichlet.values()):
+            raise NotImplementedError("the sharded linear solve takes homogeneous Dirichlet values")
+        ncomp = self._ncomp(f)
+        owned = self._owned(ncomp)
+        scale = 0 if tolerance_type == 0 else 2
+        norm = 1.0
+        if tolerance_type in (1, 3):
+            norm *= np.sqrt(self.volume)
+        tol = tolerance * norm  # one field: sqrt(n_fields) = 1 (tolerance types 1 and 2)
+
+        def A(v):
+            self.halo.exchange(v, ncomp)
+            return self.local.apply(b, 1, v, scale)
+
+        rhs = self.local.apply(b, 0, None, scale)
+        x = self.x.get(b)
+        if x is None:
+            x = self.local.zeros(rhs.numel())
+        r = rhs - A(x)
+        res = np.sqrt(self.dot(r, r, owned))
+        it = 0
+        if res >= tol:
+            p = r.clone()
+            rz = res * res
+            while it < max_iterations:
+                q = A(p)
+                alpha = rz / self.dot(p, q, owned)
+                x += alpha * p
+                r -= alpha * q
+                it += 1
+                rr = self.dot(r, r, owned)
+                res = np.sqrt(rr)
+                if res < tol:
+                    break
+                beta = rr / rz
+                rz = rr
+                p = r + beta * p
+        self.x[b] = x
+        self.iterations[b], self.residual[b] = it, res / norm
+        self.halo.exchange(x, ncomp)
+        self.local.set_current(f, x)
+        return it, res / norm
+
+    def owned(self, f: int) -> np.ndarray:
+        """This rank's owned planes of field f's current vector."""
+        return owned_part(self.slab, self.local.get(f, 0), self._ncomp(f))

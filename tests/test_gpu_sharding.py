@@ -43,3 +43,25 @@ def test_sharded_engine_one_rank_matches_plain(gpu_lib, case):
     for f, age in fields:
         got = S.assemble([slab], [run.owned(f, age)], wl.mesh)
         assert rel_l2(got, ref.download(f, age=age)) < 1e-12, (f, age)
+
+
+@pytest.mark.parametrize("tolerance_type", [0, 1])
+def test_sharded_cg_engine_one_rank_matches_plain_cg(gpu_lib, tolerance_type):
+    """The sharded CG of the elasticity block (device vectors, halo exchange with itself, owned
+    inner products) against the engine's own CG without a preconditioner: same iteration count
+    within 2 and solutions within 1e-8."""
+    import torch
+    wl = W.eshelby_3d(refine=2, degree=2, size=16.0, n_incl=5)
+    ref = wl.make_problem()
+    b = ref.apply(0, 0, None, scale=0)
+    tol = 1e-10 * float(np.linalg.norm(b)) if tolerance_type == 0 else 1e-9
+    ref.set_linear_params(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000, preconditioner=0)
+    its_ref, _ = ref.linear_solve(0)
+    slab = S.partition(wl.mesh, 0, 1)
+    p = S.local_workload(wl, slab).make_problem()
+    run = S.ShardedLinear(slab, S.EngineLocal(p), wl.fields, wl.blocks, wl.mesh)
+    its, res = run.solve(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000)
+    torch.cuda.synchronize()
+    assert abs(its - its_ref) <= 2, (its, its_ref)
+    got = S.assemble([slab], [run.owned(0)], wl.mesh, ncomp=3)
+    assert rel_l2(got, ref.download(0)) < 1e-8

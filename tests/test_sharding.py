@@ -45,6 +45,15 @@ class OracleLocal:
     def get(self, f: int, age: int) -> np.ndarray:
         return self.o.get(f, age)
 
+    def zeros(self, n: int):
+        return self.torch.zeros(n, dtype=self.torch.float64)
+
+    def apply(self, b: int, which: int, src, scale: int):
+        return self.torch.from_numpy(self.o.apply(b, which, None if src is None else src.numpy(), scale))
+
+    def set_current(self, f: int, v):
+        self.o.set(f, v.numpy().copy(), 0)
+
 
 def _ch(periodic=True):
     wl = W.cahn_hilliard_3d(refine=3, degree=2, dim=2, size=8.0, dt=2e-5, periodic=periodic)
@@ -159,3 +168,87 @@ def test_two_gloo_ranks_match_global(which):
     for i, ref in enumerate(refs):
         got = S.assemble(slabs, [res[r][i] for r in range(world)], wl.mesh)
         assert rel_l2(got, ref) < 1e-12, i
+
+
+# ---------------------------------------------------------------------------------------------
+# the sharded CG of a Linear block
+# ---------------------------------------------------------------------------------------------
+def _elasticity():
+    # 4^3 Q2 cells of [0,16]^3, five inclusions, u = 0 on x = 0; two ranks own two z-layers each
+    return W.eshelby_3d(refine=2, degree=2, size=16.0, n_incl=5)
+
+
+LINEAR_CASES = {0: 1e-10, 1: 1e-9}  # tolerance type -> tolerance (AbsoluteResidual scaled below)
+
+
+def _linear_tolerance(wl, tolerance_type):
+    from oracle import pyoracle as po
+    if tolerance_type == 0:  # absolute: relative to the right-hand side's norm
+        return LINEAR_CASES[0] * float(np.linalg.norm(po.Oracle(wl).apply(0, 0, None, scale=0)))
+    return LINEAR_CASES[tolerance_type]
+
+
+def _run_linear(wl, rank, size, tolerance_type, dist_=None):
+    from oracle import pyoracle as po
+    slab = S.partition(wl.mesh, rank, size)
+    o = po.Oracle(S.local_workload(wl, slab))
+    run = S.ShardedLinear(slab, OracleLocal(o), wl.fields, wl.blocks, wl.mesh, dist_)
+    its, res = run.solve(0, tolerance_type=tolerance_type, tolerance=_linear_tolerance(wl, tolerance_type),
+                         max_iterations=2000)
+    return slab, its, res, run.owned(0)
+
+
+def _global_linear(wl, tolerance_type):
+    from oracle import pyoracle as po
+    o = po.Oracle(wl)
+    o.set_linear_params(0, tolerance_type=tolerance_type, tolerance=_linear_tolerance(wl, tolerance_type),
+                        max_iterations=2000, preconditioner=0)
+    rc, its, res = o.linear_solve(0)
+    assert rc == 0
+    return its, o.get(0)
+
+
+def test_local_workload_drops_dirichlet_on_interior_faces():
+    wl = _elasticity()
+    wl.fields[0].dirichlet[(2, 5)] = 0.0  # u_z = 0 on z = 16 (the split axis' upper face)
+    lows = [S.local_workload(wl, S.partition(wl.mesh, r, 2)).fields[0].dirichlet for r in range(2)]
+    assert (2, 5) not in lows[0] and (2, 5) in lows[1]  # only the top slab has the global face
+    assert all((c, 0) in d for d in lows for c in range(3))  # x = 0 is in every slab
+    assert (2, 5) in wl.fields[0].dirichlet  # the global workload is unchanged
+
+
+@pytest.mark.parametrize("tolerance_type", [0, 1])
+def test_single_rank_sharded_cg_matches_global(tolerance_type):
+    wl = _elasticity()
+    slab, its, res, part = _run_linear(wl, 0, 1, tolerance_type)
+    oits, ref = _global_linear(wl, tolerance_type)
+    assert abs(its - oits) <= 2
+    assert rel_l2(S.assemble([slab], [part], wl.mesh, ncomp=3), ref) < 1e-8
+
+
+def _linear_worker(rank, world, port, tolerance_type, results):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import datetime
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=120))
+    try:
+        _, its, res, part = _run_linear(_elasticity(), rank, world, tolerance_type, dist)
+        results[rank] = (its, res, part)
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("tolerance_type", [0, 1])
+def test_two_gloo_ranks_sharded_cg_matches_global(tolerance_type):
+    world = 2
+    with mp.Manager() as m:
+        results = m.dict()
+        mp.spawn(_linear_worker, args=(world, _free_port(), tolerance_type, results), nprocs=world, join=True)
+        res = dict(results)
+    wl = _elasticity()
+    slabs = [S.partition(wl.mesh, r, world) for r in range(world)]
+    oits, ref = _global_linear(wl, tolerance_type)
+    assert res[0][0] == res[1][0]  # every rank ran the same iterations
+    assert abs(res[0][0] - oits) <= 2, (res[0][0], oits)
+    got = S.assemble(slabs, [res[r][2] for r in range(world)], wl.mesh, ncomp=3)
+    assert rel_l2(got, ref) < 1e-8
