@@ -192,11 +192,19 @@ int ppf_run(ppf_handle h, unsigned int n_increments, int output_every);
 
 /* The increment loop split open, for callers that act between blocks (the sharded driver
  * exchanges halo planes after every block): ppf_increment_block does block b's part of the
- * current increment exactly as ppf_run would (PostProcess / NucleationRate blocks only when
- * is_output; Primary blocks keep the initial condition at increment 0; old ages start from
- * the current vector at increment 0); ppf_end_increment rotates the ages, advances the
- * timer and reports a non-finite result as PPF_ERR_NAN. */
+ * current increment exactly as ppf_run would (PostProcess blocks only when is_output,
+ * NucleationRate blocks when is_output or on a nucleation-attempt increment; Primary blocks
+ * keep the initial condition at increment 0; old ages start from the current vector at
+ * increment 0); ppf_end_increment rotates the ages, advances the timer and reports a
+ * non-finite result as PPF_ERR_NAN. */
 int ppf_increment_block(ppf_handle h, int b, int is_output);
+
+/* Nucleation-attempt period (the `nucleation period` entry of the `nucleation` subsection,
+ * NucleationParameters::should_attempt_nucleation, src/user_inputs/nucleation_parameters.cc:
+ * 110-113): NucleationRate blocks run on output increments and on increments divisible by the
+ * period (problem.cc:436-443); the default is the reference's 2147483647, i.e. increment 0 and
+ * output increments. Stochastic nucleation itself is not part of this engine. */
+int ppf_set_nucleation_period(ppf_handle h, unsigned int period);
 int ppf_end_increment(ppf_handle h);
 
 /* One explicit solve of block index b (ExplicitSolver::solve_impl, explicit_solver.h:63-77). */

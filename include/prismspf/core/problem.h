@@ -356,6 +356,8 @@ class Problem {
           "set-up");
     if (user_inputs->temporal_discretization.initial_time != 0.0)
       check(ppf_set_time(handle, 0, user_inputs->temporal_discretization.initial_time), "start time");
+    check(ppf_set_nucleation_period(handle, user_inputs->nucleation_parameters.nucleation_period),
+          "nucleation period");
     if (adaptive) {
       ppf_adaptivity a{};
       a.min_refinement = (int)sd.min_refinement;

@@ -144,6 +144,12 @@ class UserInputParameters {
   BoundaryParameters boundary_parameters;
   UserConstants<dim> user_constants;
   MiscellaneousParameters misc_parameters;
+  // the nucleation-attempt schedule (nucleation_parameters.cc:25-29, 110-113): NucleationRate
+  // blocks run on output increments and on increments divisible by the period
+  struct NucleationSchedule {
+    unsigned int nucleation_period = 2147483647u;
+    bool should_attempt_nucleation(unsigned int increment) const { return increment % nucleation_period == 0; }
+  } nucleation_parameters;
   std::vector<std::string> not_applied;  // entries read but without effect in this engine
   prm::ParameterFile parameters;
 
@@ -317,8 +323,24 @@ class UserInputParameters {
     // miscellaneous (miscellaneous_parameters.cc:10-48)
     misc_parameters.set_random_seed((unsigned int)prm::to_int(P.get("miscellaneous", {"random seed"}, "2025")));
 
+    // the nucleation-attempt period decides when NucleationRate blocks run; the other
+    // nucleation entries drive stochastic nucleation, which this engine does not do
+    {
+      const long long period = prm::to_int(P.get("nucleation", {"nucleation period", "nucleation_period"},
+                                                 "2147483647"));
+      if (period < 1) throw std::invalid_argument("nucleation period must be at least 1");
+      nucleation_parameters.nucleation_period = (unsigned int)period;
+      bool other = false;
+      for (const auto& [k, v] : P.entries)
+        other |= k.rfind("nucleation/", 0) == 0 && k != "nucleation/nucleation period" &&
+                 k != "nucleation/nucleation_period";
+      if (other) {
+        P.mark_used_prefix("nucleation/");
+        not_applied.push_back("nucleation");
+      }
+    }
     // entries of subsystems outside this engine
-    for (const char* sec : {"checkpoint/", "nucleation/"}) {
+    for (const char* sec : {"checkpoint/"}) {
       bool any = false;
       for (const auto& [k, v] : P.entries) any |= k.rfind(sec, 0) == 0;
       if (any) {

@@ -433,6 +433,8 @@ struct Problem {
   std::vector<double> jxw[2], invm[2], invm_sqrt[2];
   double dt = 0.0, time = 0.0;
   unsigned increment = 0;
+  // nucleation-attempt period (nucleation_parameters.cc:110-113, default 2147483647)
+  unsigned nucleation_period = 2147483647u;
   int model = 0;
   std::vector<double> params;
   int nthreads = 0;
@@ -2284,7 +2286,10 @@ int orc_explicit_block(void* h, int b) {
 int orc_increment_block(void* h, int b, int is_output) {
   auto* P = (Problem*)h;
   Block& B = P->blocks[b];
+  // PostProcess only on output increments; NucleationRate on output and nucleation-attempt
+  // increments (problem.cc:436-443)
   if (B.timing == ORC_TIMING_POSTPROCESS && !is_output) return 0;
+  if (B.timing == ORC_TIMING_NUCLEATION_RATE && !is_output && P->increment % P->nucleation_period != 0) return 0;
   if (P->increment == 0 && B.timing == ORC_TIMING_PRIMARY) {
     // initial condition already uploaded into `cur`; like
     // SolverBase::set_initial_condition (solver_base.h:178-229) no constraints are
@@ -2302,6 +2307,12 @@ int orc_increment_block(void* h, int b, int is_output) {
       for (int a = 0; a < F.n_old; ++a) F.old[a] = F.cur;
     }
   }
+  return 0;
+}
+
+int orc_set_nucleation_period(void* h, unsigned period) {
+  if (period < 1) return -1;
+  static_cast<Problem*>(h)->nucleation_period = period;
   return 0;
 }
 

@@ -76,6 +76,7 @@ def load() -> C.CDLL:
         lib.orc_diagonal.argtypes = [C.c_void_p, C.c_int, dp]
         lib.orc_increment_block.argtypes = [C.c_void_p, C.c_int, C.c_int]
         lib.orc_end_increment.argtypes = [C.c_void_p]
+        lib.orc_set_nucleation_period.argtypes = [C.c_void_p, C.c_uint]
         lib.orc_set_solver_type.argtypes = [C.c_void_p, C.c_int, C.c_int]
         lib.orc_set_newton_params.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
         lib.orc_newton_solve.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int), dp]
@@ -314,6 +315,9 @@ class Oracle:
 
     def end_increment(self) -> int:
         return int(self.lib.orc_end_increment(self.h))
+
+    def set_nucleation_period(self, period: int):
+        assert self.lib.orc_set_nucleation_period(self.h, period) == 0
 
     def set_linear_params(self, b: int, tolerance_type=0, tolerance=1e-10, max_iterations=100, preconditioner=0,
                           mg_depth=1, smoother_degree=5, smoothing_range=15.0, eig_cg_iterations=10, solver_type=0,

@@ -178,6 +178,8 @@ struct ppf_handle_s {
   double dt = 0.0;
   std::string err;
   bool use_graph = true;
+  // NucleationRate blocks also run on increments divisible by this (nucleation_parameters.cc:110-113)
+  unsigned int nucleation_period = 2147483647u;
   double* d_scratch_src = nullptr;  // ppf_apply host-path staging
   double* d_scratch_dst = nullptr;
   long long scratch_len = 0;

@@ -855,13 +855,15 @@ static void rotate(ppf_handle h) {
 __global__ void advance_timer_kernel(prismspf::SimulationTimer* t, double dt) { t->increment(dt); }
 
 // The part of Problem::solve_increment (problem.cc:416-557) that belongs to block b: skipped
-// unless due (PostProcess / NucleationRate only on output increments), the initial condition
-// kept at increment 0 for Primary blocks, else the block's solver; at increment 0 the old ages
-// of its fields start from the current vector.
+// unless due (PostProcess only on output increments, NucleationRate on output and nucleation-
+// attempt increments, problem.cc:436-443), the initial condition kept at increment 0 for
+// Primary blocks, else the block's solver; at increment 0 the old ages of its fields start from
+// the current vector.
 static int increment_block(ppf_handle h, int b, bool is_output) {
   const unsigned inc = h->timer.get_increment();
   const ppf_block_desc& d = h->blocks[b].desc;
-  if ((d.solve_timing == PPF_POSTPROCESS || d.solve_timing == PPF_NUCLEATION_RATE) && !is_output) return PPF_OK;
+  if (d.solve_timing == PPF_POSTPROCESS && !is_output) return PPF_OK;
+  if (d.solve_timing == PPF_NUCLEATION_RATE && !is_output && inc % h->nucleation_period != 0) return PPF_OK;
   if (inc == 0 && d.solve_timing == PPF_PRIMARY) {
     // initial condition is the uploaded current vector (SolverBase::solve at increment 0)
   } else if (d.solve_type == PPF_EXPLICIT) {
@@ -1397,6 +1399,14 @@ int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
         const unsigned nr = amr_next_remesh(h, inc);
         if (nr != ~0u && nr - 1 < last) last = nr - 1;
       }
+      // nor does it cover a nucleation-attempt increment, which runs NucleationRate blocks
+      for (auto& B : h->blocks)
+        if (B.desc.solve_timing == PPF_NUCLEATION_RATE) {
+          const unsigned P = h->nucleation_period;
+          const unsigned long long due = ((unsigned long long)inc + P - 1) / P * P;  // first due >= inc
+          if (due == inc) last = inc - 1;  // this increment itself: plain launches
+          else if (due - 1 < last) last = (unsigned)(due - 1);
+        }
       const unsigned remaining = last >= inc ? last - inc + 1 : 0;
       if (remaining >= (unsigned)period) {
         if (!h->run_graph || h->graph_stream != h->stream || h->graph_phase != h->rot_count % period ||
@@ -1491,6 +1501,12 @@ int ppf_get_time(ppf_handle h, unsigned int* increment, double* time) {
   if (!h) return PPF_ERR_ARG;
   if (increment) *increment = h->timer.get_increment();
   if (time) *time = h->timer.get_time();
+  return PPF_OK;
+}
+
+int ppf_set_nucleation_period(ppf_handle h, unsigned int period) {
+  if (!h || period < 1) return PPF_ERR_ARG;
+  h->nucleation_period = period;
   return PPF_OK;
 }
 

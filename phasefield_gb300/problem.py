@@ -317,6 +317,10 @@ class Problem:
         """Problem::solve: increments from the current one through n_increments."""
         self._check(self.lib.ppf_run(self.h, n_increments, output_every))
 
+    def set_nucleation_period(self, period: int):
+        """NucleationRate blocks also run on increments divisible by `period`."""
+        self._check(self.lib.ppf_set_nucleation_period(self.h, period))
+
     def increment_block(self, b: int, is_output: bool = False):
         """Block b's part of the current increment (ppf_increment_block)."""
         self._check(self.lib.ppf_increment_block(self.h, b, int(is_output)))

@@ -31,7 +31,8 @@ def eshelby_small(dim=3, degree=2, refine=2, n_incl=5):
 # maps
 # ---------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("dim,degree,refine,sub", [(2, 1, 2, (1, 1, 1)), (2, 2, 1, (2, 3, 1)), (2, 3, 1, (1, 1, 1)),
-                                                    (2, 4, 1, (1, 2, 1)), (3, 1, 2, (1, 1, 1)), (3, 2, 1, (2, 1, 1))])
+                                                    (2, 4, 1, (1, 2, 1)), (3, 1, 2, (1, 1, 1)), (3, 2, 1, (2, 1, 1)),
+                                                    (3, 3, 1, (1, 2, 1)), (3, 4, 1, (1, 1, 2))])
 def test_dof_map_bit_exact(gpu_lib, dim, degree, refine, sub):
     wl = W.cahn_hilliard_3d(refine=refine, degree=degree, dim=dim, size=2.0, subdivisions=sub, periodic=False)
     wl.mesh.size = tuple(float(s) for s in sub[:dim]) + (1.0,) * (3 - dim)
@@ -77,12 +78,23 @@ def test_periodic_constraint_map_bit_exact(gpu_lib):
 
 def test_dirichlet_constraint_map_bit_exact(gpu_lib):
     wl = eshelby_small(dim=3, degree=2, refine=1)
+    # u = 0 on x = 0 (boundary id 0) and u_x = 0.05 on x = 16 (boundary id 1): nonzero values
+    wl.fields[0].dirichlet[(0, 1)] = 0.05
     p = wl.make_problem()
     o = po.Oracle(wl)
     ref, vals = _oracle_cmap_lattice(o, 0)
     got = p.constraint_map(0).astype(np.int64)
     assert np.array_equal(got >= 0, ref >= 0)
     assert np.array_equal(got[got >= 0], ref[got >= 0])
+    # the values: distributing the constraints on a zero vector leaves exactly the Dirichlet
+    # values in the constrained rows (AffineConstraints::distribute)
+    p.upload(0, np.zeros(p.field_length(0)))
+    p.apply_constraints(0)
+    u = p.download(0)
+    rows = ref < 0
+    assert rows.sum() > 0 and np.any(vals[rows] != 0.0)
+    assert np.array_equal(u[rows], vals[rows])
+    assert np.all(u[~rows] == 0.0)
 
 
 def test_invm_matches(gpu_lib):
@@ -109,7 +121,7 @@ def test_allen_cahn_rhs_apply(gpu_lib, degree):
         assert rel_l2(got, ref) < APPLY_TOL
 
 
-@pytest.mark.parametrize("dim,degree", [(2, 2), (3, 1), (3, 2)])
+@pytest.mark.parametrize("dim,degree", [(2, 2), (3, 1), (3, 2), (3, 3), (3, 4)])
 def test_cahn_hilliard_block_applies(gpu_lib, dim, degree):
     wl = W.cahn_hilliard_3d(refine=2 if dim == 3 else 4, degree=degree, dim=dim, size=8.0)
     p = wl.make_problem()
@@ -162,10 +174,11 @@ def test_allen_cahn_steps(gpu_lib, degree):
         assert rel_l2(got, ref) < STEPS_TOL, f
 
 
-@pytest.mark.parametrize("dim,degree", [(2, 1), (2, 2), (3, 1), (3, 2)])
+@pytest.mark.parametrize("dim,degree", [(2, 1), (2, 2), (3, 1), (3, 2), (3, 3), (3, 4)])
 def test_cahn_hilliard_steps_periodic(gpu_lib, dim, degree):
-    # time steps at about a third of the explicit stability limit of each discretisation
-    dt = {(2, 1): 5e-4, (2, 2): 1.5e-5, (3, 1): 2e-4, (3, 2): 1e-4}[(dim, degree)]
+    # time steps at about a third of the explicit stability limit of each discretisation (Q3
+    # and Q4 in 3-D: well inside it, the closer Gauss-Lobatto points make them stiffer)
+    dt = {(2, 1): 5e-4, (2, 2): 1.5e-5, (3, 1): 2e-4, (3, 2): 1e-4, (3, 3): 2e-6, (3, 4): 5e-7}[(dim, degree)]
     wl = W.cahn_hilliard_3d(refine=2 if dim == 3 else 4, degree=degree, dim=dim, size=8.0 if dim == 2 else 4.0,
                             dt=dt)
     p = wl.make_problem()
