@@ -11,8 +11,11 @@
 //     biased IEEE-754 exponent among them;
 //   * to_fixed(v, E, top) is v * 2^(1023 + top - E) rounded to an integer (ties away from
 //     zero): the largest value of the block lands in [2^top, 2^(top+1)), smaller ones keep
-//     every bit down to 2^(E - 1023 - top) — at least as fine as the rounding unit of the FP64
-//     sums they replace, whose terms are as large as the block's largest value;
+//     every bit down to 2^(E - 1023 - top). The error bound is therefore absolute, relative to
+//     the block's largest value: a sum over a line whose own values sit far below the block's
+//     largest value keeps that absolute resolution (2^(E - 1023 - top) per term), not 53 bits
+//     of its own magnitude. For lines at the block's top exponent this is as fine as the
+//     rounding of the FP64 sums it replaces;
 //   * integer sums of such values with small integer coefficients are exact while they stay
 //     below 2^63 (the callers pick `top` for the headroom of their coefficients);
 //   * to_double(x, lsb, sigma) = x * 2^lsb * sigma rounded to nearest, with sigma in [1, 2)

@@ -172,3 +172,46 @@ def test_nonfinite_value_reports_nan_in_every_mode(gpu_lib, mode):
         with pytest.raises(capi.PPFError) as e:
             p.solve(1)
         assert e.value.code == capi.PPF_ERR_NAN
+
+
+@pytest.mark.parametrize("mode", ["1", "2"])
+def test_derivative_error_is_absolute_in_the_cell_maximum(gpu_lib, mode):
+    """Per entry, a derivative taken in fixed point is exact to the block resolution of its
+    cell: the absolute error is at most (sum of |D| over the line) x 2^(e - 58) / h, e the
+    binary exponent of the cell's largest value, plus the final rounding. Every Q2 cell here
+    holds O(1) corner values and an O(1e-12) cross through its centre, so the gradient at the
+    centre node is O(1e-13) while the cell's block exponent is that of its O(1) corners: there
+    the error stays within the absolute bound (a relative error of order 1e-6 of the small
+    gradient itself), while FP64 contractions of the same line keep 1e-13 relative. The
+    post-processing block's |grad n| at each cell's centre node (interior to one cell, so the
+    lumped-mass scaling returns the point value) exposes the derivative itself."""
+    wl = W.allen_cahn_2d(refine=3, degree=2)  # 8 x 8 Q2 cells of [0,100]^2, 17 x 17 nodes
+    nc, nn, h = 8, 17, 100.0 / 8
+    rng = np.random.default_rng(23)
+    u = rng.uniform(0.5, 1.0, (nn, nn))  # [y, x]
+    small = 1e-12
+    for c in range(nc):  # the row and column through every cell centre
+        u[2 * c + 1, :] = small * rng.uniform(-1, 1, nn)
+        u[:, 2 * c + 1] = small * rng.uniform(-1, 1, nn)
+    n0 = u.ravel()
+    centre = np.array([(2 * cy + 1) * nn + 2 * cx + 1 for cy in range(nc) for cx in range(nc)])
+    # the exact centre gradients of the quadratic interpolant: (u_right - u_left) / h per direction
+    gx = np.array([(u[2 * cy + 1, 2 * cx + 2] - u[2 * cy + 1, 2 * cx]) / h for cy in range(nc) for cx in range(nc)])
+    gy = np.array([(u[2 * cy + 2, 2 * cx + 1] - u[2 * cy, 2 * cx + 1]) / h for cy in range(nc) for cx in range(nc)])
+    exact = np.hypot(gx, gy)
+    cell_max = np.array([np.abs(u[2 * cy:2 * cy + 3, 2 * cx:2 * cx + 3]).max() for cy in range(nc) for cx in range(nc)])
+    resolution = 2.0 ** (np.floor(np.log2(cell_max)) - 58)
+
+    def centre_gradients(**kw):
+        with env(**kw):
+            p = wl.make_problem()
+            p.upload(0, n0, age=0)
+            out = p.apply(1, 0, None, scale=1)  # the post-processing block: mg_n, then f_tot
+            p.close()
+        return out[:nn * nn][centre]
+
+    fp64 = centre_gradients(PPF_FP64_CONTRACTIONS="1")
+    assert np.all(np.abs(fp64 - exact) <= 1e-13 * exact)
+    fixed = centre_gradients(PPF_CONTRACTION_MODE=mode)
+    bound = 2.0 * np.sqrt(2.0) * resolution / h + 8 * np.spacing(exact)
+    assert np.all(np.abs(fixed - exact) <= bound)
