@@ -96,3 +96,8 @@ PRISMS_PF_END_NAMESPACE
 // override (see the header comment)
 #define compute_rhs ppf_compute_rhs_declared_(); public: PPF_CALLBACK_SPACE void compute_rhs
 #define compute_lhs ppf_compute_lhs_declared_(); public: PPF_CALLBACK_SPACE void compute_lhs
+// the user's `void pre_solve_block(...) override` / `void post_solve_block(...) override`
+// become public host overrides, so Problem can tell whether the operator declares them (an
+// operator without hooks keeps the CUDA-graph increment loop)
+#define pre_solve_block ppf_pre_solve_block_declared_(); public: void pre_solve_block
+#define post_solve_block ppf_post_solve_block_declared_(); public: void post_solve_block

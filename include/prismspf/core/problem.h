@@ -27,9 +27,15 @@
 //     mesh and carried through the refinement passes as the reference's solution transfer does,
 //     Dirichlet values come from set_dirichlet at the nodes of every mesh, and the output
 //     writes the active cells of the current mesh.
-// Not carried over: nucleation, checkpoints, initial conditions from files,
-// pre/post_solve_block hooks, user stop. Newton blocks run with cg or bicgstab (no
-// preconditioner, or Chebyshev for single-field blocks).
+//   * an operator that declares pre_solve_block / post_solve_block gets them called around
+//     every block solved in an increment with a SolveContext (prismspf/solvers/solve_context.h),
+//     the increment loop then running block by block (ppf_increment_block); set_user_stop(true)
+//     in a hook ends the run after that increment with its output written and "Exit triggered
+//     by user!" (problem.cc:436-477, 392-414);
+//   * NucleationRate blocks run on output increments and on increments divisible by the
+//     `nucleation period` (nucleation_parameters.cc:110-113).
+// Not carried over: stochastic nucleation, checkpoints, initial conditions from files. Newton
+// blocks run with cg or bicgstab (no preconditioner, or Chebyshev for single-field blocks).
 #pragma once
 
 #include <cmath>
@@ -55,7 +61,14 @@
 #include <prismspf/core/solution_output.h>
 #include <prismspf/core/solve_block.h>
 #include <prismspf/core/type_enums.h>
+#include <prismspf/solvers/solve_context.h>
 #include <prismspf/user_inputs/user_input_parameters.h>
+
+// the hook names are rewritten for user classes by pde_operator_base.h; this header calls them
+#pragma push_macro("pre_solve_block")
+#pragma push_macro("post_solve_block")
+#undef pre_solve_block
+#undef post_solve_block
 
 #ifdef __CUDACC__
 #include <prismspf/gpu/launch.cuh>
@@ -98,6 +111,14 @@ struct UserOperator {
     reinterpret_cast<const PDE*>(bytes)->PDE::compute_lhs(fc, t, id);
   }
 };
+
+// true when PDE itself declares pre_solve_block or post_solve_block
+template <class PDE, unsigned int dim, unsigned int degree, typename number>
+constexpr bool declares_hooks() {
+  using Own = void (PDE::*)(SolveContext<dim, degree, number>&, unsigned int);
+  return std::is_same_v<decltype(&PDE::pre_solve_block), Own> ||
+         std::is_same_v<decltype(&PDE::post_solve_block), Own>;
+}
 
 // true when PDE itself declares compute_lhs (a Linear block needs it)
 template <class PDE, unsigned int dim, unsigned int degree, typename number>
@@ -157,6 +178,8 @@ class Problem {
     object_source = b;
     object_size = sizeof(PDE);
     has_lhs = detail::declares_lhs<PDE, dim, degree, number>();
+    has_hooks = detail::declares_hooks<PDE, dim, degree, number>();
+    hooks = &_pde_operator;
 #ifdef __CUDACC__
     launcher = &detail::launch_user_operator<PDE, (int)dim, (int)degree,
                                              detail::declares_lhs<PDE, dim, degree, number>()>;
@@ -179,6 +202,10 @@ class Problem {
 
   void solve() {
     init_system();
+    if (has_hooks) {
+      solve_with_hooks();
+      return;
+    }
     const TemporalDiscretization& time = user_inputs->temporal_discretization;
     const unsigned int n = time.n_increments;
     std::vector<unsigned int> outputs;
@@ -210,6 +237,56 @@ class Problem {
 
   // engine handle (valid after solve() has started)
   ppf_handle get_handle() const { return handle; }
+
+ private:
+  // Problem::solve with the operator's pre/post_solve_block hooks (problem.cc:416-557): the
+  // blocks of an increment one at a time, each solved block between its two hooks, then the
+  // remeshing step, the rotation, the output, and the user stop (exit status 3).
+  void solve_with_hooks() {
+    const unsigned int n = user_inputs->temporal_discretization.n_increments;
+    std::set<unsigned int> outputs;
+    for (unsigned int o : user_inputs->output_parameters.output_list)
+      if (o <= n) outputs.insert(o);
+    SolveContext<dim, degree, number> ctx(field_attributes, *user_inputs, *hooks, handle);
+    for (unsigned int inc = current_increment(); inc <= n; ++inc) {
+      if (time_dependent) update_dirichlet(inc);
+      const bool is_output = outputs.count(inc) != 0;
+      const bool attempt = user_inputs->nucleation_parameters.should_attempt_nucleation(inc);
+      for (size_t b = 0; b < solve_blocks.size(); ++b) {
+        const SolveTiming t = solve_blocks[b].solve_timing;
+        const bool due = !(t == PostProcess && !is_output) && !(t == NucleationRate && !(is_output || attempt));
+        if (due) {
+          double time = 0.0;
+          unsigned int cur = 0;
+          ppf_get_time(handle, &cur, &time);
+          SimulationTimer timer(user_inputs->temporal_discretization.dt, 0.0);
+          timer.set_increment(cur);
+          timer.set_time(time);
+          ctx.set_simulation_timer(timer);
+          hooks->pre_solve_block(ctx, (unsigned int)solve_blocks[b].id);
+        }
+        const int rc = ppf_increment_block(handle, (int)b, is_output ? 1 : 0);
+        if (rc != PPF_OK && rc != PPF_ERR_NOCONV) check(rc, "solve block");
+        if (due) hooks->post_solve_block(ctx, (unsigned int)solve_blocks[b].id);
+      }
+      if (adaptive) check(ppf_remesh_if_due(handle), "remeshing");
+      const int rc = ppf_end_increment(handle);
+      if (rc == PPF_ERR_NAN) {
+        write_output(inc);
+        throw ExcNaN("Exiting early.");
+      }
+      check(rc, "end of increment");
+      const bool stop = hooks->get_user_stop();
+      if (is_output || stop) write_output(inc);
+      if (stop) {
+        std::cout << "Exit triggered by user!" << std::endl;
+        break;
+      }
+    }
+    check(ppf_synchronize(handle), "synchronize");
+  }
+
+ public:
 
  private:
   void check(int rc, const char* what) const {
@@ -607,6 +684,8 @@ class Problem {
   const UserInputParameters<dim>* user_inputs;
   PhaseFieldTools<dim>* pf_tools;
   const Base* pde;
+  Base* hooks = nullptr;  // the same operator, for its non-const hooks and user stop
+  bool has_hooks = false;
   const unsigned char* object_source = nullptr;
   size_t object_size = 0;
   bool has_lhs = false;
@@ -623,3 +702,6 @@ PRISMS_PF_END_NAMESPACE
 
 #pragma pop_macro("compute_lhs")
 #pragma pop_macro("compute_rhs")
+
+#pragma pop_macro("post_solve_block")
+#pragma pop_macro("pre_solve_block")
