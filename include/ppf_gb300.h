@@ -178,6 +178,27 @@ int ppf_upload_state(ppf_handle h, int field, int age, const double* host, int o
  * waits for the stream (ppf_run, ppf_solve_block, a download) returned. Lattice (= native)
  * order, uniform meshes. Engine-side addition for callers overlapping host work with copies. */
 int ppf_upload_state_async(ppf_handle h, int f, int age, const double* host, int ordering);
+
+/* Pipelined I/O for callers that feed every increment from host memory and read every result
+ * back (no counterpart in the reference, whose vectors live in host memory; it replaces the
+ * upload/solve/download sequence around Problem::solve_increment, problem.cc:416-557):
+ *   ppf_upload_state_staged copies `host` (lattice order, pinned memory for overlap) into a
+ *     device staging buffer of (field f, age) on the handle's upload stream right away, as soon
+ *     as the previous staged upload of that (f, age) was consumed; the next run, before its
+ *     first block, waits for it and copies it into the state. `host` must stay unchanged until
+ *     ppf_wait returned (or the run that consumes it ended).
+ *   ppf_run_async queues the increments of ppf_run and returns without waiting: streamed
+ *     outputs (ppf_set_output_stream) are copied out of a per-field staging copy, so the next
+ *     increment may start while the copy to the host is in flight; errors are reported by
+ *     ppf_wait.
+ *   ppf_wait waits for the queued runs, staged uploads and streamed-output copies, and returns
+ *     their status (PPF_ERR_NAN, PPF_ERR_DEPENDENCY) like ppf_run. The host buffers of streamed
+ *     outputs hold the last increment's results once it returned.
+ * A caller that loops { stage inputs; ppf_run_async } overlaps the copies of increment k+1 with
+ * the computation of increment k. Uniform meshes only. */
+int ppf_upload_state_staged(ppf_handle h, int f, int age, const double* host);
+int ppf_run_async(ppf_handle h, unsigned int n_increments, int output_every);
+int ppf_wait(ppf_handle h);
 int ppf_download_state(ppf_handle h, int field, int age, double* host, int ordering);
 
 /* Apply the constraints of field f to its current vector (AffineConstraints::distribute,

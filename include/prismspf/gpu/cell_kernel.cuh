@@ -103,7 +103,20 @@ struct CellLaunch {
   // (else FP64 from the nodal values), fx_int integrates in fixed point (else FP64 with jdt)
   int fx_deriv;
   int fx_int;
+  // faces of the lattice (bit 2d: lower face of axis d, 2d+1: upper) whose nodes carry no
+  // constraint in any map of the launch: a cell touching only such faces reads and scatters
+  // without the constraint maps (0: unknown, every cell uses the maps)
+  int free_faces;
 };
+
+// true when every node of cell (cx, cy, cz) is unconstrained in the launch's maps
+template <int dim>
+__device__ __forceinline__ bool cell_unconstrained(const CellLaunch& P, int cx, int cy, int cz) {
+  int touch = (cx == 0 ? 1 : 0) | (cx == P.nc[0] - 1 ? 2 : 0);
+  if (dim > 1) touch |= (cy == 0 ? 4 : 0) | (cy == P.nc[1] - 1 ? 8 : 0);
+  if (dim > 2) touch |= (cz == 0 ? 16 : 0) | (cz == P.nc[2] - 1 ? 32 : 0);
+  return (touch & ~P.free_faces) == 0;
+}
 
 template <int dim, int degree>
 struct CellShape {
@@ -121,13 +134,46 @@ __host__ __device__ constexpr bool cell_fx_capable() {
   return std::is_same<number, double>::value && degree <= 2;
 }
 
+// Shape of the warp-resident alternative kernel (prismspf/gpu/cell_kernel_warp.cuh): whole
+// cells per warp, 8 warps per thread block.
+template <int dim, int degree>
+struct WarpShape {
+  static constexpr int n = degree + 1;
+  static constexpr int nq = pg::ipow(n, dim);
+  static constexpr int cpw = 32 / nq;       // cells per warp
+  static constexpr int lanes = cpw * nq;    // lanes holding a (cell, quadrature point)
+  static constexpr int warps = 8;           // warps per thread block
+  static constexpr int threads = 32 * warps;
+};
+
+// bytes of one warp's region: nodal values, their fixed-point copies and the submitted terms
+// (32 lanes each), then the block exponents of the value rows and output components per cell
+template <int dim, int degree>
+__host__ __device__ constexpr size_t warp_region_bytes(int nrows_in, int nrows_out) {
+  using W = WarpShape<dim, degree>;
+  return (8 * 32 * (size_t)(2 * nrows_in + nrows_out) + 4 * (size_t)W::cpw * (size_t)(nrows_in + nrows_out) + 15) /
+         16 * 16;
+}
+
+template <int dim, int degree>
+__host__ __device__ constexpr size_t cell_warp_smem_bytes(int nrows_in, int nrows_out) {
+  using W = WarpShape<dim, degree>;
+  return (sizeof(pg::CellTables<dim, degree, double>) + 15) / 16 * 16 +
+         W::warps * warp_region_bytes<dim, degree>(nrows_in, nrows_out);
+}
+
+// Dynamic shared memory of a launch: enough for cell_kernel and, for FP64 Q1/Q2, for the
+// warp-resident kernel as well (the launcher picks either).
 template <int dim, int degree, typename number>
 __host__ __device__ inline size_t cell_smem_bytes(int nrows_in, int nrows_out) {
   using S = CellShape<dim, degree>;
   size_t tab = (sizeof(pg::CellTables<dim, degree, number>) + 15) / 16 * 16;
   size_t b = tab + sizeof(number) * (size_t)(nrows_in + nrows_out) * S::threads + 16;
-  if (cell_fx_capable<dim, degree, number>())
+  if (cell_fx_capable<dim, degree, number>()) {
     b += sizeof(long long) * (size_t)nrows_in * S::threads + sizeof(int) * (size_t)(nrows_in + nrows_out) * S::cpb;
+    const size_t w = cell_warp_smem_bytes<dim, degree>(nrows_in, nrows_out);
+    if (w > b) b = w;
+  }
   return b;
 }
 
@@ -242,6 +288,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
     const bool active = cell < P.ncells;
     int cx = 0, cy = 0, cz = 0;
     long long node = 0;
+    bool free_cell = false;
     if (active) {
       const unsigned int cl = (unsigned int)cell;
       const unsigned int q0 = div0.div(cl);
@@ -253,6 +300,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
         cz = (int)q1;
       }
       node = ((long long)(k * cz + qc) * P.nn[1] + (k * cy + qb)) * P.nn[0] + (k * cx + qa);
+      free_cell = cell_unconstrained<dim>(P, cx, cy, cz);
     }
     if constexpr (FXC) {
       // the value-row exponents were last read by the previous tile's callbacks; rows without a
@@ -276,7 +324,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
               number v = number(0);
               if (active) {
                 const long long idx = node + c * P.N;
-                if (sd.constrained_read) {
+                if (sd.constrained_read && !free_cell) {
                   // the value load issues with the map load: almost every entry is free, so
                   // the dependent second load is only paid on constrained entries
                   const int m = __ldg(sd.cmap + idx);
@@ -396,7 +444,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
               }
               if (has_v || has_g) {
                 const long long idx = node + c * P.N;
-                const int target = od.cmap ? od.cmap[idx] : (int)idx;
+                const int target = (od.cmap && !free_cell) ? od.cmap[idx] : (int)idx;
                 if (target >= 0) atomicAdd(static_cast<number*>(od.acc) + target, r);
               }
             }

@@ -9,8 +9,12 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <cstring>
+
 #include <prismspf/gpu/amr_cell_kernel.cuh>
 #include <prismspf/gpu/cell_kernel.cuh>
+#include <prismspf/gpu/cell_kernel_warp.cuh>
 
 namespace ppf {
 
@@ -49,11 +53,25 @@ cudaError_t launch_cell_kernel_impl(const CellLaunch& P, const void* obj, size_t
   return cudaGetLastError();
 }
 
+// PPF_CELL_KERNEL=warp runs FP64 Q1/Q2 RHS and LHS launches on the warp-resident alternative
+// (cell_kernel_warp.cuh) instead of cell_kernel's thread-block tiles
+inline bool use_warp_cell_kernel() {
+  static const int on = [] {
+    const char* e = std::getenv("PPF_CELL_KERNEL");
+    return (e && std::strcmp(e, "warp") == 0) ? 1 : 0;
+  }();
+  return on != 0;
+}
+
 // launches the instantiation with the fixed-point integration path only when the launch asks
 // for it (contraction modes 2 and 3 of FP64 Q1/Q2 operators)
 template <class PDE, int dim, int degree, int mode, typename number>
 cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
   if constexpr (cell_fx_capable<dim, degree, number>() && mode != MODE_DIAG) {
+    if (use_warp_cell_kernel() && smem >= cell_warp_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out)) {
+      if (P.fx_int) return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, true>(P, obj, smem, s);
+      return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, false>(P, obj, smem, s);
+    }
     if (P.fx_int) return launch_cell_kernel_impl<PDE, dim, degree, mode, number, true>(P, obj, smem, s);
   }
   return launch_cell_kernel_impl<PDE, dim, degree, mode, number, false>(P, obj, smem, s);

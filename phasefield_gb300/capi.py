@@ -41,7 +41,7 @@ EXPORTED = [
     "ppf_device_fp64_peak", "ppf_allen_cahn_step_noalloc", "ppf_allen_cahn_step_noalloc_status",
     "ppf_default_linear_params", "ppf_set_linear_params", "ppf_linear_solve", "ppf_lhs_diagonal",
     "ppf_set_newton_params", "ppf_newton_solve", "ppf_linear_stats", "ppf_increment_block", "ppf_end_increment",
-    "ppf_set_nucleation_period",
+    "ppf_set_nucleation_period", "ppf_upload_state_staged", "ppf_run_async", "ppf_wait",
     # ensembles (bound in phasefield_gb300/ensemble.py)
     "ppf_ensemble_create", "ppf_ensemble_destroy", "ppf_ensemble_last_error", "ppf_ensemble_instance_length",
     "ppf_ensemble_upload", "ppf_ensemble_download", "ppf_ensemble_run", "ppf_ensemble_autotune",
@@ -167,6 +167,9 @@ def load() -> C.CDLL:
     lib.ppf_linear_solve.argtypes = [H, C.c_int, P(C.c_int), dp]
     lib.ppf_increment_block.argtypes = [H, C.c_int, C.c_int]
     lib.ppf_set_nucleation_period.argtypes = [H, C.c_uint]
+    lib.ppf_upload_state_staged.argtypes = [H, C.c_int, C.c_int, dp]
+    lib.ppf_run_async.argtypes = [H, C.c_uint, C.c_int]
+    lib.ppf_wait.argtypes = [H]
     lib.ppf_end_increment.argtypes = [H]
     lib.ppf_linear_stats.argtypes = [H, C.c_int, dp, dp, dp, dp]
     lib.ppf_set_newton_params.argtypes = [H, C.c_int, C.c_int, C.c_double, C.c_double]

@@ -30,10 +30,22 @@ struct FieldState {
   std::vector<double> h_dvals;
   std::vector<long long> h_drow;  // position (component-major lattice index) of Dirichlet row j
   bool constrained = false;
+  // lattice faces (bit 2d lower, 2d+1 upper face of axis d) without a constrained node
+  int free_faces = 0;
   ppf_field_desc desc;
   // host destination the field is streamed to after every increment (ppf_set_output_stream)
   double* stream_out = nullptr;
   bool streamed = false;  // copied during the current increment
+  // pipelined I/O (ppf_upload_state_staged, ppf_run_async): per age a device staging buffer the
+  // upload stream fills ahead of the run that consumes it, with its ready / consumed events
+  double* in_stage[5] = {};
+  cudaEvent_t in_ready[5] = {};
+  cudaEvent_t in_free[5] = {};
+  bool in_pending[5] = {};
+  // a queued run streams the field out of this copy, so the next increment may overwrite the
+  // state while the copy to the host is in flight; out_free marks the end of that copy
+  double* out_stage = nullptr;
+  cudaEvent_t out_free = nullptr;
 };
 
 struct BlockPlan {
@@ -67,6 +79,7 @@ struct MGLevel {
   int precision = 0;            // 0 FP64, 1 FP32
   int* cmap = nullptr;          // homogeneous level constraints
   bool constrained = false;
+  int free_faces = 0;           // faces without a constrained node (CellLaunch::free_faces)
   void* invm_sqrt = nullptr;    // per node, level precision
   void* inv_diag = nullptr;     // len, level precision
   void* tables = nullptr;       // CellTables for the LHS (level precision)
@@ -174,6 +187,8 @@ struct ppf_handle_s {
   cudaStream_t copy_stream = nullptr; // device-to-host copies of streamed outputs
   cudaEvent_t copy_ev = nullptr;
   bool copies_pending = false;
+  cudaStream_t upload_stream = nullptr;  // host-to-device copies of staged uploads
+  bool async_run = false;                // inside ppf_run_async: no host waits
   prismspf::SimulationTimer timer;
   double dt = 0.0;
   std::string err;

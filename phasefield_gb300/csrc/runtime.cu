@@ -413,6 +413,15 @@ static void build_constraints(ppf_handle h, FieldState& F, const ppf_field_desc&
     if (m >= 0 && m != (int)gi && F.h_cmap[m] < 0) F.h_cmap[gi] = F.h_cmap[m];
   }
   F.constrained = any;
+  // faces whose nodes are all free in every component (the kernels skip the map there)
+  F.free_faces = 0x3f;
+  for (int b = 0; b < 2 * h->dim; ++b)
+    for (int c = 0; c < F.ncomp && ((F.free_faces >> b) & 1); ++c)
+      for (long long i = 0; i < N; ++i)
+        if (node_on_boundary(h, i, b) && F.h_cmap[c * N + i] != (int)(c * N + i)) {
+          F.free_faces &= ~(1 << b);
+          break;
+        }
 }
 
 static void build_invm(ppf_handle h) {
@@ -669,6 +678,12 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   L.tables = P.d_tables;
   L.timer = h->timer;
   L.timer_dev = h->capturing ? h->d_timer : nullptr;
+  // faces free of constraints in every map this launch reads (constrained src, condensed outputs)
+  L.free_faces = 0x3f;
+  for (int s = 0; s < P.nslots; ++s)
+    if (L.slots[s].constrained_read) L.free_faces &= h->fields[P.slot_field[s]].free_faces;
+  for (int i = 0; i < B.desc.n_fields; ++i)
+    if (L.outs[i].cmap) L.free_faces &= h->fields[B.desc.field_indices[i]].free_faces;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
   // adaptive meshes: integer derivatives with every level's tables, FP64 integration
@@ -813,17 +828,49 @@ static int explicit_solve(ppf_handle h, int b) {
 }
 
 // Queues the device-to-host copy of a streamed output on the copy stream, ordered after the
-// work already queued on the handle's stream (ppf_set_output_stream).
+// work already queued on the handle's stream (ppf_set_output_stream). Inside a queued run
+// (ppf_run_async) the field is first copied on the device into its output staging buffer
+// (once the previous increment's copy out of it ended), so later increments may overwrite the
+// state while the copy to the host is in flight.
 int stream_field_out(ppf_handle h, FieldState& F, const double* src) {
   if (!h->copy_stream) {
     PPF_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     PPF_CUDA(h, cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
   }
+  if (h->async_run) {
+    if (!F.out_stage) {
+      PPF_CUDA(h, cudaMalloc(&F.out_stage, sizeof(double) * F.len));
+      PPF_CUDA(h, cudaEventCreateWithFlags(&F.out_free, cudaEventDisableTiming));
+      PPF_CUDA(h, cudaEventRecord(F.out_free, h->copy_stream));
+    }
+    PPF_CUDA(h, cudaStreamWaitEvent(h->stream, F.out_free, 0));
+    PPF_CUDA(h, cudaMemcpyAsync(F.out_stage, src, sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
+    src = F.out_stage;
+  }
   PPF_CUDA(h, cudaEventRecord(h->copy_ev, h->stream));
   PPF_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->copy_ev, 0));
   PPF_CUDA(h, cudaMemcpyAsync(F.stream_out, src, sizeof(double) * F.len, cudaMemcpyDeviceToHost, h->copy_stream));
+  if (h->async_run) PPF_CUDA(h, cudaEventRecord(F.out_free, h->copy_stream));
   F.streamed = true;
   h->copies_pending = true;
+  return PPF_OK;
+}
+
+// Staged uploads waiting for the next run: the handle's stream waits for each upload, copies
+// the staging buffer into the state of its age, and marks the buffer free for the next upload.
+int consume_staged_uploads(ppf_handle h) {
+  for (size_t f = 0; f < h->fields.size(); ++f) {
+    FieldState& F = h->fields[f];
+    for (int a = 0; a < 5; ++a) {
+      if (!F.in_pending[a]) continue;
+      double* dst = state_ptr(h, (int)f, a);
+      if (!dst) return fail(h, PPF_ERR_ARG, "staged upload for an age that is not stored");
+      PPF_CUDA(h, cudaStreamWaitEvent(h->stream, F.in_ready[a], 0));
+      PPF_CUDA(h, cudaMemcpyAsync(dst, F.in_stage[a], sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
+      PPF_CUDA(h, cudaEventRecord(F.in_free[a], h->stream));
+      F.in_pending[a] = false;
+    }
+  }
   return PPF_OK;
 }
 
@@ -922,7 +969,7 @@ int finish_streamed_outputs(ppf_handle h) {
       int rc = stream_field_out(h, F, F.cur);
       if (rc) return rc;
     }
-  if (h->copies_pending) {
+  if (h->copies_pending && !h->async_run) {
     PPF_CUDA(h, cudaStreamSynchronize(h->copy_stream));
     h->copies_pending = false;
   }
@@ -1134,6 +1181,19 @@ void ppf_destroy(ppf_handle h) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
     cudaEventDestroy(h->copy_ev);
+  }
+  if (h->upload_stream) {
+    cudaStreamSynchronize(h->upload_stream);
+    cudaStreamDestroy(h->upload_stream);
+  }
+  for (auto& F : h->fields) {
+    for (int a = 0; a < 5; ++a) {
+      cudaFree(F.in_stage[a]);
+      if (F.in_ready[a]) cudaEventDestroy(F.in_ready[a]);
+      if (F.in_free[a]) cudaEventDestroy(F.in_free[a]);
+    }
+    cudaFree(F.out_stage);
+    if (F.out_free) cudaEventDestroy(F.out_free);
   }
   for (auto& F : h->fields) {
     cudaFree(F.cur);
@@ -1384,8 +1444,11 @@ static int capture_graph(ppf_handle h) {
   return PPF_OK;
 }
 
-int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
-  if (!h) return PPF_ERR_ARG;
+static int run_increments(ppf_handle h, unsigned int n_increments, int output_every) {
+  {
+    const int rc = consume_staged_uploads(h);
+    if (rc) return rc;
+  }
   while (h->timer.get_increment() <= n_increments) {
     const unsigned inc = h->timer.get_increment();
     // increment 0 (initial conditions) and the first explicit increment run as plain launches,
@@ -1428,7 +1491,52 @@ int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
     int rc = solve_increment(h, output_every);
     if (rc) return rc;
   }
+  return PPF_OK;
+}
+
+int ppf_run(ppf_handle h, unsigned int n_increments, int output_every) {
+  if (!h) return PPF_ERR_ARG;
+  const int rc = run_increments(h, n_increments, output_every);
+  if (rc) return rc;
   return check_err(h);
+}
+
+int ppf_run_async(ppf_handle h, unsigned int n_increments, int output_every) {
+  if (!h) return PPF_ERR_ARG;
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "queued runs on an adaptive mesh (use ppf_run)");
+  h->async_run = true;
+  const int rc = run_increments(h, n_increments, output_every);
+  h->async_run = false;
+  return rc;
+}
+
+int ppf_wait(ppf_handle h) {
+  if (!h) return PPF_ERR_ARG;
+  if (h->upload_stream) PPF_CUDA(h, cudaStreamSynchronize(h->upload_stream));
+  PPF_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->copy_stream) PPF_CUDA(h, cudaStreamSynchronize(h->copy_stream));
+  h->copies_pending = false;
+  return check_err(h);
+}
+
+int ppf_upload_state_staged(ppf_handle h, int f, int age, const double* host) {
+  if (!h || !host || f < 0 || f >= (int)h->fields.size() || age < 0 || age > 4) return PPF_ERR_ARG;
+  if (h->amr) return fail(h, PPF_ERR_UNSUPPORTED, "staged uploads on an adaptive mesh (use ppf_upload_state)");
+  FieldState& F = h->fields[f];
+  if (age > F.n_old) return fail(h, PPF_ERR_ARG, "age not stored for this field");
+  if (!h->upload_stream) PPF_CUDA(h, cudaStreamCreateWithFlags(&h->upload_stream, cudaStreamNonBlocking));
+  if (!F.in_stage[age]) {
+    PPF_CUDA(h, cudaMalloc(&F.in_stage[age], sizeof(double) * F.len));
+    PPF_CUDA(h, cudaEventCreateWithFlags(&F.in_ready[age], cudaEventDisableTiming));
+    PPF_CUDA(h, cudaEventCreateWithFlags(&F.in_free[age], cudaEventDisableTiming));
+    PPF_CUDA(h, cudaEventRecord(F.in_free[age], h->upload_stream));
+  }
+  // the staging buffer is free once the run that consumed the previous upload copied it
+  PPF_CUDA(h, cudaStreamWaitEvent(h->upload_stream, F.in_free[age], 0));
+  PPF_CUDA(h, cudaMemcpyAsync(F.in_stage[age], host, sizeof(double) * F.len, cudaMemcpyHostToDevice, h->upload_stream));
+  PPF_CUDA(h, cudaEventRecord(F.in_ready[age], h->upload_stream));
+  F.in_pending[age] = true;
+  return PPF_OK;
 }
 
 int ppf_increment_block(ppf_handle h, int b, int is_output) {
