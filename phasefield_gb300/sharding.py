@@ -17,8 +17,9 @@ Linear blocks (ShardedLinear): deal.II's SolverCG as LinearSolver::do_linear_sol
 rank is complete on the rows it owns (its ghost cells contribute locally), so an apply needs
 only the ghost planes of its input, refreshed by the same halo exchange; inner products sum
 the owned rows of every rank and meet in one all-reduce of a float64 scalar
-(linear_solver.h:357-379 reduces them over MPI the same way). No preconditioner: the
-multigrid hierarchy and the Chebyshev eigenvalue estimate stay per GPU.
+(linear_solver.h:357-379 reduces them over MPI the same way). Preconditioners: none, or the
+reference's PreconditionerType::Chebyshev, whose diagonal is local and whose eigenvalue estimate
+and inner applies use the same exchange and reductions; the multigrid hierarchy stays per GPU.
 
 Scope: explicit, constant and post-processing blocks (the explicit increment loop), and single-
 field Linear blocks with homogeneous Dirichlet values through ShardedLinear. Newton blocks are
@@ -211,6 +212,17 @@ class EngineLocal:
         self.p.device_view(f, 0).copy_(v)
         self.p.apply_constraints(f)
 
+    def lhs_diagonal(self, b: int, tolerance_type: int):
+        """The block's LHS diagonal on this slab (scaled by invM^1/2 unless AbsoluteResidual,
+        zero entries one); rows this rank owns are complete."""
+        self.p.set_linear_params(b, tolerance_type=tolerance_type)
+        return self.torch.from_numpy(self.p.lhs_diagonal(b)).to("cuda")
+
+    def constrained(self, f: int) -> np.ndarray:
+        """Rows of field f the slab's constraint map ties to a master or a Dirichlet value."""
+        m = self.p.constraint_map(f).astype(np.int64)
+        return m != np.arange(m.size)
+
 
 
 # ---------------------------------------------------------------------------------------------
@@ -371,10 +383,43 @@ def local_workload(wl, slab: Slab):
     return w
 
 
+def _tridiag_max(a, b) -> float:
+    """Largest eigenvalue of the symmetric tridiagonal matrix (diagonal a, off-diagonal b) by
+    Sturm-count bisection inside its Gershgorin interval."""
+    m = len(a)
+    if not m:
+        return 1.0
+    lo, hi = a[0], a[0]
+    for i in range(m):
+        r = (abs(b[i - 1]) if i > 0 else 0.0) + (abs(b[i]) if i + 1 < m else 0.0)
+        lo, hi = min(lo, a[i] - r), max(hi, a[i] + r)
+
+    def below(x):
+        cnt, q = 0, a[0] - x
+        if q < 0:
+            cnt += 1
+        for i in range(1, m):
+            qq = 1e-300 if q == 0.0 else q
+            q = a[i] - x - b[i - 1] * b[i - 1] / qq
+            if q < 0:
+                cnt += 1
+        return cnt
+
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if below(mid) >= m:
+            hi = mid
+        else:
+            lo = mid
+        if hi - lo <= 1e-14 * max(1.0, abs(hi)):
+            break
+    return hi
+
+
 class ShardedLinear:
     """The CG solve of a single-field Linear block over all ranks: deal.II's SolverCG as
-    LinearSolver::solve_impl / do_linear_solve run it (linear_solver.h:305-402), without a
-    preconditioner, from the previous solution of the block (zero at first), to
+    LinearSolver::solve_impl / do_linear_solve run it (linear_solver.h:305-402), with no
+    preconditioner or a Chebyshev one, from the previous solution of the block (zero at first), to
     ||S (b - A x)|| < tolerance x normalization (S = invM^1/2 unless AbsoluteResidual;
     linear_solver.h:414-427). Vectors are local lattice vectors (ghost planes included); each
     operator apply first refreshes the ghost planes of its input; inner products sum the owned
@@ -386,6 +431,7 @@ class ShardedLinear:
         self.halo = HaloExchange(slab, dist)
         self.volume = float(np.prod([global_mesh.size[d] for d in range(global_mesh.dim)]))
         self.x = {}
+        self.eig = {}
         self.iterations = {}
         self.residual = {}
 
@@ -397,6 +443,62 @@ class ShardedLinear:
         lo, hi = self.slab.owned_planes()
         return [(c * n + lo * P, c * n + hi * P) for c in range(ncomp)]
 
+    def _global_index(self, ncomp: int) -> np.ndarray:
+        """Global lattice index (component-major) of every local row."""
+        sl = self.slab
+        P, n = sl.plane_size, sl.n_nodes
+        N_global = sl.plane_size * (sl.degree * sl.n_cells + 1)
+        planes = np.array([sl.global_plane(L) for L in range(sl.local_planes)], dtype=np.int64)
+        node = (planes[:, None] * P + np.arange(P, dtype=np.int64)[None, :]).ravel()
+        return np.concatenate([c * N_global + node for c in range(ncomp)])
+
+    def _estimate_eig(self, b, A, inv_diag, f, ncomp, owned, eig_its, smoothing_range):
+        """Largest eigenvalue of D^-1 A from eig_its CG steps on A x = pattern, x0 = 0, pattern
+        the global lattice index mod 11 minus its mean over the unconstrained rows (the engine's
+        and the oracle's estimate), reduced over the ranks; lambda_max x 1.2 and
+        lambda_min = lambda_max / range as the Chebyshev interval."""
+        torch = __import__("torch")
+        cons = self.local.constrained(f)
+        gi = self._global_index(ncomp)
+        own = np.zeros(gi.size, dtype=bool)
+        for a, e in owned:
+            own[a:e] = True
+        pat = (gi % 11).astype(np.float64)
+        free = own & ~cons
+        sums = torch.tensor([pat[free].sum(), float(free.sum())], dtype=torch.float64, device=inv_diag.device)
+        if self.dist is not None and self.slab.size > 1:
+            self.dist.all_reduce(sums, op=self.dist.ReduceOp.SUM)
+        mean = float(sums[0]) / max(1.0, float(sums[1]))
+        rhs = torch.from_numpy(np.where(cons, 0.0, pat - mean)).to(inv_diag.device)
+        x = torch.zeros_like(rhs)
+        r = rhs.clone()
+        z = inv_diag * r
+        p = z.clone()
+        rz, r0 = self.dot(r, z, owned), self.dot(r, r, owned)
+        al, be = [], []
+        for _ in range(eig_its):
+            q = A(p)
+            pq = self.dot(p, q, owned)
+            if pq <= 0.0 or not np.isfinite(pq):
+                break
+            alpha = rz / pq
+            x += alpha * p
+            r -= alpha * q
+            al.append(alpha)
+            if np.sqrt(self.dot(r, r, owned)) < 1e-10 * np.sqrt(r0):
+                break
+            z = inv_diag * r
+            rzn = self.dot(r, z, owned)
+            beta = rzn / rz
+            rz = rzn
+            be.append(beta)
+            p = z + beta * p
+        m = len(al)
+        a = [1.0 / al[i] + (be[i - 1] / al[i - 1] if i > 0 else 0.0) for i in range(m)]
+        o = [np.sqrt(max(0.0, be[i])) / al[i] for i in range(m - 1)]
+        lmax = 1.2 * _tridiag_max(a, o)
+        return lmax, lmax / smoothing_range
+
     def dot(self, u, v, owned) -> float:
         torch = __import__("torch")
         s = torch.zeros(1, dtype=torch.float64, device=u.device)
@@ -406,7 +508,12 @@ class ShardedLinear:
             self.dist.all_reduce(s, op=self.dist.ReduceOp.SUM)
         return float(s.item())
 
-    def solve(self, b: int, tolerance_type: int = 0, tolerance: float = 1e-10, max_iterations: int = 1000):
+    def solve(self, b: int, tolerance_type: int = 0, tolerance: float = 1e-10, max_iterations: int = 1000,
+              preconditioner: int = 0, smoother_degree: int = 5, smoothing_range: float = 15.0,
+              eig_cg_iterations: int = 10):
+        """preconditioner 0: none; 1: Chebyshev (PreconditionerType::Chebyshev) of
+        smoother_degree steps on the inverse diagonal, the interval from eig_cg_iterations
+        CG-Lanczos steps (estimated at the block's first solve, the diagonal at every solve)."""
         blk = self.blocks[b]
         if len(blk.field_indices) != 1:
             raise ValueError("the sharded linear solve covers single-field Linear blocks")
@@ -426,6 +533,34 @@ class ShardedLinear:
             return self.local.apply(b, 1, v, scale)
 
         rhs = self.local.apply(b, 0, None, scale)
+        if preconditioner == 1:
+            inv_diag = 1.0 / self.local.lhs_diagonal(b, tolerance_type)
+            if b not in self.eig:
+                self.eig[b] = self._estimate_eig(b, A, inv_diag, f, ncomp, owned, eig_cg_iterations, smoothing_range)
+            lmax, lmin = self.eig[b]
+            theta, delta = 0.5 * (lmax + lmin), 0.5 * (lmax - lmin)
+            sigma = theta / delta
+
+            def M(rr):  # Chebyshev of the first kind from a zero start (the oracle's smoother)
+                xx = self.local.zeros(rr.numel())
+                u = self.local.zeros(rr.numel())
+                rho_prev = 1.0 / sigma
+                for k in range(smoother_degree):
+                    res_k = rr if k == 0 else rr - A(xx)
+                    if k == 0:
+                        c1, c2 = 0.0, 1.0 / theta
+                    else:
+                        rho = 1.0 / (2.0 * sigma - rho_prev)
+                        c1, c2 = rho * rho_prev, 2.0 * rho / delta
+                        rho_prev = rho
+                    u = c1 * u + c2 * inv_diag * res_k
+                    xx = xx + u
+                return xx
+        elif preconditioner == 0:
+            def M(rr):
+                return rr
+        else:
+            raise ValueError("the sharded linear solve takes no preconditioner (0) or Chebyshev (1)")
         x = self.x.get(b)
         if x is None:
             x = self.local.zeros(rhs.numel())
@@ -433,21 +568,23 @@ class ShardedLinear:
         res = np.sqrt(self.dot(r, r, owned))
         it = 0
         if res >= tol:
-            p = r.clone()
-            rz = res * res
+            z = M(r)
+            p = z.clone()
+            rz = self.dot(r, z, owned)
             while it < max_iterations:
                 q = A(p)
                 alpha = rz / self.dot(p, q, owned)
                 x += alpha * p
                 r -= alpha * q
                 it += 1
-                rr = self.dot(r, r, owned)
-                res = np.sqrt(rr)
+                res = np.sqrt(self.dot(r, r, owned))
                 if res < tol:
                     break
-                beta = rr / rz
-                rz = rr
-                p = r + beta * p
+                z = M(r)
+                rzn = self.dot(r, z, owned)
+                beta = rzn / rz
+                rz = rzn
+                p = z + beta * p
         self.x[b] = x
         self.iterations[b], self.residual[b] = it, res / norm
         self.halo.exchange(x, ncomp)

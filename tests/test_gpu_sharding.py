@@ -45,22 +45,25 @@ def test_sharded_engine_one_rank_matches_plain(gpu_lib, case):
         assert rel_l2(got, ref.download(f, age=age)) < 1e-12, (f, age)
 
 
-@pytest.mark.parametrize("tolerance_type", [0, 1])
-def test_sharded_cg_engine_one_rank_matches_plain_cg(gpu_lib, tolerance_type):
+@pytest.mark.parametrize("tolerance_type,preconditioner", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_sharded_cg_engine_one_rank_matches_plain_cg(gpu_lib, tolerance_type, preconditioner):
     """The sharded CG of the elasticity block (device vectors, halo exchange with itself, owned
-    inner products) against the engine's own CG without a preconditioner: same iteration count
-    within 2 and solutions within 1e-8."""
+    inner products), without a preconditioner and with the Chebyshev one, against the engine's
+    own CG with the same preconditioner: same iteration count within 2, solutions within 1e-8."""
     import torch
+    cheb = dict(smoother_degree=4, smoothing_range=15.0, eig_cg_iterations=10)
     wl = W.eshelby_3d(refine=2, degree=2, size=16.0, n_incl=5)
     ref = wl.make_problem()
     b = ref.apply(0, 0, None, scale=0)
     tol = 1e-10 * float(np.linalg.norm(b)) if tolerance_type == 0 else 1e-9
-    ref.set_linear_params(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000, preconditioner=0)
+    ref.set_linear_params(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000,
+                          preconditioner=preconditioner, mg_depth=1, **cheb)
     its_ref, _ = ref.linear_solve(0)
     slab = S.partition(wl.mesh, 0, 1)
     p = S.local_workload(wl, slab).make_problem()
     run = S.ShardedLinear(slab, S.EngineLocal(p), wl.fields, wl.blocks, wl.mesh)
-    its, res = run.solve(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000)
+    its, res = run.solve(0, tolerance_type=tolerance_type, tolerance=tol, max_iterations=2000,
+                         preconditioner=preconditioner, **cheb)
     torch.cuda.synchronize()
     assert abs(its - its_ref) <= 2, (its, its_ref)
     got = S.assemble([slab], [run.owned(0)], wl.mesh, ncomp=3)

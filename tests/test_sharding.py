@@ -54,6 +54,17 @@ class OracleLocal:
     def set_current(self, f: int, v):
         self.o.set(f, v.numpy().copy(), 0)
 
+    def lhs_diagonal(self, b: int, tolerance_type: int):
+        self.o.set_linear_params(b, tolerance_type=tolerance_type)
+        return self.torch.from_numpy(self.o.diagonal(b))
+
+    def constrained(self, f: int) -> np.ndarray:
+        kind, _, _ = self.o.constraints(f)
+        perm = self.o.dealii_to_lattice(self.o.wl.fields[f].field_type)
+        out = np.zeros(perm.size, dtype=bool)
+        out[perm] = np.asarray(kind) != 0
+        return out
+
 
 def _ch(periodic=True):
     wl = W.cahn_hilliard_3d(refine=3, degree=2, dim=2, size=8.0, dt=2e-5, periodic=periodic)
@@ -188,21 +199,24 @@ def _linear_tolerance(wl, tolerance_type):
     return LINEAR_CASES[tolerance_type]
 
 
-def _run_linear(wl, rank, size, tolerance_type, dist_=None):
+CHEBYSHEV = dict(smoother_degree=4, smoothing_range=15.0, eig_cg_iterations=10)
+
+
+def _run_linear(wl, rank, size, tolerance_type, dist_=None, preconditioner=0):
     from oracle import pyoracle as po
     slab = S.partition(wl.mesh, rank, size)
     o = po.Oracle(S.local_workload(wl, slab))
     run = S.ShardedLinear(slab, OracleLocal(o), wl.fields, wl.blocks, wl.mesh, dist_)
     its, res = run.solve(0, tolerance_type=tolerance_type, tolerance=_linear_tolerance(wl, tolerance_type),
-                         max_iterations=2000)
+                         max_iterations=2000, preconditioner=preconditioner, **CHEBYSHEV)
     return slab, its, res, run.owned(0)
 
 
-def _global_linear(wl, tolerance_type):
+def _global_linear(wl, tolerance_type, preconditioner=0):
     from oracle import pyoracle as po
     o = po.Oracle(wl)
     o.set_linear_params(0, tolerance_type=tolerance_type, tolerance=_linear_tolerance(wl, tolerance_type),
-                        max_iterations=2000, preconditioner=0)
+                        max_iterations=2000, preconditioner=preconditioner, mg_depth=1, **CHEBYSHEV)
     rc, its, res = o.linear_solve(0)
     assert rc == 0
     return its, o.get(0)
@@ -217,37 +231,38 @@ def test_local_workload_drops_dirichlet_on_interior_faces():
     assert (2, 5) in wl.fields[0].dirichlet  # the global workload is unchanged
 
 
-@pytest.mark.parametrize("tolerance_type", [0, 1])
-def test_single_rank_sharded_cg_matches_global(tolerance_type):
+@pytest.mark.parametrize("tolerance_type,preconditioner", [(0, 0), (1, 0), (0, 1), (1, 1)])
+def test_single_rank_sharded_cg_matches_global(tolerance_type, preconditioner):
     wl = _elasticity()
-    slab, its, res, part = _run_linear(wl, 0, 1, tolerance_type)
-    oits, ref = _global_linear(wl, tolerance_type)
-    assert abs(its - oits) <= 2
+    slab, its, res, part = _run_linear(wl, 0, 1, tolerance_type, preconditioner=preconditioner)
+    oits, ref = _global_linear(wl, tolerance_type, preconditioner)
+    assert abs(its - oits) <= 2, (its, oits)
     assert rel_l2(S.assemble([slab], [part], wl.mesh, ncomp=3), ref) < 1e-8
 
 
-def _linear_worker(rank, world, port, tolerance_type, results):
+def _linear_worker(rank, world, port, tolerance_type, preconditioner, results):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
     import datetime
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=120))
     try:
-        _, its, res, part = _run_linear(_elasticity(), rank, world, tolerance_type, dist)
+        _, its, res, part = _run_linear(_elasticity(), rank, world, tolerance_type, dist, preconditioner)
         results[rank] = (its, res, part)
     finally:
         dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("tolerance_type", [0, 1])
-def test_two_gloo_ranks_sharded_cg_matches_global(tolerance_type):
+@pytest.mark.parametrize("tolerance_type,preconditioner", [(0, 0), (1, 1)])
+def test_two_gloo_ranks_sharded_cg_matches_global(tolerance_type, preconditioner):
     world = 2
     with mp.Manager() as m:
         results = m.dict()
-        mp.spawn(_linear_worker, args=(world, _free_port(), tolerance_type, results), nprocs=world, join=True)
+        mp.spawn(_linear_worker, args=(world, _free_port(), tolerance_type, preconditioner, results), nprocs=world,
+                 join=True)
         res = dict(results)
     wl = _elasticity()
     slabs = [S.partition(wl.mesh, r, world) for r in range(world)]
-    oits, ref = _global_linear(wl, tolerance_type)
+    oits, ref = _global_linear(wl, tolerance_type, preconditioner)
     assert res[0][0] == res[1][0]  # every rank ran the same iterations
     assert abs(res[0][0] - oits) <= 2, (res[0][0], oits)
     got = S.assemble(slabs, [res[r][2] for r in range(world)], wl.mesh, ncomp=3)
