@@ -241,49 +241,38 @@ class HaloExchange:
         return [(c * N + planes[0] * P, c * N + planes[1] * P) for c in range(ncomp)]
 
     def exchange(self, v, ncomp: int):
-        """Fills the ghost planes of the local lattice vector v (torch tensor) in place."""
+        """Fills the ghost planes of the local lattice vector v (torch tensor) in place. Each
+        component's plane range is one contiguous slice of v, so it is sent from and received
+        into a view of v directly: no packing or unpacking copies."""
         s = self.slab
-        torch = __import__("torch")
-        gather = lambda rs: torch.cat([v[a:b] for a, b in rs]) if rs else None  # noqa: E731
-
-        def scatter(rs, buf):
-            o = 0
-            for a, b in rs:
-                v[a:b].copy_(buf[o:o + b - a])
-                o += b - a
-
-        to_left = gather(self._ranges(s.send_left_planes(), ncomp)) if s.left is not None else None
-        to_right = gather(self._ranges(s.send_right_planes(), ncomp)) if s.right is not None else None
-        r_right = self._ranges(s.recv_right_planes(), ncomp) if s.right is not None else []
-        r_left = self._ranges(s.recv_left_planes(), ncomp) if s.left is not None else []
-        from_right = torch.empty(sum(b - a for a, b in r_right), dtype=v.dtype, device=v.device) if r_right else None
-        from_left = torch.empty(sum(b - a for a, b in r_left), dtype=v.dtype, device=v.device) if r_left else None
+        send_l = self._ranges(s.send_left_planes(), ncomp) if s.left is not None else []
+        send_r = self._ranges(s.send_right_planes(), ncomp) if s.right is not None else []
+        recv_r = self._ranges(s.recv_right_planes(), ncomp) if s.right is not None else []
+        recv_l = self._ranges(s.recv_left_planes(), ncomp) if s.left is not None else []
         if s.size == 1:
-            if from_right is not None:
-                from_right.copy_(to_left)
-            if from_left is not None:
-                from_left.copy_(to_right)
-        else:
-            # With two periodic ranks both neighbours are the same process: messages carry a
-            # direction tag (gloo), and every rank posts in the same order (leftward sends,
-            # rightward sends, receipts of leftward messages, of rightward messages) so that
-            # backends that pair point-to-point messages by order (NCCL) match them too.
-            LEFTWARD, RIGHTWARD = 1, 2
-            reqs = []
-            if s.left is not None:
-                reqs.append(self.dist.isend(to_left.contiguous(), s.left, tag=LEFTWARD))
-            if s.right is not None:
-                reqs.append(self.dist.isend(to_right.contiguous(), s.right, tag=RIGHTWARD))
-            if s.right is not None:
-                reqs.append(self.dist.irecv(from_right, s.right, tag=LEFTWARD))
-            if s.left is not None:
-                reqs.append(self.dist.irecv(from_left, s.left, tag=RIGHTWARD))
-            for r in reqs:
-                r.wait()
-        if from_right is not None:
-            scatter(r_right, from_right)
-        if from_left is not None:
-            scatter(r_left, from_left)
+            # the rank is its own neighbour (periodic split axis): local copies (the ranges of a
+            # pair never overlap: the sent planes are owned, the received ones ghosts)
+            for (a, b), (c, d) in zip(send_l, recv_r):
+                v[c:d].copy_(v[a:b])
+            for (a, b), (c, d) in zip(send_r, recv_l):
+                v[c:d].copy_(v[a:b])
+            return
+        # With two periodic ranks both neighbours are the same process: messages carry a
+        # direction and component tag (gloo), and every rank posts in the same order (leftward
+        # sends, rightward sends, receipts of leftward messages, of rightward messages) so that
+        # backends that pair point-to-point messages by order (NCCL) match them too.
+        LEFTWARD, RIGHTWARD = 1, 2
+        reqs = []
+        for c, (a, b) in enumerate(send_l):
+            reqs.append(self.dist.isend(v[a:b], s.left, tag=8 * LEFTWARD + c))
+        for c, (a, b) in enumerate(send_r):
+            reqs.append(self.dist.isend(v[a:b], s.right, tag=8 * RIGHTWARD + c))
+        for c, (a, b) in enumerate(recv_r):
+            reqs.append(self.dist.irecv(v[a:b], s.right, tag=8 * LEFTWARD + c))
+        for c, (a, b) in enumerate(recv_l):
+            reqs.append(self.dist.irecv(v[a:b], s.left, tag=8 * RIGHTWARD + c))
+        for r in reqs:
+            r.wait()
 
 
 class ShardedExplicit:
