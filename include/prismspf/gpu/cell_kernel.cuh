@@ -103,20 +103,7 @@ struct CellLaunch {
   // (else FP64 from the nodal values), fx_int integrates in fixed point (else FP64 with jdt)
   int fx_deriv;
   int fx_int;
-  // faces of the lattice (bit 2d: lower face of axis d, 2d+1: upper) whose nodes carry no
-  // constraint in any map of the launch: a cell touching only such faces reads and scatters
-  // without the constraint maps (0: unknown, every cell uses the maps)
-  int free_faces;
 };
-
-// true when every node of cell (cx, cy, cz) is unconstrained in the launch's maps
-template <int dim>
-__device__ __forceinline__ bool cell_unconstrained(const CellLaunch& P, int cx, int cy, int cz) {
-  int touch = (cx == 0 ? 1 : 0) | (cx == P.nc[0] - 1 ? 2 : 0);
-  if (dim > 1) touch |= (cy == 0 ? 4 : 0) | (cy == P.nc[1] - 1 ? 8 : 0);
-  if (dim > 2) touch |= (cz == 0 ? 16 : 0) | (cz == P.nc[2] - 1 ? 32 : 0);
-  return (touch & ~P.free_faces) == 0;
-}
 
 template <int dim, int degree>
 struct CellShape {
@@ -288,7 +275,6 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
     const bool active = cell < P.ncells;
     int cx = 0, cy = 0, cz = 0;
     long long node = 0;
-    bool free_cell = false;
     if (active) {
       const unsigned int cl = (unsigned int)cell;
       const unsigned int q0 = div0.div(cl);
@@ -300,7 +286,6 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
         cz = (int)q1;
       }
       node = ((long long)(k * cz + qc) * P.nn[1] + (k * cy + qb)) * P.nn[0] + (k * cx + qa);
-      free_cell = cell_unconstrained<dim>(P, cx, cy, cz);
     }
     if constexpr (FXC) {
       // the value-row exponents were last read by the previous tile's callbacks; rows without a
@@ -324,7 +309,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
               number v = number(0);
               if (active) {
                 const long long idx = node + c * P.N;
-                if (sd.constrained_read && !free_cell) {
+                if (sd.constrained_read) {
                   // the value load issues with the map load: almost every entry is free, so
                   // the dependent second load is only paid on constrained entries
                   const int m = __ldg(sd.cmap + idx);
@@ -444,7 +429,7 @@ __global__ void __launch_bounds__(CellShape<dim, degree>::threads, CellMinBlocks
               }
               if (has_v || has_g) {
                 const long long idx = node + c * P.N;
-                const int target = (od.cmap && !free_cell) ? od.cmap[idx] : (int)idx;
+                const int target = od.cmap ? od.cmap[idx] : (int)idx;
                 if (target >= 0) atomicAdd(static_cast<number*>(od.acc) + target, r);
               }
             }

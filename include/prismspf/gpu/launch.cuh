@@ -53,14 +53,35 @@ cudaError_t launch_cell_kernel_impl(const CellLaunch& P, const void* obj, size_t
   return cudaGetLastError();
 }
 
-// PPF_CELL_KERNEL=warp runs FP64 Q1/Q2 RHS and LHS launches on the warp-resident alternative
-// (cell_kernel_warp.cuh) instead of cell_kernel's thread-block tiles
-inline bool use_warp_cell_kernel() {
-  static const int on = [] {
+// An operator may run its FP64 Q1/Q2 left-hand side on the warp-resident kernel
+// (cell_kernel_warp.cuh) through `static constexpr bool cell_warp_lhs = true`; everything else
+// runs cell_kernel's thread-block tiles.
+template <class PDE, class = void>
+struct CellWarpLhs {
+  static constexpr bool value = false;
+};
+template <class PDE>
+struct CellWarpLhs<PDE, std::void_t<decltype(PDE::cell_warp_lhs)>> {
+  static constexpr bool value = PDE::cell_warp_lhs;
+};
+
+// PPF_CELL_KERNEL=warp runs every FP64 Q1/Q2 RHS and LHS launch on the warp-resident kernel,
+// PPF_CELL_KERNEL=block none; otherwise the operator's choice (0 operator, 1 warp, 2 block)
+inline int cell_kernel_override() {
+  static const int v = [] {
     const char* e = std::getenv("PPF_CELL_KERNEL");
-    return (e && std::strcmp(e, "warp") == 0) ? 1 : 0;
+    if (e && std::strcmp(e, "warp") == 0) return 1;
+    if (e && std::strcmp(e, "block") == 0) return 2;
+    return 0;
   }();
-  return on != 0;
+  return v;
+}
+
+template <class PDE, int mode>
+inline bool use_warp_cell_kernel() {
+  const int o = cell_kernel_override();
+  if (o) return o == 1;
+  return mode == MODE_LHS && CellWarpLhs<PDE>::value;
 }
 
 // launches the instantiation with the fixed-point integration path only when the launch asks
@@ -68,7 +89,7 @@ inline bool use_warp_cell_kernel() {
 template <class PDE, int dim, int degree, int mode, typename number>
 cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
   if constexpr (cell_fx_capable<dim, degree, number>() && mode != MODE_DIAG) {
-    if (use_warp_cell_kernel() && smem >= cell_warp_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out)) {
+    if (use_warp_cell_kernel<PDE, mode>() && smem >= cell_warp_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out)) {
       if (P.fx_int) return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, true>(P, obj, smem, s);
       return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, false>(P, obj, smem, s);
     }

@@ -30,8 +30,6 @@ struct FieldState {
   std::vector<double> h_dvals;
   std::vector<long long> h_drow;  // position (component-major lattice index) of Dirichlet row j
   bool constrained = false;
-  // lattice faces (bit 2d lower, 2d+1 upper face of axis d) without a constrained node
-  int free_faces = 0;
   ppf_field_desc desc;
   // host destination the field is streamed to after every increment (ppf_set_output_stream)
   double* stream_out = nullptr;
@@ -79,7 +77,6 @@ struct MGLevel {
   int precision = 0;            // 0 FP64, 1 FP32
   int* cmap = nullptr;          // homogeneous level constraints
   bool constrained = false;
-  int free_faces = 0;           // faces without a constrained node (CellLaunch::free_faces)
   void* invm_sqrt = nullptr;    // per node, level precision
   void* inv_diag = nullptr;     // len, level precision
   void* tables = nullptr;       // CellTables for the LHS (level precision)

@@ -444,7 +444,6 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   L.timer = h->timer;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
-  L.free_faces = lv.free_faces;
   // integer contractions where the level's tables allow them (FP64 Q1/Q2); the mode is timed
   // online over the level's first plain LHS launches, so choosing costs no extra launches
   int slot = -1;
@@ -793,12 +792,6 @@ static int init_linear(ppf_handle h, int b) {
           any_constraint = true;
         }
     lv.constrained = any_constraint;
-    // the level map constrains exactly the upper faces of periodic axes and the Dirichlet faces
-    // (level_cmap_kernel); every other face is free of constraints
-    lv.free_faces = 0x3f;
-    for (int d = 0; d < h->dim; ++d)
-      if (geom.periodic[d]) lv.free_faces &= ~(1 << (2 * d + 1));
-    for (int c = 0; c < F.ncomp; ++c) lv.free_faces &= ~(int)dmask[c];
     PPF_CUDA(h, cudaMalloc(&lv.cmap, sizeof(int) * std::max<long long>(1, lv.len)));
     level_cmap_kernel<<<grid_for(lv.len), 256, 0, h->stream>>>(lv.cmap, geom, F.ncomp, dmask[0], dmask[1], dmask[2]);
     level_cmap_close_kernel<<<grid_for(lv.len), 256, 0, h->stream>>>(lv.cmap, lv.len);

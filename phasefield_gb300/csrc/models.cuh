@@ -97,7 +97,9 @@ struct Eshelby {
   using VectorGrad = dealii::Tensor<2, dim, ScalarValue>;
   // register budget of the FP32 operator (the multigrid smoothing levels)
   static constexpr int cell_min_blocks = std::is_same_v<number, float> ? PPF_ESHELBY_F32_MIN_BLOCKS : 1;
-  // the FP64 warp-resident kernel (Voigt stress of a 3x3 gradient): 64 registers, no spill
+  // the FP64 left-hand side runs on the warp-resident kernel (measured: the 64^3 Q2 GMG-CG
+  // iterations 282 ms against 307 ms on the thread-block tiles), 64 registers, no spill
+  static constexpr bool cell_warp_lhs = true;
   static constexpr int cell_warp_min_blocks = 4;
   static constexpr unsigned int nv = Mechanics::voigt_tensor_size<dim>;
   dealii::Tensor<2, nv, number> stiffness;

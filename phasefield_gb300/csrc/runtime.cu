@@ -413,15 +413,6 @@ static void build_constraints(ppf_handle h, FieldState& F, const ppf_field_desc&
     if (m >= 0 && m != (int)gi && F.h_cmap[m] < 0) F.h_cmap[gi] = F.h_cmap[m];
   }
   F.constrained = any;
-  // faces whose nodes are all free in every component (the kernels skip the map there)
-  F.free_faces = 0x3f;
-  for (int b = 0; b < 2 * h->dim; ++b)
-    for (int c = 0; c < F.ncomp && ((F.free_faces >> b) & 1); ++c)
-      for (long long i = 0; i < N; ++i)
-        if (node_on_boundary(h, i, b) && F.h_cmap[c * N + i] != (int)(c * N + i)) {
-          F.free_faces &= ~(1 << b);
-          break;
-        }
 }
 
 static void build_invm(ppf_handle h) {
@@ -678,12 +669,6 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   L.tables = P.d_tables;
   L.timer = h->timer;
   L.timer_dev = h->capturing ? h->d_timer : nullptr;
-  // faces free of constraints in every map this launch reads (constrained src, condensed outputs)
-  L.free_faces = 0x3f;
-  for (int s = 0; s < P.nslots; ++s)
-    if (L.slots[s].constrained_read) L.free_faces &= h->fields[P.slot_field[s]].free_faces;
-  for (int i = 0; i < B.desc.n_fields; ++i)
-    if (L.outs[i].cmap) L.free_faces &= h->fields[B.desc.field_indices[i]].free_faces;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
   // adaptive meshes: integer derivatives with every level's tables, FP64 integration
