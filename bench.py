@@ -441,7 +441,8 @@ def run_ours(args):
     cell_n, all_n = C.c_longlong(), C.c_longlong()
     lib.ppf_kernel_stats(p.h, C.byref(cell_ms), C.byref(cell_n), C.byref(all_n))
     lib.ppf_kernel_timing(p.h, 0)
-    # 0 FP64 contractions, 1 fixed-point derivatives + FP64 integration, 2 both fixed point
+    # 0 FP64 contractions, 1 fixed-point derivatives + FP64 integration, 2 both fixed point,
+    # 3 FP64 derivatives + fixed-point integration, 4 the lane kernel (all in fixed point)
     modes = {"c_block": p.contraction_mode(0, 0), "mu_block": p.contraction_mode(1, 0)}
     from phasefield_gb300 import replicas
     max_ms, dof_updates = replicas.aggregate(total_ms, 2 * N * args.steps, dist if ws > 1 else None, dev)

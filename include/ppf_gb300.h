@@ -456,9 +456,11 @@ int ppf_kernel_stats_reset(ppf_handle h);
 /* Contraction arithmetic of block b's operator (which: 0 rhs, 1 lhs) on a uniform mesh:
  * *mode = 0 FP64 contractions (degrees 3-4, or PPF_FP64_CONTRACTIONS=1), 1 exact fixed-point
  * derivatives with FP64 integration, 2 fixed-point derivatives and integration, 3 FP64
- * derivatives with fixed-point integration, -1 not chosen yet (the first plain launch of an
- * explicit right-hand side or of a left-hand side times 1, 2 and 3 and keeps the fastest; a
- * linear or Newton right-hand side takes 1; PPF_CONTRACTION_MODE=1/2/3 fixes the mode).
+ * derivatives with fixed-point integration, 4 the lane kernel (cubic cells: derivatives,
+ * integration and value terms all in fixed point, one cell per lane), -1 not chosen yet (the
+ * first plain launch of an explicit right-hand side or of a left-hand side times 1, 2, 3 and,
+ * on cubic cells, 4 and keeps the fastest; a linear or Newton right-hand side takes 4 on cubic
+ * cells, else 1; PPF_CONTRACTION_MODE=1-4 fixes the mode, 4 falling back to 1 on other cells).
  * Engine-side only: the reference contracts in FP64 (fe_evaluation sum factorisation). */
 int ppf_contraction_mode(ppf_handle h, int b, int which, int* mode);
 

@@ -69,6 +69,15 @@ struct CellTables {
   int dk[3];
   unsigned long long isig[3];     // c_d = detJ / (h_d W^dim), W = 2 (Q1) or 6 (Q2): isig / 2^63 * 2^ik
   int ik[3];
+  // the lane kernel (prismspf/gpu/cell_kernel_lanes.cuh, cubic cells): value terms are integrated
+  // in fixed point as h v next to the gradient terms, with the weight 2^vw_sh[q] = prod_e w_int(q_e)
+  // and h = hsig / 2^63 * 2^hk (hpow2: h is a power of two); dpow2[d]: 1/h_d is a power of two
+  int fx_lanes;
+  int hpow2;
+  int hk;
+  int dpow2[3];
+  unsigned long long hsig;
+  signed char vw_sh[nq];
 };
 
 template <int dim, int degree, typename number = double>
@@ -89,6 +98,13 @@ struct CellCtx {
   const long long* vals_fx = nullptr;
   const int* ex_in = nullptr;
   int cpb = 0;
+  // Row layout: point q of the thread's cell sits at lc * nq + q, or at q * cpt + lc when cpt > 0
+  // (the lane kernel, prismspf/gpu/cell_kernel_lanes.cuh). lean: the lane kernel's all-integer
+  // contractions (value terms stored unweighted, derivatives rounded by to_double_fast), with the
+  // point's index along each direction in qi.
+  int cpt = 0;
+  int lean = 0;
+  int qi[3] = {0, 0, 0};
 };
 
 }  // namespace gpu
@@ -297,14 +313,15 @@ class FieldContainer {
   PPF_HD void set_value_term(unsigned int field_index, const ScalarValue& val) {
     const int o = out_row(field_index);
     if (o < 0) return;
-    ctx.outs[o * ctx.stride + slot()] = val.v * ctx.tab->jxw[ctx.q];
+    ctx.outs[o * ctx.stride + slot()] = ctx.lean ? val.v : val.v * ctx.tab->jxw[ctx.q];
     ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
   }
 
   PPF_HD void set_value_term(unsigned int field_index, const dealii::Tensor<1, dim, ScalarValue>& val) {
     const int o = out_row(field_index);
     if (o < 0) return;
-    for (int c = 0; c < int(dim); ++c) ctx.outs[(o + c * (1 + dim)) * ctx.stride + slot()] = val[c].v * ctx.tab->jxw[ctx.q];
+    for (int c = 0; c < int(dim); ++c)
+      ctx.outs[(o + c * (1 + dim)) * ctx.stride + slot()] = ctx.lean ? val[c].v : val[c].v * ctx.tab->jxw[ctx.q];
     ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
   }
 
@@ -332,7 +349,9 @@ class FieldContainer {
  private:
   Ctx& ctx;
 
-  PPF_HD int slot() const { return ctx.lc * int(dofs_per_component) + ctx.q; }
+  // offset of point p of this thread's cell within a row
+  PPF_HD int pt(int p) const { return ctx.cpt ? p * ctx.cpt + ctx.lc : ctx.lc * int(dofs_per_component) + p; }
+  PPF_HD int slot() const { return pt(ctx.q); }
 
   PPF_HD int row_of(unsigned int field_index, DependencyType type) const {
     const int age = gpu::age_of(type);
@@ -358,16 +377,40 @@ class FieldContainer {
     return ctx.tab->out_row0[o];
   }
 
-  PPF_HD number nodal(int row, int q) const { return ctx.vals[row * ctx.stride + ctx.lc * int(dofs_per_component) + q]; }
+  PPF_HD number nodal(int row, int q) const { return ctx.vals[row * ctx.stride + pt(q)]; }
 
   // first derivative along direction d at this thread's quadrature point
   PPF_HD number deriv(int row, int d) const {
     int stride_d = 1;
     for (int e = 0; e < d; ++e) stride_d *= n;
+    if constexpr (std::is_same<number, double>::value && degree <= 2) {
+      if (ctx.lean && ((ctx.tab->fx_rows >> row) & 1u)) {
+        // the lane kernel (rows read as gradients have a fixed-point copy; the test is uniform):
+        // the line's fixed-point values at a point stride of cpt, the exact sum for this point's
+        // position qd on the line, rounded once with 1/h_d folded in; NaN for a cell holding a
+        // non-finite value (block exponent 2047)
+        const int qd = ctx.qi[d];
+        const int E = ctx.ex_in[row * ctx.cpb + ctx.lc];
+        const int sq = stride_d * ctx.cpt;
+        const long long* u = ctx.vals_fx + row * ctx.stride + (ctx.q - qd * stride_d) * ctx.cpt + ctx.lc;
+        long long s;
+        if constexpr (n == 2) {
+          s = u[sq] - u[0];
+        } else {
+          const long long u0 = u[0], u2 = u[2 * sq];
+          const long long a = u2 - u0;
+          const long long b = (u0 + u2 - (u[sq] << 1)) << 1;
+          s = qd == 1 ? a : (qd == 0 ? a - b : a + b);
+        }
+        const double g = gpu::fx::to_double_fast(s, E - 1023 - gpu::fx::TOP_VALUES + ctx.tab->dk[d],
+                                                 ctx.tab->dsig[d], ctx.tab->dpow2[d] == 0);
+        return E == gpu::fx::EXP_NONFINITE ? gpu::fx::quiet_nan() : g;
+      }
+    }
     const int qd = (ctx.q / stride_d) % n;
     const int base = row * ctx.stride + ctx.lc * int(dofs_per_component) + (ctx.q - qd * stride_d);
     if constexpr (std::is_same<number, double>::value && degree <= 2) {
-      if (ctx.vals_fx) {
+      if (ctx.vals_fx && !ctx.lean) {
         // exact integer sum of the line's fixed-point values, rounded once (1/h_d folded in)
         const int E = ctx.ex_in[row * ctx.cpb + ctx.lc];
         if (E == gpu::fx::EXP_NONFINITE) return gpu::fx::quiet_nan();
@@ -380,8 +423,17 @@ class FieldContainer {
         // a row declared without gradients has no fixed-point copy (exponent -1)
       }
     }
-    const number* u = ctx.vals + base;
+    // FP64 contraction over the nodal values
+    const int q0 = ctx.q - qd * stride_d;
     const number* Dr = ctx.tab->Dh[d][qd];
+    if (ctx.cpt) {
+      const number* u = ctx.vals + row * ctx.stride + q0 * ctx.cpt + ctx.lc;
+      number s = Dr[0] * u[0];
+#pragma unroll
+      for (int j = 1; j < n; ++j) s = fma(Dr[j], u[j * stride_d * ctx.cpt], s);
+      return s;
+    }
+    const number* u = ctx.vals + base;
     number s = Dr[0] * u[0];
 #pragma unroll
     for (int j = 1; j < n; ++j) s = fma(Dr[j], u[j * stride_d], s);
@@ -394,19 +446,19 @@ class FieldContainer {
     for (int k = 0; k < d; ++k) sd *= n;
     for (int k = 0; k < e; ++k) se *= n;
     const int qd = (ctx.q / sd) % n, qe = (ctx.q / se) % n;
-    const number* base = ctx.vals + row * ctx.stride + ctx.lc * int(dofs_per_component);
+    const number* base = ctx.vals + row * ctx.stride;
     if (d == e) {
-      const number* u = base + (ctx.q - qd * sd);
+      const int q0 = ctx.q - qd * sd;
       const number* Dr = ctx.tab->D2h[d][qd];
       number s = 0;
-      for (int j = 0; j < n; ++j) s = fma(Dr[j], u[j * sd], s);
+      for (int j = 0; j < n; ++j) s = fma(Dr[j], base[pt(q0 + j * sd)], s);
       return s;
     }
-    const number* u = base + (ctx.q - qd * sd - qe * se);
+    const int q0 = ctx.q - qd * sd - qe * se;
     number s = 0;
     for (int j = 0; j < n; ++j) {
       number t = 0;
-      for (int k = 0; k < n; ++k) t = fma(ctx.tab->Dh[e][qe][k], u[j * sd + k * se], t);
+      for (int k = 0; k < n; ++k) t = fma(ctx.tab->Dh[e][qe][k], base[pt(q0 + j * sd + k * se)], t);
       s = fma(ctx.tab->Dh[d][qd][j], t, s);
     }
     return s;

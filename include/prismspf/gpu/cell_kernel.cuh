@@ -103,6 +103,11 @@ struct CellLaunch {
   // (else FP64 from the nodal values), fx_int integrates in fixed point (else FP64 with jdt)
   int fx_deriv;
   int fx_int;
+  // the lane kernel (prismspf/gpu/cell_kernel_lanes.cuh): all-integer contractions of an FP64
+  // Q1/Q2 operator on cubic cells, when the tables allow it (fx_lanes); it takes the host copy
+  // of `tables` (tables_host) as a kernel parameter
+  int fx_lanes;
+  const void* tables_host;
 };
 
 template <int dim, int degree>

@@ -1,0 +1,411 @@
+// Lane kernel: the cell loop of an FP64 Q1/Q2 operator on cubic cells with every contraction in
+// exact 64-bit integers, laid out so that one lane of a warp is one cell.
+//
+// The same per-cell work as cell_kernel (MFOperator::compute_local_operator,
+// src/solvers/mf_operator.cc:34-80, with FieldContainer::reinit_and_eval /
+// integrate_and_distribute, include/prismspf/core/field_container.h:794-882): gather ->
+// user callback per quadrature point -> integrate -> condensed scatter. The layout and the
+// arithmetic differ:
+//   * a thread block owns a tile of CPT cells (32, or 16 when an operator asks for it); lane
+//     l of every warp is cell l of the tile, and the warps take the quadrature points in turn
+//     (CPT = 32: warp w is point w of every cell). Rows of shared memory are [point][cell], so a
+//     point's line neighbours are whole warps' rows away and every access is a contiguous warp
+//     row; the per-cell block exponents are shared-memory atomics on CPT distinct words (no
+//     conflicts), and a point's position on its lines is uniform across the warp;
+//   * derivatives: exact integer line sums of the nodal values' fixed-point copies, rounded
+//     once by to_double_fast (prismspf/gpu/fixed_point.cuh) with 1/h_d folded in;
+//   * integration: the submitted value term (as h v) and gradient terms of a cell and output
+//     component share one block exponent; every node's integral is the exact integer sum
+//     2^vw(q) X(q) + sum_d 2^wo_d(q) L_d(q) (L_d the Gauss-Lobatto line integral of the
+//     gradient terms along d, 2^vw and 2^wo the integer quadrature weights) rounded once with the
+//     scale detJ / (h W^dim): no FP64 instruction outside the user's callback. On GB300 the FP64
+//     pipe retires about two operations per SM per clock and every FP64 conversion runs on it
+//     too, so the integer path (issue slots) replaces 9-10 FP64 operations per point.
+//   * four block barriers per tile: nodal values and exponents, fixed-point copies, submitted
+//     terms and exponents, their fixed-point copies. The value-row exponents alternate between
+//     two buffers so that clearing the next tile's needs no extra barrier.
+// Accuracy: every derivative and every node's integral is one rounding of an exact sum of
+// values quantised to 2^-58 (derivatives) or 2^-52 (integration) of the largest magnitude of
+// their cell and row, as in the other integer-contraction kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include <prismspf/gpu/cell_kernel.cuh>
+
+#pragma push_macro("compute_rhs")
+#pragma push_macro("compute_lhs")
+#undef compute_rhs
+#undef compute_lhs
+
+namespace ppf {
+
+template <int dim, int degree, int CPT>
+struct LaneShape {
+  static constexpr int n = degree + 1;
+  static constexpr int nq = pg::ipow(n, dim);
+  static constexpr int ppw = 32 / CPT;  // points per warp
+  static constexpr int warps = (nq + ppw - 1) / ppw;
+  static constexpr int threads = 32 * warps;
+};
+
+// fixed-point top of the integration: |X| <= 2^53 and |L_d| <= 8 * 2^53 keep the weighted sum
+// below 2^53 (2^6 + 3 * 2^4 * 8) < 2^62
+constexpr int LANE_TOP_TERMS = 52;
+
+// An operator may ask for 16 cells per tile (`static constexpr int cell_lane_cpt = 16`), which
+// halves the shared memory of a tile for operators with many rows, and for a register budget
+// (`cell_lane_min_blocks`, resident blocks per SM).
+template <class PDE, class = void>
+struct CellLaneCpt {
+  static constexpr int value = 32;
+};
+template <class PDE>
+struct CellLaneCpt<PDE, std::void_t<decltype(PDE::cell_lane_cpt)>> {
+  static constexpr int value = PDE::cell_lane_cpt;
+};
+template <class PDE, int threads, class = void>
+struct CellLaneMinBlocks {
+  static constexpr int value = 2048 / threads > 0 ? 2048 / threads : 1;
+};
+template <class PDE, int threads>
+struct CellLaneMinBlocks<PDE, threads, std::void_t<decltype(PDE::cell_lane_min_blocks)>> {
+  static constexpr int value = PDE::cell_lane_min_blocks;
+};
+
+// shared memory of a tile: nodal values and their fixed-point copies (nrows_in rows each), the
+// submitted terms (nrows_out rows), then the block exponents
+template <int dim, int degree, int CPT>
+__host__ __device__ constexpr size_t lane_smem_bytes(int nrows_in, int nrows_out) {
+  using S = LaneShape<dim, degree, CPT>;
+  return (size_t)S::nq * CPT * 8 * (size_t)(2 * nrows_in + nrows_out) + 4 * (size_t)CPT * (size_t)(2 * nrows_in + nrows_out);
+}
+
+// Gauss-Lobatto line integral of the terms g at the line's node j (line_integral of
+// fixed_point.cuh), with j uniform across a warp when CPT = 32
+template <int n>
+__device__ __forceinline__ long long lane_line_integral(int j, long long g0, long long g1, long long g2) {
+  if constexpr (n == 2) {
+    const long long s = g0 + g1;
+    return j == 0 ? -s : s;
+  } else {
+    const long long A = g2 - g0;
+    if (j == 1) return A * -4;
+    const long long B = g0 + g2 + g1 * 4;
+    return j == 0 ? A * 2 - B : A * 2 + B;
+  }
+}
+
+// The rows of one launch as flat lists (built on the host from the launch record): input rows
+// (one per component of each dependency slot) and output components (one per component of each
+// block field, with its value row and dim gradient rows).
+constexpr int LANE_MAX_IN = 6;
+constexpr int LANE_MAX_OUT = 3;
+struct LaneRows {
+  int nin;
+  int nout;
+  unsigned int div_m[2], div_l[2];       // cell index -> (x, y, z): multiply-high divisors of nc[0], nc[1]
+  const double* in_base[LANE_MAX_IN];    // vector of the row's slot
+  const int* in_cmap[LANE_MAX_IN];       // constraint map for a constrained read, else null
+  unsigned int in_off[LANE_MAX_IN];      // component offset c * N
+  double* out_acc[LANE_MAX_OUT];         // accumulator of the output's field
+  const int* out_cmap[LANE_MAX_OUT];     // condensation map, else null
+  unsigned int out_off[LANE_MAX_OUT];    // component offset c * N
+  int out_row[LANE_MAX_OUT];             // value row of the component (dim gradient rows follow)
+};
+
+template <class PDE, int dim, int degree, int MODE, int CPT, int MINB>
+__global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
+    cell_kernel_lanes(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde,
+                      const __grid_constant__ pg::CellTables<dim, degree, double> T,
+                      const __grid_constant__ LaneRows R) {
+  static_assert(degree <= 2 && MODE != MODE_DIAG, "the lane kernel covers FP64 Q1/Q2 RHS and LHS launches");
+  static_assert(CPT == 32 || CPT == 16, "16 or 32 cells per tile");
+  using S = LaneShape<dim, degree, CPT>;
+  using Tab = pg::CellTables<dim, degree, double>;
+  namespace fx = pg::fx;
+  constexpr int n = S::n, nq = S::nq, k = degree;
+  constexpr int ROW = nq * CPT;  // entries of one row
+  constexpr int TOPT = LANE_TOP_TERMS;
+  constexpr bool ALL_Q = S::warps * S::ppw == nq;  // every thread holds a quadrature point
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the tables are a kernel parameter: read-only constant-bank loads, uniform where their index is
+  const Tab* tab = &T;
+  double* vals = reinterpret_cast<double*>(smem_raw);                // [nin][q][cell]
+  long long* vfx = reinterpret_cast<long long*>(vals + R.nin * ROW);  // [nin][q][cell]
+  double* outs = reinterpret_cast<double*>(vfx + R.nin * ROW);       // [out rows][q][cell]
+  const int nrows_out = R.nout * (1 + dim);
+  int* ex_in = reinterpret_cast<int*>(outs + nrows_out * ROW);       // [2][nin][cell]
+  int* ex_out = ex_in + 2 * R.nin * CPT;                             // [nout][cell]
+
+  const int t = threadIdx.x;
+  const int lane = t & 31;
+  const int lc = lane & (CPT - 1);
+  const int q = (t >> 5) * S::ppw + lane / CPT;
+  const bool qv = ALL_Q || q < nq;
+  const int qs = qv ? q : 0;  // a point to address with (threads past the last point mirror point 0)
+  const int p = qs * CPT + lc;  // this thread's entry in a row
+  const int qa = qs % n;
+  const int qb = dim > 1 ? (qs / n) % n : 0;
+  const int qc = dim > 2 ? qs / (n * n) : 0;
+  const unsigned int fx_rows = tab->fx_rows;  // input rows read as gradients (fixed-point copies)
+  const int hpow2 = tab->hpow2, hk = tab->hk;
+  const unsigned long long hsig = tab->hsig;
+  // both exponent buffers: 0 for rows with a fixed-point copy, -1 for rows read as values only
+  for (int i = t; i < 2 * R.nin * CPT; i += S::threads) ex_in[i] = ((fx_rows >> ((i / CPT) % R.nin)) & 1u) ? 0 : -1;
+  const unsigned int nn0 = (unsigned int)P.nn[0], nn1 = (unsigned int)P.nn[1];
+  const unsigned int ncells = (unsigned int)P.ncells;
+  const unsigned int ntiles = (ncells + CPT - 1) / CPT;
+  const int qi[3] = {qa, qb, qc};
+  __syncthreads();  // exponent buffers set
+
+  int par = 0;
+  for (unsigned int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, par ^= 1) {
+    int* exi = ex_in + par * R.nin * CPT;
+    int* exn = ex_in + (par ^ 1) * R.nin * CPT;
+    // lanes past the last cell redo the last cell and skip its scatter
+    const unsigned int cell_t = tile * CPT + lc;
+    const bool active = qv && cell_t < ncells;
+    const unsigned int cell = cell_t < ncells ? cell_t : ncells - 1;
+    int cx, cy = 0, cz = 0;
+    {
+      const unsigned int q0 = (__umulhi(cell, R.div_m[0]) + cell) >> R.div_l[0];
+      cx = (int)(cell - q0 * (unsigned int)P.nc[0]);
+      if (dim == 2) cy = (int)q0;
+      if (dim > 2) {
+        const unsigned int q1 = (__umulhi(q0, R.div_m[1]) + q0) >> R.div_l[1];
+        cy = (int)(q0 - q1 * (unsigned int)P.nc[1]);
+        cz = (int)q1;
+      }
+    }
+    const unsigned int node =
+        ((unsigned int)(k * cz + qc) * nn1 + (unsigned int)(k * cy + qb)) * nn0 + (unsigned int)(k * cx + qa);
+
+    // gather (read_dof_values_plain, or read_dof_values for a constrained src) and the block
+    // exponents of the rows read as gradients
+#pragma unroll
+    for (int r = 0; r < LANE_MAX_IN; ++r) {
+      if (r < R.nin) {
+        const double* base = R.in_base[r];
+        const unsigned int idx = node + R.in_off[r];
+        double v;
+        if (R.in_cmap[r]) {
+          const int m = __ldg(R.in_cmap[r] + idx);
+          const double own = __ldg(base + idx);
+          v = m == (int)idx ? own : (m >= 0 ? __ldg(base + m) : 0.0);
+        } else {
+          v = __ldg(base + idx);
+        }
+        if (qv) vals[r * ROW + p] = v;
+        if (((fx_rows >> r) & 1u) && qv) atomicMax(&exi[r * CPT + lc], fx::exponent(v));
+      }
+    }
+    __syncthreads();  // nodal values and their block exponents complete
+
+    // fixed-point copies; clear the submitted terms, their exponents and the next tile's
+    // value-row exponents
+#pragma unroll
+    for (int r = 0; r < LANE_MAX_IN; ++r) {
+      if (r < R.nin && ((fx_rows >> r) & 1u)) {
+        const int E = exi[r * CPT + lc];
+        const long long x = fx::to_fixed_fast<fx::TOP_VALUES>(vals[r * ROW + p], E);
+        if (qv) vfx[r * ROW + p] = E == fx::EXP_NONFINITE ? 0ll : x;
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o)
+      if (o < R.nout && qv)
+#pragma unroll
+        for (int j = 0; j <= dim; ++j) outs[(R.out_row[o] + j) * ROW + p] = 0.0;
+    for (int i = t; i < R.nin * CPT; i += S::threads) exn[i] = ((fx_rows >> (i / CPT)) & 1u) ? 0 : -1;
+    for (int i = t; i < R.nout * CPT; i += S::threads) ex_out[i] = 0;
+    __syncthreads();  // fixed-point copies visible
+
+    pg::CellCtx<dim, degree, double> ctx;
+    ctx.tab = tab;
+    ctx.vals = vals;
+    ctx.outs = outs;
+    ctx.stride = ROW;
+    ctx.lc = lc;
+    ctx.q = qs;
+    ctx.cell[0] = cx;
+    ctx.cell[1] = cy;
+    ctx.cell[2] = cz;
+    ctx.err = P.err;
+    ctx.submitted = 0;
+    ctx.vals_fx = vfx;
+    ctx.ex_in = exi;
+    ctx.cpb = CPT;
+    ctx.cpt = CPT;
+    ctx.lean = 1;
+    ctx.qi[0] = qa;
+    ctx.qi[1] = qb;
+    ctx.qi[2] = qc;
+    if (qv) {
+      FieldContainer<dim, degree, double> fc(ctx);
+      // the clock from the launch record, or from device memory during graph replays
+      const SimulationTimer& timer = P.timer_dev ? *P.timer_dev : P.timer;
+      if constexpr (MODE == MODE_LHS) pde.compute_lhs(fc, timer, P.block_id);
+      else pde.compute_rhs(fc, timer, P.block_id);
+    }
+    // block exponents of every output component's terms (rows the callback left are zero): the
+    // value term enters as h v (one binade more when h is not a power of two)
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o) {
+      if (o < R.nout) {
+        const int rv = R.out_row[o];
+        const int ev = fx::exponent(outs[rv * ROW + p]);
+        const int eh = ev + hk + (hpow2 ? 0 : 1);
+        int e = ev == 0 ? 0 : (ev == fx::EXP_NONFINITE || eh >= fx::EXP_NONFINITE ? fx::EXP_NONFINITE : max(eh, 0));
+#pragma unroll
+        for (int d = 0; d < dim; ++d) e = max(e, fx::exponent(outs[(rv + 1 + d) * ROW + p]));
+        if (qv) atomicMax(&ex_out[o * CPT + lc], e);
+      }
+    }
+    __syncthreads();  // submitted terms and their block exponents complete
+
+    // the submitted terms in place to fixed point
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o) {
+      if (o < R.nout) {
+        const int rv = R.out_row[o];
+        const int E = ex_out[o * CPT + lc];
+        const bool nf = E == fx::EXP_NONFINITE;
+        double* vp = outs + rv * ROW + p;
+        const double v = *vp;
+        const long long xv = hpow2 ? fx::to_fixed_fast<TOPT>(v, E - hk) : fx::to_fixed_scaled<TOPT>(v, E, hsig, hk);
+        long long xg[dim];
+#pragma unroll
+        for (int d = 0; d < dim; ++d) xg[d] = fx::to_fixed_fast<TOPT>(outs[(rv + 1 + d) * ROW + p], E);
+        if (qv) {
+          *reinterpret_cast<long long*>(vp) = nf ? 0ll : xv;
+#pragma unroll
+          for (int d = 0; d < dim; ++d) reinterpret_cast<long long*>(outs)[(rv + 1 + d) * ROW + p] = nf ? 0ll : xg[d];
+        }
+      }
+    }
+    __syncthreads();  // fixed-point terms visible
+
+    // integrate and scatter (distribute_local_to_global through the constraint map)
+    const long long* ox = reinterpret_cast<const long long*>(outs);
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o) {
+      if (o < R.nout) {
+        const int rv = R.out_row[o];
+        const int E = ex_out[o * CPT + lc];
+        // this point's integration weights: powers of two from the tables
+        long long Tx = (long long)((unsigned long long)ox[rv * ROW + p] << tab->vw_sh[qs]);
+#pragma unroll
+        for (int d = 0; d < dim; ++d) {
+          const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+          const long long* g = ox + (rv + 1 + d) * ROW + (qs - qi[d] * sd) * CPT + lc;
+          const long long L = lane_line_integral<n>(qi[d], g[0], g[sd * CPT], n > 2 ? g[2 * sd * CPT] : 0ll);
+          Tx += (long long)((unsigned long long)L << tab->wo_sh[d][qs]);
+        }
+        const double rr = fx::to_double_fast(Tx, E - 1023 - TOPT + tab->ik[0], tab->isig[0], true);
+        const double r = E == fx::EXP_NONFINITE ? fx::quiet_nan() : rr;
+        const unsigned int idx = node + R.out_off[o];
+        const int target = R.out_cmap[o] ? __ldg(R.out_cmap[o] + idx) : (int)idx;
+        if (active && target >= 0) atomicAdd(R.out_acc[o] + target, r);
+      }
+    }
+  }
+}
+
+template <class PDE, int dim, int degree>
+constexpr int lane_cpt() {
+  return CellLaneCpt<PDE>::value;
+}
+
+// the flat row lists of a launch record; false when they exceed the lane kernel's limits
+inline bool lane_rows(const CellLaunch& P, int dim, LaneRows* R) {
+  std::memset(R, 0, sizeof(*R));
+  int r = 0;
+  for (int s = 0; s < P.nslots; ++s) {
+    const SlotDesc& sd = P.slots[s];
+    for (int c = 0; c < sd.ncomp; ++c, ++r) {
+      if (r >= LANE_MAX_IN) return false;
+      R->in_base[r] = static_cast<const double*>(sd.ptr);
+      R->in_cmap[r] = sd.constrained_read ? sd.cmap : nullptr;
+      R->in_off[r] = (unsigned int)(c * P.N);
+    }
+  }
+  R->nin = r;
+  if (r != P.nrows_in) return false;
+  int o = 0, row = 0;
+  for (int i = 0; i < P.nout; ++i) {
+    const OutDesc& od = P.outs[i];
+    for (int c = 0; c < od.ncomp; ++c, ++o) {
+      if (o >= LANE_MAX_OUT) return false;
+      R->out_acc[o] = static_cast<double*>(od.acc);
+      R->out_cmap[o] = od.cmap;
+      R->out_off[o] = (unsigned int)(c * P.N);
+      R->out_row[o] = row;
+      row += 1 + dim;
+    }
+  }
+  R->nout = o;
+  for (int d = 0; d < 2; ++d) {
+    pg::fx::FastDiv f;
+    f.init((unsigned int)P.nc[d]);
+    R->div_m[d] = f.m;
+    R->div_l[d] = f.l;
+  }
+  return row == P.nrows_out;
+}
+
+template <class PDE, int dim, int degree, int mode, int CPT, int MINB>
+cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj, cudaStream_t s) {
+  using S = LaneShape<dim, degree, CPT>;
+  auto kern = cell_kernel_lanes<PDE, dim, degree, mode, CPT, MINB>;
+  const size_t smem = lane_smem_bytes<dim, degree, CPT>(P.nrows_in, P.nrows_out);
+  constexpr int MAX_DEVICES = 64;
+  static size_t attr_smem_of[MAX_DEVICES] = {};
+  static int occ_of[MAX_DEVICES] = {};
+  static int sms_of[MAX_DEVICES] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  size_t& attr_smem = attr_smem_of[dev];
+  int& occ = occ_of[dev];
+  int& sms = sms_of[dev];
+  if (smem > attr_smem) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_smem = smem;
+    occ = 0;
+  }
+  if (occ == 0) {
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  const long long ntiles = (P.ncells + CPT - 1) / CPT;
+  long long grid = (long long)sms * occ;
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj),
+                                                *reinterpret_cast<const pg::CellTables<dim, degree, double>*>(P.tables_host),
+                                                R);
+  return cudaGetLastError();
+}
+
+// launches the lane kernel, or returns cudaErrorNotSupported when the launch's rows exceed its
+// limits (the caller then takes the thread-block kernel)
+template <class PDE, int dim, int degree, int mode>
+cudaError_t launch_cell_kernel_lanes_impl(const CellLaunch& P, const void* obj, cudaStream_t s) {
+  constexpr int CPT = lane_cpt<PDE, dim, degree>();
+  constexpr int MINB = CellLaneMinBlocks<PDE, LaneShape<dim, degree, CPT>::threads>::value;
+  LaneRows R;
+  if (!P.tables_host || !lane_rows(P, dim, &R) || lane_smem_bytes<dim, degree, CPT>(P.nrows_in, P.nrows_out) > 232448)
+    return cudaErrorNotSupported;
+  return launch_lanes<PDE, dim, degree, mode, CPT, MINB>(P, R, obj, s);
+}
+
+}  // namespace ppf
+
+#pragma pop_macro("compute_lhs")
+#pragma pop_macro("compute_rhs")

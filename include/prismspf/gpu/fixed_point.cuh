@@ -124,6 +124,75 @@ PPF_FX double to_double(long long x, int lsb, unsigned long long sig) {
   return double_of(s | (((unsigned long long)(be - 1) << 52) + r));
 }
 
+// The lane kernel's conversions (prismspf/gpu/cell_kernel_lanes.cuh). GB300 runs every
+// conversion instruction that touches FP64 (int64 <-> double, and float <-> double as well) on
+// its FP64 pipe, at the rate of an FP64 fused multiply-add (about two per SM per clock), so these
+// are bit operations on 32- and 64-bit integers, written for the shortest instruction sequence
+// in the common case: a normal result of a non-zero sum.
+
+// round(v * 2^(1023 + TOP - E)) for exponent(v) <= E, ties away from zero: the same value as
+// to_fixed(v, E, TOP) with one variable shift instead of two. 52 <= TOP <= 60.
+template <int TOP>
+PPF_FX long long to_fixed_fast(double v, int E) {
+  static_assert(TOP >= 52 && TOP <= 60, "fixed-point top out of range");
+  const unsigned long long b = bits_of(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  // significand with one extra bit below it, at the top position
+  const unsigned long long m2 = ((b & 0xfffffffffffffull) | (1ull << 52)) << (TOP - 51);
+#ifdef __CUDA_ARCH__
+  const int r = e == 0 ? 63 : min(E - e, 63);
+#else
+  const int r = e == 0 ? 63 : std::min(E - e, 63);
+#endif
+  const unsigned long long a = ((m2 >> r) + 1) >> 1;
+  const unsigned long long sg = (unsigned long long)((long long)b >> 63);
+  return (long long)((a ^ sg) - sg);
+}
+
+// round(v * sigma * 2^(k + 1023 + TOP - E)) for a scale sigma = sig / 2^63 in [1, 2) and
+// exponent(v) + k + 1 <= E, from the floor of the 64-bit product of the significands (off by at
+// most half a unit plus 2^-10 units). Zeros and subnormals give 0.
+template <int TOP>
+PPF_FX long long to_fixed_scaled(double v, int E, unsigned long long sig, int k) {
+  static_assert(TOP >= 52 && TOP <= 60, "fixed-point top out of range");
+  const unsigned long long b = bits_of(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  // P = floor(m * 2^11 * sig / 2^64) in [2^62, 2^64): v * sigma = P * 2^(e - 1085)
+  const unsigned long long P = mulhi64(((b & 0xfffffffffffffull) | (1ull << 52)) << 11, sig);
+  // (P >> r + 1) >> 1 with r = E - e - k + 61 - TOP >= 2, taken as (P / 2) >> (r - 1) so that
+  // the clamped shift stays below 64 for every P
+#ifdef __CUDA_ARCH__
+  const int r1 = e == 0 ? 63 : min(E - e - k + 60 - TOP, 63);
+#else
+  const int r1 = e == 0 ? 63 : std::min(E - e - k + 60 - TOP, 63);
+#endif
+  const unsigned long long a = (((P >> 1) >> r1) + 1) >> 1;
+  const unsigned long long sg = (unsigned long long)((long long)b >> 63);
+  return (long long)((a ^ sg) - sg);
+}
+
+// x * 2^lsb * sigma with sigma = sig / 2^63 in [1, 2) when `scaled` (else 1), |x| < 2^63:
+// the product's 64-bit floor (as to_double) rounded to nearest with ties away from zero, which
+// differs from to_double's ties-to-even only on exact ties; zero gives +0, results below the
+// normal range flush to a signed zero and above it become infinities (as to_double), by selects
+// rather than branches.
+PPF_FX double to_double_fast(long long x, int lsb, unsigned long long sig, bool scaled) {
+  const unsigned long long sg = (unsigned long long)(x >> 63);
+  unsigned long long a = ((unsigned long long)x ^ sg) - sg;
+  if (scaled) a = mulhi64(a << 1, sig);
+  const int lz = clz64(a);  // 64 for a == 0
+  const unsigned long long nrm = a << (lz & 63);
+  const unsigned long long r = (nrm >> 11) + ((nrm >> 10) & 1ull);  // 53 bits, or 2^53 on a carry
+  const int be1 = 1085 + lsb - lz;                                  // biased exponent - 1
+  const unsigned long long s63 = sg << 63;
+  const unsigned long long bits = s63 | (((unsigned long long)(unsigned int)be1 << 52) + r);
+  // zero, below the normal range (signed zero) or above it (signed infinity): the low word is
+  // zero and the high word sign (and exponent) only
+  const bool ok = (unsigned int)be1 < 2046u && a != 0;
+  const unsigned long long edge = a == 0 ? 0ull : (be1 < 0 ? s63 : (s63 | 0x7ff0000000000000ull));
+  return double_of(ok ? bits : edge);
+}
+
 // Gauss-Lobatto line contractions on the unit interval, exact in integers.
 // Derivative at node qd of the line values u: sum_j D[qd][j] u_j with D = {-1, 1 / -1, 1} (Q1)
 // or {-3, 4, -1 / -1, 0, 1 / 1, -4, 3} (Q2); for Q2 with a = u2 - u0 and b = 2 (u0 - 2 u1 + u2)

@@ -14,6 +14,7 @@
 
 #include <prismspf/gpu/amr_cell_kernel.cuh>
 #include <prismspf/gpu/cell_kernel.cuh>
+#include <prismspf/gpu/cell_kernel_lanes.cuh>
 #include <prismspf/gpu/cell_kernel_warp.cuh>
 
 namespace ppf {
@@ -89,6 +90,13 @@ inline bool use_warp_cell_kernel() {
 template <class PDE, int dim, int degree, int mode, typename number>
 cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
   if constexpr (cell_fx_capable<dim, degree, number>() && mode != MODE_DIAG) {
+    if (P.fx_lanes) {
+      // the lane kernel when its rows and tile fit (and the host tables came with the launch),
+      // else integer derivatives on the thread-block tiles
+      const cudaError_t e = launch_cell_kernel_lanes_impl<PDE, dim, degree, mode>(P, obj, s);
+      if (e != cudaErrorNotSupported) return e;
+      return launch_cell_kernel_impl<PDE, dim, degree, mode, number, false>(P, obj, smem, s);
+    }
     if (use_warp_cell_kernel<PDE, mode>() && smem >= cell_warp_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out)) {
       if (P.fx_int) return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, true>(P, obj, smem, s);
       return launch_cell_kernel_warp_impl<PDE, dim, degree, mode, false>(P, obj, smem, s);

@@ -52,6 +52,7 @@ struct BlockPlan {
   int slot_age[pg::MAX_SLOTS];
   int nrows_in = 0, nrows_out = 0;
   void* d_tables = nullptr;
+  std::vector<unsigned char> h_tables;  // host copy (the lane kernel takes it as a kernel parameter)
   bool valid = false;
   // the slot tables of the plan (host copies; adaptive meshes build one CellTables per level)
   signed char slot_of[pg::MAX_FIELDS][pg::NAGE];
@@ -60,8 +61,10 @@ struct BlockPlan {
   signed char out_row0[pg::MAX_OUTS];
   // integer contractions (FP64 Q1/Q2): on in the tables; arithmetic chosen for this plan
   // (-1 until the first plain launch times the modes; 1 integer derivatives + FP64
-  // integration, 2 both in integers, 3 FP64 derivatives + integer integration)
+  // integration, 2 both in integers, 3 FP64 derivatives + integer integration, 4 the lane kernel:
+  // every contraction in integers, cubic cells only)
   bool fx = false;
+  bool fx_lanes = false;
   int fx_mode = -1;
   int fx_timed = 0;                // online timing of the multigrid outer operator
   cudaEvent_t fx_ev[12] = {};

@@ -175,6 +175,21 @@ static void fixed_point_tables(pg::CellTables<dim, degree, double>& t, const GLR
   t.fx_cubic = 1;
   for (int d = 1; d < dim; ++d)
     if (t.isig[d] != t.isig[0] || t.ik[d] != t.ik[0]) t.fx_cubic = 0;
+  for (int q = 0; q < nq; ++q) {
+    int sh = 0, r = q;
+    for (int e = 0; e < dim; ++e) {
+      sh += wsh[r % n];
+      r /= n;
+    }
+    t.vw_sh[q] = (signed char)sh;
+  }
+  for (int d = 0; d < 3; ++d) t.dpow2[d] = t.dsig[d] == (1ull << 63) ? 1 : 0;
+  const pg::fx::Scale hs = pg::fx::make_scale(h[0]);
+  t.hsig = hs.sig;
+  t.hk = hs.k;
+  t.hpow2 = hs.sig == (1ull << 63) ? 1 : 0;
+  // the lane kernel integrates every direction with one scale (cubic cells)
+  t.fx_lanes = t.fx_cubic;
   t.fx = 1;
 }
 template <int dim, int degree>
@@ -287,6 +302,34 @@ static bool tables_fx(const std::vector<unsigned char>& tab, int dim, int degree
   const unsigned char* t = tab.data();
   PPF_DD_SWITCH(tables_fx_impl, t)
   return false;
+}
+template <int dim, int degree>
+static bool tables_lanes_impl(const unsigned char* tab) {
+  const auto* t = reinterpret_cast<const pg::CellTables<dim, degree, double>*>(tab);
+  return t->fx != 0 && t->fx_lanes != 0;
+}
+// whether the tables allow the lane kernel (integer contractions on cubic cells)
+bool tables_lanes(const std::vector<unsigned char>& tab, int dim, int degree) {
+  if (tab.empty()) return false;
+  const unsigned char* t = tab.data();
+  PPF_DD_SWITCH(tables_lanes_impl, t)
+  return false;
+}
+
+// the launch-record fields of a contraction mode (1-4, see BlockPlan::fx_mode)
+void set_fx_mode(CellLaunch& L, int m) {
+  L.fx_deriv = m != 3;
+  L.fx_int = m == 2 || m == 3;
+  L.fx_lanes = m == 4;
+}
+
+// PPF_CONTRACTION_MODE: a fixed contraction mode (1-4), or 0 when unset; mode 4 falls back to
+// mode 1 where the lane kernel does not apply
+int env_fx_mode(bool lanes_ok) {
+  const char* env = std::getenv("PPF_CONTRACTION_MODE");
+  if (!(env && env[0] >= '1' && env[0] <= '4' && env[1] == 0)) return 0;
+  const int m = env[0] - '0';
+  return m == 4 && !lanes_ok ? 1 : m;
 }
 
 std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
@@ -600,6 +643,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memcpy(P.out_of, out_of, sizeof(out_of));
   std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
   P.fx = tables_fx(tab, h->dim, h->k);
+  P.fx_lanes = tables_lanes(tab, h->dim, h->k);
   P.fx_mode = -1;
   P.fx_timed = 0;
   for (auto& ev : P.fx_ev)
@@ -609,6 +653,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
     }
   PPF_CUDA(h, cudaMalloc(&P.d_tables, tab.size()));
   PPF_CUDA(h, cudaMemcpy(P.d_tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+  P.h_tables = tab;
   P.valid = true;
   return PPF_OK;
 }
@@ -667,6 +712,7 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   L.nrows_in = P.nrows_in;
   L.nrows_out = P.nrows_out;
   L.tables = P.d_tables;
+  L.tables_host = P.h_tables.data();
   L.timer = h->timer;
   L.timer_dev = h->capturing ? h->d_timer : nullptr;
   L.block_id = (unsigned)B.desc.id;
@@ -679,17 +725,16 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
   if (P.fx) {
     if (P.fx_mode < 0) {
       // timing the modes pays off for plans launched every increment or iteration; the
-      // right-hand side of a linear or Newton block (once per solve) takes mode 1
-      const char* env = std::getenv("PPF_CONTRACTION_MODE");
-      if (which == 0 && B.desc.solve_type != PPF_EXPLICIT && !(env && env[0] >= '1' && env[0] <= '3')) {
-        P.fx_mode = 1;
+      // right-hand side of a linear or Newton block (once per solve) takes the lane kernel
+      // where it applies, else mode 1
+      if (which == 0 && B.desc.solve_type != PPF_EXPLICIT && !env_fx_mode(P.fx_lanes)) {
+        P.fx_mode = P.fx_lanes ? 4 : 1;
       } else {
         const int rc = choose_fx_mode(h, P, mode, L, smem);
         if (rc) return rc;
       }
     }
-    L.fx_deriv = P.fx_mode != 3;
-    L.fx_int = P.fx_mode >= 2;
+    set_fx_mode(L, P.fx_mode);
   }
   return timed_cell_launch(h, 0, mode, L, h->model_obj.data(), smem);
 }
@@ -697,45 +742,43 @@ int launch_cell(ppf_handle h, int b, int which, const double* const* src, bool p
 // The integer-contraction kernels (FP64 Q1/Q2) can take their derivatives and their integration
 // each in fixed point (issue slots) or in FP64 (the FP64 pipe). Which split is cheapest depends
 // on how much FP64 work the callback itself does, so the first plain launch of a plan times
-// modes 1 (integer derivatives, FP64 integration), 2 (both integer) and 3 (FP64 derivatives,
-// integer integration), twice each, back to back into the block's accumulators (which every
-// caller has just zeroed, and which are zeroed again afterwards), and keeps the fastest.
-// PPF_CONTRACTION_MODE=1, 2 or 3 fixes the mode; a plan first launched inside a graph capture
-// takes mode 1.
+// modes 1 (integer derivatives, FP64 integration), 2 (both integer), 3 (FP64 derivatives,
+// integer integration) and, on cubic cells, 4 (the lane kernel), twice each, back to back into
+// the block's accumulators (which every caller has just zeroed, and which are zeroed again
+// afterwards), and keeps the fastest. PPF_CONTRACTION_MODE=1-4 fixes the mode; a plan first
+// launched inside a graph capture takes mode 4 where it applies, else mode 1.
 static int choose_fx_mode(ppf_handle h, BlockPlan& P, int mode, const CellLaunch& L, size_t smem) {
-  const char* env = std::getenv("PPF_CONTRACTION_MODE");
-  if (env && env[0] >= '1' && env[0] <= '3') {
-    P.fx_mode = env[0] - '0';
+  if (const int m = env_fx_mode(P.fx_lanes)) {
+    P.fx_mode = m;
     return PPF_OK;
   }
   // no timing inside a graph capture (the engine's own, or one the caller runs on its stream)
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   PPF_CUDA(h, cudaStreamIsCapturing(h->stream, &cs));
   if (h->capturing || cs != cudaStreamCaptureStatusNone) {
-    P.fx_mode = 1;
+    P.fx_mode = P.fx_lanes ? 4 : 1;
     return PPF_OK;
   }
-  constexpr int NT = 6;  // modes 1, 2, 3, then again
-  cudaEvent_t ev[NT + 1] = {};
+  const int nm = P.fx_lanes ? 4 : 3;
+  const int NT = 2 * nm;  // every mode, then again
+  cudaEvent_t ev[9] = {};
   cudaError_t e = cudaSuccess;
   for (int i = 0; i <= NT && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
   CellLaunch T = L;
   if (e == cudaSuccess) e = cudaEventRecord(ev[0], h->stream);
   for (int r = 0; r < NT && e == cudaSuccess; ++r) {
-    const int m = 1 + r % 3;
-    T.fx_deriv = m != 3;
-    T.fx_int = m >= 2;
+    set_fx_mode(T, 1 + r % nm);
     e = h->custom_launch ? (cudaError_t)h->custom_launch(h->dim, h->k, mode, 0, &T, h->model_obj.data(), smem,
                                                          (void*)h->stream)
                          : h->model->launch(h->dim, h->k, mode, 0, T, h->model_obj.data(), smem, h->stream);
     if (e == cudaSuccess) e = cudaEventRecord(ev[r + 1], h->stream);
   }
   if (e == cudaSuccess) e = cudaEventSynchronize(ev[NT]);
-  float best[3] = {1e30f, 1e30f, 1e30f};
+  float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
   for (int r = 0; r < NT && e == cudaSuccess; ++r) {
     float ms = 0.f;
     e = cudaEventElapsedTime(&ms, ev[r], ev[r + 1]);
-    if (e == cudaSuccess && ms < best[r % 3]) best[r % 3] = ms;
+    if (e == cudaSuccess && ms < best[r % nm]) best[r % nm] = ms;
   }
   for (int i = 0; i < L.nout && e == cudaSuccess; ++i)
     e = cudaMemsetAsync(L.outs[i].acc, 0, sizeof(double) * (size_t)L.outs[i].ncomp * (size_t)L.N, h->stream);
@@ -743,7 +786,7 @@ static int choose_fx_mode(ppf_handle h, BlockPlan& P, int mode, const CellLaunch
     if (ev[i]) cudaEventDestroy(ev[i]);
   if (e != cudaSuccess) return fail(h, PPF_ERR_CUDA, std::string("contraction timing: ") + cudaGetErrorString(e));
   int m = 0;
-  for (int i = 1; i < 3; ++i)
+  for (int i = 1; i < nm; ++i)
     if (best[i] < best[m]) m = i;
   P.fx_mode = 1 + m;
   return PPF_OK;

@@ -36,5 +36,11 @@ std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
                                              const signed char* out_row0, unsigned int fx_rows = 0xffffffffu);
+// whether FP64 tables allow the lane kernel (integer contractions, cubic cells)
+bool tables_lanes(const std::vector<unsigned char>& tab, int dim, int degree);
+// the launch-record fields of contraction mode m (1-4)
+void set_fx_mode(CellLaunch& L, int m);
+// PPF_CONTRACTION_MODE (1-4, mode 4 only where the lane kernel applies, else 1), 0 when unset
+int env_fx_mode(bool lanes_ok);
 
 }  // namespace ppf

@@ -191,7 +191,8 @@ class Problem:
 
     def contraction_mode(self, block: int, which: int = 0) -> int:
         """0 FP64 contractions, 1 fixed-point derivatives with FP64 integration, 2 both in fixed
-        point, 3 FP64 derivatives with fixed-point integration, -1 not chosen yet
+        point, 3 FP64 derivatives with fixed-point integration, 4 the lane kernel (every
+        contraction and the value terms in fixed point, cubic cells), -1 not chosen yet
         (ppf_contraction_mode)."""
         m = C.c_int()
         self._check(self.lib.ppf_contraction_mode(self.h, block, which, C.byref(m)))

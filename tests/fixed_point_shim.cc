@@ -18,6 +18,20 @@ unsigned int fxs_fastdiv(unsigned int n, unsigned int d) {
   f.init(d);
   return f.div(n);
 }
+long long fxs_to_fixed_fast(double v, int E, int top) {
+  switch (top) {
+    case 52: return fx::to_fixed_fast<52>(v, E);
+    case 53: return fx::to_fixed_fast<53>(v, E);
+    case 58: return fx::to_fixed_fast<58>(v, E);
+    default: return fx::to_fixed_fast<60>(v, E);
+  }
+}
+long long fxs_to_fixed_scaled(double v, int E, unsigned long long sig, int k) {
+  return fx::to_fixed_scaled<52>(v, E, sig, k);
+}
+double fxs_to_double_fast(long long x, int lsb, unsigned long long sig, int scaled) {
+  return fx::to_double_fast(x, lsb, sig, scaled != 0);
+}
 long long fxs_line_derivative(int n, int qd, long long u0, long long u1, long long u2) {
   return n == 2 ? fx::line_derivative<2>(qd, u0, u1, u2) : fx::line_derivative<3>(qd, u0, u1, u2);
 }

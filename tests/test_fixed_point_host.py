@@ -41,6 +41,12 @@ def fx(tmp_path_factory):
         f.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_longlong]
     lib.fxs_fastdiv.restype = C.c_uint
     lib.fxs_fastdiv.argtypes = [C.c_uint, C.c_uint]
+    lib.fxs_to_fixed_fast.restype = C.c_longlong
+    lib.fxs_to_fixed_fast.argtypes = [C.c_double, C.c_int, C.c_int]
+    lib.fxs_to_fixed_scaled.restype = C.c_longlong
+    lib.fxs_to_fixed_scaled.argtypes = [C.c_double, C.c_int, C.c_ulonglong, C.c_int]
+    lib.fxs_to_double_fast.restype = C.c_double
+    lib.fxs_to_double_fast.argtypes = [C.c_longlong, C.c_int, C.c_ulonglong, C.c_int]
     return lib
 
 
@@ -202,3 +208,88 @@ def test_line_formulas_match_the_gauss_lobatto_matrices(fx):
                 g = [v >> 4 for v in u]  # integration terms sit 4 bits lower (headroom)
                 want = sum(int(Di[q][j]) * int(Wi[q]) * g[q] for q in range(n))
                 assert fx.fxs_line_integral(n, j, *g) == want
+
+
+# --- the lane kernel's conversions ----------------------------------------------------------
+
+
+def round_half_away(q: Fraction) -> int:
+    a = abs(q)
+    n = int(a)
+    if a - n >= Fraction(1, 2):
+        n += 1
+    return -n if q < 0 else n
+
+
+def test_to_fixed_fast_equals_to_fixed(fx):
+    rng = np.random.default_rng(11)
+    for _ in range(6000):
+        top = int(rng.choice([52, 53, 58, 60]))
+        v = float(rng.standard_normal() * 10.0 ** rng.integers(-300, 300))
+        e = fx.fxs_exponent(v)
+        E = e + int(rng.integers(0, 80))
+        assert fx.fxs_to_fixed_fast(v, E, top) == fx.fxs_to_fixed(v, E, top) == exact_fixed(v, E, top), (v, E, top)
+    for v in (0.0, -0.0, 5e-324, -2.2e-308, 1.0, -1.0, 0.5, 1.5, -(2.0 ** 52 + 1), 1.7976931348623157e308):
+        E = max(fx.fxs_exponent(v), 1)
+        for top in (52, 58):
+            assert fx.fxs_to_fixed_fast(v, E, top) == exact_fixed(v, E, top)
+
+
+def test_to_fixed_scaled_within_half_a_unit(fx):
+    """h v in fixed point for a scale h that is not a power of two: the significands' 64-bit
+    product floor, rounded; within half a unit plus 2^-10 of the exact value."""
+    rng = np.random.default_rng(12)
+    for _ in range(4000):
+        h = float(rng.uniform(0.001, 1000.0))
+        sig, k = scale(fx, h)
+        v = float(rng.standard_normal() * 10.0 ** rng.integers(-100, 100))
+        e = fx.fxs_exponent(v)
+        E = e + k + 1 + int(rng.integers(0, 60))
+        got = fx.fxs_to_fixed_scaled(v, E, sig, k)
+        exact = Fraction(v) * Fraction(sig, ONE) * Fraction(2) ** (k + 1023 + 52 - E)
+        assert abs(got) < 2 ** 53
+        assert abs(Fraction(got) - exact) <= Fraction(1, 2) + Fraction(1, 1024), (v, h, E)
+    for v in (0.0, -0.0, 5e-324):
+        assert fx.fxs_to_fixed_scaled(v, 1000, scale(fx, 3.0)[0], 1) == 0
+
+
+def test_to_double_fast_rounds_to_nearest(fx):
+    rng = np.random.default_rng(13)
+    for _ in range(6000):
+        bits = int(rng.integers(1, 62))
+        x = int(rng.integers(0, 2 ** 61)) >> (61 - bits)
+        if rng.random() < 0.5:
+            x = -x
+        lsb = int(rng.integers(-1150, 1000))
+        got = fx.fxs_to_double_fast(x, lsb, ONE, 0)
+        want = exact_double(x, lsb)
+        exact = Fraction(x) * Fraction(2) ** lsb
+        if x != 0 and 2.0 ** -1022 <= abs(want) < math.inf:
+            # nearest, ties away from zero (to_double breaks ties to even)
+            assert abs(Fraction(got) - exact) <= Fraction(float(np.spacing(abs(want)))) / 2, (x, lsb)
+            if Fraction(got) != exact and abs(Fraction(got) - exact) * 2 != Fraction(float(np.spacing(abs(want)))):
+                assert got == want
+        else:
+            assert got == fx.fxs_to_double(x, lsb, ONE), (x, lsb)
+    assert fx.fxs_to_double_fast(0, -60, ONE, 0) == 0.0
+    assert math.copysign(1.0, fx.fxs_to_double_fast(0, -60, ONE, 0)) == 1.0
+    # ties away from zero, carries into the exponent, both range ends
+    assert fx.fxs_to_double_fast((1 << 53) + 1, 0, ONE, 0) == float((1 << 53) + 2)
+    assert fx.fxs_to_double_fast(-((1 << 53) + 1), 0, ONE, 0) == -float((1 << 53) + 2)
+    assert fx.fxs_to_double_fast((1 << 54) - 1, 0, ONE, 0) == float(1 << 54)
+    for x, lsb in [(1, 1023), (3, 1023), ((1 << 61) - 1, 962), (1, -1022), (1, -1023), (1, -1080), (3, -1075)]:
+        assert fx.fxs_to_double_fast(x, lsb, ONE, 0) == fx.fxs_to_double(x, lsb, ONE), (x, lsb)
+
+
+def test_to_double_fast_scaled(fx):
+    rng = np.random.default_rng(14)
+    for _ in range(4000):
+        s = float(rng.uniform(0.001, 1000.0))
+        sig, k = scale(fx, s)
+        x = int(rng.integers(-(2 ** 61), 2 ** 61))
+        lsb = int(rng.integers(-200, 200))
+        got = fx.fxs_to_double_fast(x, lsb + k, sig, 1)
+        exact = Fraction(x) * Fraction(sig, ONE) * Fraction(2) ** (lsb + k)
+        want = float(exact) if exact != 0 else 0.0
+        err = abs(Fraction(got) - exact)
+        assert err <= Fraction(float(np.spacing(abs(want)))) / 2 + Fraction(2) ** (lsb + k), (x, lsb, s)

@@ -57,7 +57,7 @@ def ch_problem(dim, degree, size=None, scale_c=1.0, scale_mu=1.0, seed=3):
     return p, o
 
 
-MODES = ["1", "2", "3"]
+MODES = ["1", "2", "3", "4"]
 
 
 @pytest.mark.parametrize("mode", MODES)
@@ -83,6 +83,7 @@ def test_non_cubic_cells(gpu_lib, dim, mode):
             got = p.apply(b, 0, None, scale=1)
             ref = o.apply(b, 0, None, scale=1)
             assert rel_l2(got, ref) < APPLY_TOL, b
+            assert p.contraction_mode(b, 0) == (1 if mode == "4" else int(mode))
 
 
 @pytest.mark.parametrize("mode", MODES)
@@ -134,12 +135,13 @@ def test_fixed_point_against_fp64_contractions(gpu_lib):
     """Every mode against FP64 contractions on the same inputs."""
     outs = {}
     for key, kw in (("0", {"PPF_FP64_CONTRACTIONS": "1"}), ("1", {"PPF_CONTRACTION_MODE": "1"}),
-                    ("2", {"PPF_CONTRACTION_MODE": "2"}), ("3", {"PPF_CONTRACTION_MODE": "3"})):
+                    ("2", {"PPF_CONTRACTION_MODE": "2"}), ("3", {"PPF_CONTRACTION_MODE": "3"}),
+                    ("4", {"PPF_CONTRACTION_MODE": "4"})):
         with env(**kw):
             p, _ = ch_problem(3, 2)
             outs[key] = [p.apply(b, 0, None, scale=1) for b in (0, 1)]
             assert p.contraction_mode(0, 0) == int(key)
-    for key in ("1", "2", "3"):
+    for key in ("1", "2", "3", "4"):
         for b in (0, 1):
             assert rel_l2(outs[key][b], outs["0"][b]) < 1e-13, (key, b)
 
@@ -154,7 +156,7 @@ def test_modes_outside_the_fixed_point_path(gpu_lib):
     p = wl.make_problem()
     p.upload(0, wl.initial[0], age=1)
     p.apply(0, 0, None, scale=1)
-    assert p.contraction_mode(0, 0) in (1, 2, 3)  # chosen by timing the modes on the first launch
+    assert p.contraction_mode(0, 0) in (1, 2, 3, 4)  # chosen by timing the modes on the first launch
 
 
 @pytest.mark.parametrize("mode", MODES)
@@ -174,7 +176,7 @@ def test_nonfinite_value_reports_nan_in_every_mode(gpu_lib, mode):
         assert e.value.code == capi.PPF_ERR_NAN
 
 
-@pytest.mark.parametrize("mode", ["1", "2"])
+@pytest.mark.parametrize("mode", ["1", "2", "4"])
 def test_derivative_error_is_absolute_in_the_cell_maximum(gpu_lib, mode):
     """Per entry, a derivative taken in fixed point is exact to the block resolution of its
     cell: the absolute error is at most (sum of |D| over the line) x 2^(e - 58) / h, e the
@@ -184,7 +186,9 @@ def test_derivative_error_is_absolute_in_the_cell_maximum(gpu_lib, mode):
     the error stays within the absolute bound (a relative error of order 1e-6 of the small
     gradient itself), while FP64 contractions of the same line keep 1e-13 relative. The
     post-processing block's |grad n| at each cell's centre node (interior to one cell, so the
-    lumped-mass scaling returns the point value) exposes the derivative itself."""
+    lumped-mass scaling returns the point value) exposes the derivative itself. In mode 4 (the
+    lane kernel) the value term |grad n| is integrated in fixed point too, with the block exponent
+    of the cell's largest submitted term: one more unit of 2^-52 of that term."""
     wl = W.allen_cahn_2d(refine=3, degree=2)  # 8 x 8 Q2 cells of [0,100]^2, 17 x 17 nodes
     nc, nn, h = 8, 17, 100.0 / 8
     rng = np.random.default_rng(23)
@@ -214,4 +218,14 @@ def test_derivative_error_is_absolute_in_the_cell_maximum(gpu_lib, mode):
     assert np.all(np.abs(fp64 - exact) <= 1e-13 * exact)
     fixed = centre_gradients(PPF_CONTRACTION_MODE=mode)
     bound = 2.0 * np.sqrt(2.0) * resolution / h + 8 * np.spacing(exact)
+    if mode == "4":
+        # the lane kernel integrates the value terms in fixed point as well, as h |grad n| with
+        # the block exponent of the cell's largest one (one binade up, h = 12.5 not being a power
+        # of two): one unit of that resolution more, relative to the cell's largest |grad n|
+        D = np.array([[-3.0, 4.0, -1.0], [-1.0, 0.0, 1.0], [1.0, -4.0, 3.0]]) / h
+        gmax = np.array([np.hypot(u[2 * cy:2 * cy + 3, 2 * cx:2 * cx + 3] @ D.T,
+                                  D @ u[2 * cy:2 * cy + 3, 2 * cx:2 * cx + 3]).max()
+                         for cy in range(nc) for cx in range(nc)])
+        hk = np.floor(np.log2(h))
+        bound = bound + 2.0 ** (np.floor(np.log2(gmax)) + hk + 1 - 52) / h
     assert np.all(np.abs(fixed - exact) <= bound)
