@@ -6,24 +6,30 @@
 // integrate_and_distribute, include/prismspf/core/field_container.h:794-882): gather ->
 // user callback per quadrature point -> integrate -> condensed scatter. The layout and the
 // arithmetic differ:
-//   * a thread block owns a tile of CPT cells (32, or 16 when an operator asks for it); lane
-//     l of every warp is cell l of the tile, and the warps take the quadrature points in turn
-//     (CPT = 32: warp w is point w of every cell). Rows of shared memory are [point][cell], so a
-//     point's line neighbours are whole warps' rows away and every access is a contiguous warp
-//     row; the per-cell block exponents are shared-memory atomics on CPT distinct words (no
-//     conflicts), and a point's position on its lines is uniform across the warp;
+//   * a thread block owns a tile of 32 cells; lane l of every warp is cell l of the tile. Warp w
+//     takes the w-th point of the cell's first dim-1 directions and each of its threads the n
+//     points above it along the last direction (a line of its cell): point (w, j) is
+//     q = w + j * n^(dim-1) (Q2 3-D: 9 warps, 3 points a thread). Rows of shared memory are
+//     [point][cell], so every access is a contiguous warp row, a point's position on its lines
+//     is uniform across the warp, and the per-cell block exponents are shared-memory atomics on
+//     32 distinct words, one per thread and row;
 //   * derivatives: exact integer line sums of the nodal values' fixed-point copies, rounded
 //     once by to_double_fast (prismspf/gpu/fixed_point.cuh) with 1/h_d folded in;
 //   * integration: the submitted value term (as h v) and gradient terms of a cell and output
 //     component share one block exponent; every node's integral is the exact integer sum
 //     2^vw(q) X(q) + sum_d 2^wo_d(q) L_d(q) (L_d the Gauss-Lobatto line integral of the
-//     gradient terms along d, 2^vw and 2^wo the integer quadrature weights) rounded once with the
-//     scale detJ / (h W^dim): no FP64 instruction outside the user's callback. On GB300 the FP64
-//     pipe retires about two operations per SM per clock and every FP64 conversion runs on it
-//     too, so the integer path (issue slots) replaces 9-10 FP64 operations per point.
+//     gradient terms along d, the last direction's taken from the thread's own points; 2^vw and
+//     2^wo the integer quadrature weights) rounded once with the scale detJ / (h W^dim): no FP64
+//     instruction outside the user's callback. On GB300 the FP64 pipe retires about two
+//     operations per SM per clock and every FP64 conversion runs on it too, so the integer path
+//     (issue slots) replaces 9-10 FP64 operations per point;
 //   * four block barriers per tile: nodal values and exponents, fixed-point copies, submitted
 //     terms and exponents, their fixed-point copies. The value-row exponents alternate between
-//     two buffers so that clearing the next tile's needs no extra barrier.
+//     two buffers so that clearing the next tile's needs no extra barrier;
+//   * the cell tables and the flat row lists are kernel parameters (constant-bank loads); every
+//     output component is integrated (rows the callback leaves stay zero), so no branch depends
+//     on which terms were submitted; lanes past the last cell recompute the last cell and skip
+//     its scatter.
 // Accuracy: every derivative and every node's integral is one rounding of an exact sum of
 // values quantised to 2^-58 (derivatives) or 2^-52 (integration) of the largest magnitude of
 // their cell and row, as in the other integer-contraction kernels.
@@ -42,33 +48,27 @@
 
 namespace ppf {
 
-template <int dim, int degree, int CPT>
+// Q1/Q2 on a lane kernel tile: lane l of every warp is cell l of a 32-cell tile; warp w holds
+// the w-th point of the cell's first dim-1 directions, and its thread the n points above it
+// along the last direction (a line of the cell): point (w, j) is q = w + j * cols.
+template <int dim, int degree>
 struct LaneShape {
   static constexpr int n = degree + 1;
   static constexpr int nq = pg::ipow(n, dim);
-  static constexpr int ppw = 32 / CPT;  // points per warp
-  static constexpr int warps = (nq + ppw - 1) / ppw;
-  static constexpr int threads = 32 * warps;
+  static constexpr int cols = nq / n;  // warps per block
+  static constexpr int threads = 32 * cols;
 };
+constexpr int LANE_CPT = 32;  // cells per tile
 
 // fixed-point top of the integration: |X| <= 2^53 and |L_d| <= 8 * 2^53 keep the weighted sum
 // below 2^53 (2^6 + 3 * 2^4 * 8) < 2^62
 constexpr int LANE_TOP_TERMS = 52;
 
-// An operator may ask for 16 cells per tile (`static constexpr int cell_lane_cpt = 16`), which
-// halves the shared memory of a tile for operators with many rows, and for a register budget
-// (`cell_lane_min_blocks`, resident blocks per SM).
-template <class PDE, class = void>
-struct CellLaneCpt {
-  static constexpr int value = 32;
-};
-template <class PDE>
-struct CellLaneCpt<PDE, std::void_t<decltype(PDE::cell_lane_cpt)>> {
-  static constexpr int value = PDE::cell_lane_cpt;
-};
+// An operator may ask for a register budget (`cell_lane_min_blocks`, resident blocks per SM);
+// the default aims at about 48 registers a thread.
 template <class PDE, int threads, class = void>
 struct CellLaneMinBlocks {
-  static constexpr int value = 2048 / threads > 0 ? 2048 / threads : 1;
+  static constexpr int value = 65536 / (threads * 48) > 0 ? (65536 / (threads * 48) < 32 ? 65536 / (threads * 48) : 32) : 1;
 };
 template <class PDE, int threads>
 struct CellLaneMinBlocks<PDE, threads, std::void_t<decltype(PDE::cell_lane_min_blocks)>> {
@@ -77,14 +77,15 @@ struct CellLaneMinBlocks<PDE, threads, std::void_t<decltype(PDE::cell_lane_min_b
 
 // shared memory of a tile: nodal values and their fixed-point copies (nrows_in rows each), the
 // submitted terms (nrows_out rows), then the block exponents
-template <int dim, int degree, int CPT>
+template <int dim, int degree>
 __host__ __device__ constexpr size_t lane_smem_bytes(int nrows_in, int nrows_out) {
-  using S = LaneShape<dim, degree, CPT>;
-  return (size_t)S::nq * CPT * 8 * (size_t)(2 * nrows_in + nrows_out) + 4 * (size_t)CPT * (size_t)(2 * nrows_in + nrows_out);
+  using S = LaneShape<dim, degree>;
+  return (size_t)S::nq * LANE_CPT * 8 * (size_t)(2 * nrows_in + nrows_out) +
+         4 * (size_t)LANE_CPT * (size_t)(2 * nrows_in + nrows_out);
 }
 
 // Gauss-Lobatto line integral of the terms g at the line's node j (line_integral of
-// fixed_point.cuh), with j uniform across a warp when CPT = 32
+// fixed_point.cuh), with j uniform across a warp
 template <int n>
 __device__ __forceinline__ long long lane_line_integral(int j, long long g0, long long g1, long long g2) {
   if constexpr (n == 2) {
@@ -116,20 +117,19 @@ struct LaneRows {
   int out_row[LANE_MAX_OUT];             // value row of the component (dim gradient rows follow)
 };
 
-template <class PDE, int dim, int degree, int MODE, int CPT, int MINB>
-__global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
+template <class PDE, int dim, int degree, int MODE, int MINB>
+__global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
     cell_kernel_lanes(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde,
                       const __grid_constant__ pg::CellTables<dim, degree, double> T,
                       const __grid_constant__ LaneRows R) {
   static_assert(degree <= 2 && MODE != MODE_DIAG, "the lane kernel covers FP64 Q1/Q2 RHS and LHS launches");
-  static_assert(CPT == 32 || CPT == 16, "16 or 32 cells per tile");
-  using S = LaneShape<dim, degree, CPT>;
+  using S = LaneShape<dim, degree>;
   using Tab = pg::CellTables<dim, degree, double>;
   namespace fx = pg::fx;
-  constexpr int n = S::n, nq = S::nq, k = degree;
-  constexpr int ROW = nq * CPT;  // entries of one row
+  constexpr int n = S::n, nq = S::nq, cols = S::cols, k = degree, CPT = LANE_CPT;
+  constexpr int ROW = nq * CPT;   // entries of one row
+  constexpr int JS = cols * CPT;  // entry stride between a thread's points
   constexpr int TOPT = LANE_TOP_TERMS;
-  constexpr bool ALL_Q = S::warps * S::ppw == nq;  // every thread holds a quadrature point
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // the tables are a kernel parameter: read-only constant-bank loads, uniform where their index is
   const Tab* tab = &T;
@@ -141,24 +141,20 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
   int* ex_out = ex_in + 2 * R.nin * CPT;                             // [nout][cell]
 
   const int t = threadIdx.x;
-  const int lane = t & 31;
-  const int lc = lane & (CPT - 1);
-  const int q = (t >> 5) * S::ppw + lane / CPT;
-  const bool qv = ALL_Q || q < nq;
-  const int qs = qv ? q : 0;  // a point to address with (threads past the last point mirror point 0)
-  const int p = qs * CPT + lc;  // this thread's entry in a row
-  const int qa = qs % n;
-  const int qb = dim > 1 ? (qs / n) % n : 0;
-  const int qc = dim > 2 ? qs / (n * n) : 0;
+  const int lc = t & 31;
+  const int w = t >> 5;          // point of the first dim-1 directions
+  const int p0 = w * CPT + lc;   // entry of the thread's first point; point j at p0 + j * JS
+  const int qa = w % n;
+  const int qb = dim > 2 ? w / n : 0;
   const unsigned int fx_rows = tab->fx_rows;  // input rows read as gradients (fixed-point copies)
   const int hpow2 = tab->hpow2, hk = tab->hk;
   const unsigned long long hsig = tab->hsig;
   // both exponent buffers: 0 for rows with a fixed-point copy, -1 for rows read as values only
   for (int i = t; i < 2 * R.nin * CPT; i += S::threads) ex_in[i] = ((fx_rows >> ((i / CPT) % R.nin)) & 1u) ? 0 : -1;
   const unsigned int nn0 = (unsigned int)P.nn[0], nn1 = (unsigned int)P.nn[1];
+  const unsigned int lstride = dim > 2 ? nn0 * nn1 : nn0;  // lattice stride of the last direction
   const unsigned int ncells = (unsigned int)P.ncells;
   const unsigned int ntiles = (ncells + CPT - 1) / CPT;
-  const int qi[3] = {qa, qb, qc};
   __syncthreads();  // exponent buffers set
 
   int par = 0;
@@ -167,8 +163,8 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
     int* exn = ex_in + (par ^ 1) * R.nin * CPT;
     // lanes past the last cell redo the last cell and skip its scatter
     const unsigned int cell_t = tile * CPT + lc;
-    const bool active = qv && cell_t < ncells;
-    const unsigned int cell = cell_t < ncells ? cell_t : ncells - 1;
+    const bool active = cell_t < ncells;
+    const unsigned int cell = active ? cell_t : ncells - 1;
     int cx, cy = 0, cz = 0;
     {
       const unsigned int q0 = (__umulhi(cell, R.div_m[0]) + cell) >> R.div_l[0];
@@ -180,8 +176,9 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
         cz = (int)q1;
       }
     }
-    const unsigned int node =
-        ((unsigned int)(k * cz + qc) * nn1 + (unsigned int)(k * cy + qb)) * nn0 + (unsigned int)(k * cx + qa);
+    // lattice node of the thread's first point (last-direction index 0)
+    const unsigned int node0 = dim > 2 ? ((unsigned int)(k * cz) * nn1 + (unsigned int)(k * cy + qb)) * nn0 + (unsigned int)(k * cx + qa)
+                                       : (unsigned int)(k * cy) * nn0 + (unsigned int)(k * cx + qa);
 
     // gather (read_dof_values_plain, or read_dof_values for a constrained src) and the block
     // exponents of the rows read as gradients
@@ -189,17 +186,22 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
     for (int r = 0; r < LANE_MAX_IN; ++r) {
       if (r < R.nin) {
         const double* base = R.in_base[r];
-        const unsigned int idx = node + R.in_off[r];
-        double v;
-        if (R.in_cmap[r]) {
-          const int m = __ldg(R.in_cmap[r] + idx);
-          const double own = __ldg(base + idx);
-          v = m == (int)idx ? own : (m >= 0 ? __ldg(base + m) : 0.0);
-        } else {
-          v = __ldg(base + idx);
+        int e = 0;
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          const unsigned int idx = node0 + (unsigned int)j * lstride + R.in_off[r];
+          double v;
+          if (R.in_cmap[r]) {
+            const int m = __ldg(R.in_cmap[r] + idx);
+            const double own = __ldg(base + idx);
+            v = m == (int)idx ? own : (m >= 0 ? __ldg(base + m) : 0.0);
+          } else {
+            v = __ldg(base + idx);
+          }
+          vals[r * ROW + p0 + j * JS] = v;
+          e = max(e, fx::exponent(v));
         }
-        if (qv) vals[r * ROW + p] = v;
-        if (((fx_rows >> r) & 1u) && qv) atomicMax(&exi[r * CPT + lc], fx::exponent(v));
+        if ((fx_rows >> r) & 1u) atomicMax(&exi[r * CPT + lc], e);
       }
     }
     __syncthreads();  // nodal values and their block exponents complete
@@ -210,43 +212,49 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
     for (int r = 0; r < LANE_MAX_IN; ++r) {
       if (r < R.nin && ((fx_rows >> r) & 1u)) {
         const int E = exi[r * CPT + lc];
-        const long long x = fx::to_fixed_fast<fx::TOP_VALUES>(vals[r * ROW + p], E);
-        if (qv) vfx[r * ROW + p] = E == fx::EXP_NONFINITE ? 0ll : x;
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          const long long x = fx::to_fixed_fast<fx::TOP_VALUES>(vals[r * ROW + p0 + j * JS], E);
+          vfx[r * ROW + p0 + j * JS] = E == fx::EXP_NONFINITE ? 0ll : x;
+        }
       }
     }
 #pragma unroll
     for (int o = 0; o < LANE_MAX_OUT; ++o)
-      if (o < R.nout && qv)
+      if (o < R.nout)
 #pragma unroll
-        for (int j = 0; j <= dim; ++j) outs[(R.out_row[o] + j) * ROW + p] = 0.0;
+        for (int i = 0; i <= dim; ++i)
+#pragma unroll
+          for (int j = 0; j < n; ++j) outs[(R.out_row[o] + i) * ROW + p0 + j * JS] = 0.0;
     for (int i = t; i < R.nin * CPT; i += S::threads) exn[i] = ((fx_rows >> (i / CPT)) & 1u) ? 0 : -1;
     for (int i = t; i < R.nout * CPT; i += S::threads) ex_out[i] = 0;
     __syncthreads();  // fixed-point copies visible
 
-    pg::CellCtx<dim, degree, double> ctx;
-    ctx.tab = tab;
-    ctx.vals = vals;
-    ctx.outs = outs;
-    ctx.stride = ROW;
-    ctx.lc = lc;
-    ctx.q = qs;
-    ctx.cell[0] = cx;
-    ctx.cell[1] = cy;
-    ctx.cell[2] = cz;
-    ctx.err = P.err;
-    ctx.submitted = 0;
-    ctx.vals_fx = vfx;
-    ctx.ex_in = exi;
-    ctx.cpb = CPT;
-    ctx.cpt = CPT;
-    ctx.lean = 1;
-    ctx.qi[0] = qa;
-    ctx.qi[1] = qb;
-    ctx.qi[2] = qc;
-    if (qv) {
+    // the user callback at each of the thread's points
+    const SimulationTimer& timer = P.timer_dev ? *P.timer_dev : P.timer;
+#pragma unroll
+    for (int j = 0; j < n; ++j) {
+      pg::CellCtx<dim, degree, double> ctx;
+      ctx.tab = tab;
+      ctx.vals = vals;
+      ctx.outs = outs;
+      ctx.stride = ROW;
+      ctx.lc = lc;
+      ctx.q = w + j * cols;
+      ctx.cell[0] = cx;
+      ctx.cell[1] = cy;
+      ctx.cell[2] = cz;
+      ctx.err = P.err;
+      ctx.submitted = 0;
+      ctx.vals_fx = vfx;
+      ctx.ex_in = exi;
+      ctx.cpb = CPT;
+      ctx.cpt = CPT;
+      ctx.lean = 1;
+      ctx.qi[0] = qa;
+      ctx.qi[1] = dim > 2 ? qb : j;
+      ctx.qi[2] = dim > 2 ? j : 0;
       FieldContainer<dim, degree, double> fc(ctx);
-      // the clock from the launch record, or from device memory during graph replays
-      const SimulationTimer& timer = P.timer_dev ? *P.timer_dev : P.timer;
       if constexpr (MODE == MODE_LHS) pde.compute_lhs(fc, timer, P.block_id);
       else pde.compute_rhs(fc, timer, P.block_id);
     }
@@ -256,12 +264,16 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
     for (int o = 0; o < LANE_MAX_OUT; ++o) {
       if (o < R.nout) {
         const int rv = R.out_row[o];
-        const int ev = fx::exponent(outs[rv * ROW + p]);
-        const int eh = ev + hk + (hpow2 ? 0 : 1);
-        int e = ev == 0 ? 0 : (ev == fx::EXP_NONFINITE || eh >= fx::EXP_NONFINITE ? fx::EXP_NONFINITE : max(eh, 0));
+        int e = 0;
 #pragma unroll
-        for (int d = 0; d < dim; ++d) e = max(e, fx::exponent(outs[(rv + 1 + d) * ROW + p]));
-        if (qv) atomicMax(&ex_out[o * CPT + lc], e);
+        for (int j = 0; j < n; ++j) {
+          const int ev = fx::exponent(outs[rv * ROW + p0 + j * JS]);
+          const int eh = ev + hk + (hpow2 ? 0 : 1);
+          e = max(e, ev == 0 ? 0 : (ev == fx::EXP_NONFINITE || eh >= fx::EXP_NONFINITE ? fx::EXP_NONFINITE : max(eh, 0)));
+#pragma unroll
+          for (int d = 0; d < dim; ++d) e = max(e, fx::exponent(outs[(rv + 1 + d) * ROW + p0 + j * JS]));
+        }
+        atomicMax(&ex_out[o * CPT + lc], e);
       }
     }
     __syncthreads();  // submitted terms and their block exponents complete
@@ -273,16 +285,18 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
         const int rv = R.out_row[o];
         const int E = ex_out[o * CPT + lc];
         const bool nf = E == fx::EXP_NONFINITE;
-        double* vp = outs + rv * ROW + p;
-        const double v = *vp;
-        const long long xv = hpow2 ? fx::to_fixed_fast<TOPT>(v, E - hk) : fx::to_fixed_scaled<TOPT>(v, E, hsig, hk);
-        long long xg[dim];
+        long long* ox = reinterpret_cast<long long*>(outs);
 #pragma unroll
-        for (int d = 0; d < dim; ++d) xg[d] = fx::to_fixed_fast<TOPT>(outs[(rv + 1 + d) * ROW + p], E);
-        if (qv) {
-          *reinterpret_cast<long long*>(vp) = nf ? 0ll : xv;
+        for (int j = 0; j < n; ++j) {
+          const int e0 = rv * ROW + p0 + j * JS;
+          const double v = outs[e0];
+          const long long xv = hpow2 ? fx::to_fixed_fast<TOPT>(v, E - hk) : fx::to_fixed_scaled<TOPT>(v, E, hsig, hk);
+          ox[e0] = nf ? 0ll : xv;
 #pragma unroll
-          for (int d = 0; d < dim; ++d) reinterpret_cast<long long*>(outs)[(rv + 1 + d) * ROW + p] = nf ? 0ll : xg[d];
+          for (int d = 0; d < dim; ++d) {
+            const long long xg = fx::to_fixed_fast<TOPT>(outs[e0 + (1 + d) * ROW], E);
+            ox[e0 + (1 + d) * ROW] = nf ? 0ll : xg;
+          }
         }
       }
     }
@@ -295,28 +309,34 @@ __global__ void __launch_bounds__(LaneShape<dim, degree, CPT>::threads, MINB)
       if (o < R.nout) {
         const int rv = R.out_row[o];
         const int E = ex_out[o * CPT + lc];
-        // this point's integration weights: powers of two from the tables
-        long long Tx = (long long)((unsigned long long)ox[rv * ROW + p] << tab->vw_sh[qs]);
+        // the last direction's line is the thread's own points
+        const long long* gl = ox + (rv + dim) * ROW + p0;
+        const long long z0 = gl[0], z1 = gl[JS], z2 = n > 2 ? gl[2 * JS] : 0ll;
 #pragma unroll
-        for (int d = 0; d < dim; ++d) {
-          const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
-          const long long* g = ox + (rv + 1 + d) * ROW + (qs - qi[d] * sd) * CPT + lc;
-          const long long L = lane_line_integral<n>(qi[d], g[0], g[sd * CPT], n > 2 ? g[2 * sd * CPT] : 0ll);
-          Tx += (long long)((unsigned long long)L << tab->wo_sh[d][qs]);
+        for (int j = 0; j < n; ++j) {
+          const int q = w + j * cols;
+          const int e0 = rv * ROW + p0 + j * JS;
+          // this point's integration weights: powers of two from the tables
+          long long Tx = (long long)((unsigned long long)ox[e0] << tab->vw_sh[q]);
+#pragma unroll
+          for (int d = 0; d < dim - 1; ++d) {
+            const int sd = d == 0 ? 1 : n;
+            const int id = d == 0 ? qa : qb;
+            const long long* g = ox + (rv + 1 + d) * ROW + (q - id * sd) * CPT + lc;
+            const long long L = lane_line_integral<n>(id, g[0], g[sd * CPT], n > 2 ? g[2 * sd * CPT] : 0ll);
+            Tx += (long long)((unsigned long long)L << tab->wo_sh[d][q]);
+          }
+          const long long Lz = lane_line_integral<n>(j, z0, z1, z2);
+          Tx += (long long)((unsigned long long)Lz << tab->wo_sh[dim - 1][q]);
+          const double rr = fx::to_double_fast(Tx, E - 1023 - TOPT + tab->ik[0], tab->isig[0], true);
+          const double r = E == fx::EXP_NONFINITE ? fx::quiet_nan() : rr;
+          const unsigned int idx = node0 + (unsigned int)j * lstride + R.out_off[o];
+          const int target = R.out_cmap[o] ? __ldg(R.out_cmap[o] + idx) : (int)idx;
+          if (active && target >= 0) atomicAdd(R.out_acc[o] + target, r);
         }
-        const double rr = fx::to_double_fast(Tx, E - 1023 - TOPT + tab->ik[0], tab->isig[0], true);
-        const double r = E == fx::EXP_NONFINITE ? fx::quiet_nan() : rr;
-        const unsigned int idx = node + R.out_off[o];
-        const int target = R.out_cmap[o] ? __ldg(R.out_cmap[o] + idx) : (int)idx;
-        if (active && target >= 0) atomicAdd(R.out_acc[o] + target, r);
       }
     }
   }
-}
-
-template <class PDE, int dim, int degree>
-constexpr int lane_cpt() {
-  return CellLaneCpt<PDE>::value;
 }
 
 // the flat row lists of a launch record; false when they exceed the lane kernel's limits
@@ -356,11 +376,11 @@ inline bool lane_rows(const CellLaunch& P, int dim, LaneRows* R) {
   return row == P.nrows_out;
 }
 
-template <class PDE, int dim, int degree, int mode, int CPT, int MINB>
+template <class PDE, int dim, int degree, int mode, int MINB>
 cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj, cudaStream_t s) {
-  using S = LaneShape<dim, degree, CPT>;
-  auto kern = cell_kernel_lanes<PDE, dim, degree, mode, CPT, MINB>;
-  const size_t smem = lane_smem_bytes<dim, degree, CPT>(P.nrows_in, P.nrows_out);
+  using S = LaneShape<dim, degree>;
+  auto kern = cell_kernel_lanes<PDE, dim, degree, mode, MINB>;
+  const size_t smem = lane_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out);
   constexpr int MAX_DEVICES = 64;
   static size_t attr_smem_of[MAX_DEVICES] = {};
   static int occ_of[MAX_DEVICES] = {};
@@ -383,7 +403,7 @@ cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }
-  const long long ntiles = (P.ncells + CPT - 1) / CPT;
+  const long long ntiles = (P.ncells + LANE_CPT - 1) / LANE_CPT;
   long long grid = (long long)sms * occ;
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) grid = 1;
@@ -397,12 +417,11 @@ cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj
 // limits (the caller then takes the thread-block kernel)
 template <class PDE, int dim, int degree, int mode>
 cudaError_t launch_cell_kernel_lanes_impl(const CellLaunch& P, const void* obj, cudaStream_t s) {
-  constexpr int CPT = lane_cpt<PDE, dim, degree>();
-  constexpr int MINB = CellLaneMinBlocks<PDE, LaneShape<dim, degree, CPT>::threads>::value;
+  constexpr int MINB = CellLaneMinBlocks<PDE, LaneShape<dim, degree>::threads>::value;
   LaneRows R;
-  if (!P.tables_host || !lane_rows(P, dim, &R) || lane_smem_bytes<dim, degree, CPT>(P.nrows_in, P.nrows_out) > 232448)
+  if (!P.tables_host || !lane_rows(P, dim, &R) || lane_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out) > 232448)
     return cudaErrorNotSupported;
-  return launch_lanes<PDE, dim, degree, mode, CPT, MINB>(P, R, obj, s);
+  return launch_lanes<PDE, dim, degree, mode, MINB>(P, R, obj, s);
 }
 
 }  // namespace ppf
