@@ -29,6 +29,7 @@ constexpr int NAGE = 6;  // current, old_1..old_4, src
 constexpr int MAX_SLOTS = 8;
 constexpr int MAX_OUTS = 4;
 constexpr int MAX_N = 5;  // up to degree 4
+constexpr int LANE_ROW_SLOTS = 8;  // value rows the lane kernel's slot tables cover
 
 enum ErrorBits : int {
   ERR_UNDECLARED_DEPENDENCY = 1,
@@ -78,6 +79,12 @@ struct CellTables {
   int dpow2[3];
   unsigned long long hsig;
   signed char vw_sh[nq];
+  // the lane kernel keeps a double copy only of the value rows read as values or Hessians
+  // (val_rows) and a fixed-point copy only of those read as gradients (fx_rows): slot of row r
+  // in each, -1 without one (rows below LANE_ROW_SLOTS)
+  unsigned int val_rows;
+  signed char lane_vslot[LANE_ROW_SLOTS];
+  signed char lane_gslot[LANE_ROW_SLOTS];
 };
 
 template <int dim, int degree, typename number = double>
@@ -377,7 +384,28 @@ class FieldContainer {
     return ctx.tab->out_row0[o];
   }
 
-  PPF_HD number nodal(int row, int q) const { return ctx.vals[row * ctx.stride + pt(q)]; }
+  PPF_HD number nodal(int row, int q) const {
+    if constexpr (std::is_same<number, double>::value && degree <= 2) {
+      if (ctx.lean) {
+        // the lane kernel: the row's double copy, or for a row read only as a gradient its
+        // value rebuilt from the fixed-point copy (exact to 2^-58 of the cell's largest value)
+        const int vs = ctx.tab->lane_vslot[row];
+        if (vs >= 0) return ctx.vals[vs * ctx.stride + pt(q)];
+        const int E = ctx.ex_in[row * ctx.cpb + ctx.lc];
+        const long long x = ctx.vals_fx[ctx.tab->lane_gslot[row] * ctx.stride + pt(q)];
+        const double v = gpu::fx::to_double_fast(x, E - 1023 - gpu::fx::TOP_VALUES, 1ull << 63, false);
+        return E == gpu::fx::EXP_NONFINITE ? gpu::fx::quiet_nan() : v;
+      }
+    }
+    return ctx.vals[row * ctx.stride + pt(q)];
+  }
+  // the row's first entry in the double copies (the lane kernel's slot, else the row itself)
+  PPF_HD int vrow(int row) const {
+    if constexpr (std::is_same<number, double>::value && degree <= 2) {
+      if (ctx.lean) return ctx.tab->lane_vslot[row];
+    }
+    return row;
+  }
 
   // first derivative along direction d at this thread's quadrature point
   PPF_HD number deriv(int row, int d) const {
@@ -392,7 +420,8 @@ class FieldContainer {
         const int qd = ctx.qi[d];
         const int E = ctx.ex_in[row * ctx.cpb + ctx.lc];
         const int sq = stride_d * ctx.cpt;
-        const long long* u = ctx.vals_fx + row * ctx.stride + (ctx.q - qd * stride_d) * ctx.cpt + ctx.lc;
+        const long long* u =
+            ctx.vals_fx + ctx.tab->lane_gslot[row] * ctx.stride + (ctx.q - qd * stride_d) * ctx.cpt + ctx.lc;
         long long s;
         if constexpr (n == 2) {
           s = u[sq] - u[0];
@@ -427,7 +456,7 @@ class FieldContainer {
     const int q0 = ctx.q - qd * stride_d;
     const number* Dr = ctx.tab->Dh[d][qd];
     if (ctx.cpt) {
-      const number* u = ctx.vals + row * ctx.stride + q0 * ctx.cpt + ctx.lc;
+      const number* u = ctx.vals + vrow(row) * ctx.stride + q0 * ctx.cpt + ctx.lc;
       number s = Dr[0] * u[0];
 #pragma unroll
       for (int j = 1; j < n; ++j) s = fma(Dr[j], u[j * stride_d * ctx.cpt], s);
@@ -446,7 +475,15 @@ class FieldContainer {
     for (int k = 0; k < d; ++k) sd *= n;
     for (int k = 0; k < e; ++k) se *= n;
     const int qd = (ctx.q / sd) % n, qe = (ctx.q / se) % n;
-    const number* base = ctx.vals + row * ctx.stride;
+    const int vr = vrow(row);
+    if (vr < 0) {
+      // the lane kernel keeps no double copy of a row declared without values or Hessians
+#ifdef __CUDA_ARCH__
+      atomicOr(ctx.err, int(gpu::ERR_UNDECLARED_DEPENDENCY));
+#endif
+      return number(0);
+    }
+    const number* base = ctx.vals + vr * ctx.stride;
     if (d == e) {
       const int q0 = ctx.q - qd * sd;
       const number* Dr = ctx.tab->D2h[d][qd];

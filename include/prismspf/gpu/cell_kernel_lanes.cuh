@@ -65,23 +65,24 @@ constexpr int LANE_CPT = 32;  // cells per tile
 constexpr int LANE_TOP_TERMS = 52;
 
 // An operator may ask for a register budget (`cell_lane_min_blocks`, resident blocks per SM);
-// the default aims at about 48 registers a thread.
+// the default aims at about 40 registers a thread.
 template <class PDE, int threads, class = void>
 struct CellLaneMinBlocks {
-  static constexpr int value = 65536 / (threads * 48) > 0 ? (65536 / (threads * 48) < 32 ? 65536 / (threads * 48) : 32) : 1;
+  static constexpr int value = 65536 / (threads * 40) > 0 ? (65536 / (threads * 40) < 32 ? 65536 / (threads * 40) : 32) : 1;
 };
 template <class PDE, int threads>
 struct CellLaneMinBlocks<PDE, threads, std::void_t<decltype(PDE::cell_lane_min_blocks)>> {
   static constexpr int value = PDE::cell_lane_min_blocks;
 };
 
-// shared memory of a tile: nodal values and their fixed-point copies (nrows_in rows each), the
-// submitted terms (nrows_out rows), then the block exponents
+// shared memory of a tile: the double copies of the nv value rows, the fixed-point copies of the
+// ng gradient rows, the submitted terms (nout components of 1 + dim rows), then the block
+// exponents (two buffers of nrows_in rows, one of nout)
 template <int dim, int degree>
-__host__ __device__ constexpr size_t lane_smem_bytes(int nrows_in, int nrows_out) {
+__host__ __device__ constexpr size_t lane_smem_bytes(int nv, int ng, int nrows_in, int nout) {
   using S = LaneShape<dim, degree>;
-  return (size_t)S::nq * LANE_CPT * 8 * (size_t)(2 * nrows_in + nrows_out) +
-         4 * (size_t)LANE_CPT * (size_t)(2 * nrows_in + nrows_out);
+  return (size_t)S::nq * LANE_CPT * 8 * (size_t)(nv + ng + nout * (1 + dim)) +
+         4 * (size_t)LANE_CPT * (size_t)(2 * nrows_in + nout);
 }
 
 // Gauss-Lobatto line integral of the terms g at the line's node j (line_integral of
@@ -107,6 +108,8 @@ constexpr int LANE_MAX_OUT = 3;
 struct LaneRows {
   int nin;
   int nout;
+  int nv;                                // input rows with a double copy (read as values or Hessians)
+  int ng;                                // input rows with a fixed-point copy (read as gradients)
   unsigned int div_m[2], div_l[2];       // cell index -> (x, y, z): multiply-high divisors of nc[0], nc[1]
   const double* in_base[LANE_MAX_IN];    // vector of the row's slot
   const int* in_cmap[LANE_MAX_IN];       // constraint map for a constrained read, else null
@@ -133,9 +136,9 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // the tables are a kernel parameter: read-only constant-bank loads, uniform where their index is
   const Tab* tab = &T;
-  double* vals = reinterpret_cast<double*>(smem_raw);                // [nin][q][cell]
-  long long* vfx = reinterpret_cast<long long*>(vals + R.nin * ROW);  // [nin][q][cell]
-  double* outs = reinterpret_cast<double*>(vfx + R.nin * ROW);       // [out rows][q][cell]
+  double* vals = reinterpret_cast<double*>(smem_raw);               // [nv][q][cell]
+  long long* vfx = reinterpret_cast<long long*>(vals + R.nv * ROW);  // [ng][q][cell]
+  double* outs = reinterpret_cast<double*>(vfx + R.ng * ROW);       // [out rows][q][cell]
   const int nrows_out = R.nout * (1 + dim);
   int* ex_in = reinterpret_cast<int*>(outs + nrows_out * ROW);       // [2][nin][cell]
   int* ex_out = ex_in + 2 * R.nin * CPT;                             // [nout][cell]
@@ -198,7 +201,10 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
           } else {
             v = __ldg(base + idx);
           }
-          vals[r * ROW + p0 + j * JS] = v;
+          const int vs = tab->lane_vslot[r], gs = tab->lane_gslot[r];
+          if (vs >= 0) vals[vs * ROW + p0 + j * JS] = v;
+          // a gradient row's double stays in its fixed-point slot until converted in place
+          if (gs >= 0) vfx[gs * ROW + p0 + j * JS] = __double_as_longlong(v);
           e = max(e, fx::exponent(v));
         }
         if ((fx_rows >> r) & 1u) atomicMax(&exi[r * CPT + lc], e);
@@ -211,12 +217,12 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
 #pragma unroll
     for (int r = 0; r < LANE_MAX_IN; ++r) {
       if (r < R.nin && ((fx_rows >> r) & 1u)) {
+        // (a cell holding a non-finite value gets meaningless copies: every result read from them
+        // is replaced by NaN)
         const int E = exi[r * CPT + lc];
+        long long* x = vfx + tab->lane_gslot[r] * ROW + p0;
 #pragma unroll
-        for (int j = 0; j < n; ++j) {
-          const long long x = fx::to_fixed_fast<fx::TOP_VALUES>(vals[r * ROW + p0 + j * JS], E);
-          vfx[r * ROW + p0 + j * JS] = E == fx::EXP_NONFINITE ? 0ll : x;
-        }
+        for (int j = 0; j < n; ++j) x[j * JS] = fx::to_fixed_fast<fx::TOP_VALUES>(__longlong_as_double(x[j * JS]), E);
       }
     }
 #pragma unroll
@@ -232,7 +238,8 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
 
     // the user callback at each of the thread's points
     const SimulationTimer& timer = P.timer_dev ? *P.timer_dev : P.timer;
-#pragma unroll
+    // (one copy of the callback's code: unrolling the points measured slower)
+#pragma unroll 1
     for (int j = 0; j < n; ++j) {
       pg::CellCtx<dim, degree, double> ctx;
       ctx.tab = tab;
@@ -283,20 +290,16 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
     for (int o = 0; o < LANE_MAX_OUT; ++o) {
       if (o < R.nout) {
         const int rv = R.out_row[o];
+        // (with E = 2047 the copies are meaningless and the integral is replaced by NaN)
         const int E = ex_out[o * CPT + lc];
-        const bool nf = E == fx::EXP_NONFINITE;
         long long* ox = reinterpret_cast<long long*>(outs);
 #pragma unroll
         for (int j = 0; j < n; ++j) {
           const int e0 = rv * ROW + p0 + j * JS;
           const double v = outs[e0];
-          const long long xv = hpow2 ? fx::to_fixed_fast<TOPT>(v, E - hk) : fx::to_fixed_scaled<TOPT>(v, E, hsig, hk);
-          ox[e0] = nf ? 0ll : xv;
+          ox[e0] = hpow2 ? fx::to_fixed_fast<TOPT>(v, E - hk) : fx::to_fixed_scaled<TOPT>(v, E, hsig, hk);
 #pragma unroll
-          for (int d = 0; d < dim; ++d) {
-            const long long xg = fx::to_fixed_fast<TOPT>(outs[e0 + (1 + d) * ROW], E);
-            ox[e0 + (1 + d) * ROW] = nf ? 0ll : xg;
-          }
+          for (int d = 0; d < dim; ++d) ox[e0 + (1 + d) * ROW] = fx::to_fixed_fast<TOPT>(outs[e0 + (1 + d) * ROW], E);
         }
       }
     }
@@ -380,7 +383,7 @@ template <class PDE, int dim, int degree, int mode, int MINB>
 cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj, cudaStream_t s) {
   using S = LaneShape<dim, degree>;
   auto kern = cell_kernel_lanes<PDE, dim, degree, mode, MINB>;
-  const size_t smem = lane_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out);
+  const size_t smem = lane_smem_bytes<dim, degree>(R.nv, R.ng, R.nin, R.nout);
   constexpr int MAX_DEVICES = 64;
   static size_t attr_smem_of[MAX_DEVICES] = {};
   static int occ_of[MAX_DEVICES] = {};
@@ -419,8 +422,12 @@ template <class PDE, int dim, int degree, int mode>
 cudaError_t launch_cell_kernel_lanes_impl(const CellLaunch& P, const void* obj, cudaStream_t s) {
   constexpr int MINB = CellLaneMinBlocks<PDE, LaneShape<dim, degree>::threads>::value;
   LaneRows R;
-  if (!P.tables_host || !lane_rows(P, dim, &R) || lane_smem_bytes<dim, degree>(P.nrows_in, P.nrows_out) > 232448)
-    return cudaErrorNotSupported;
+  if (!P.tables_host || !lane_rows(P, dim, &R)) return cudaErrorNotSupported;
+  const auto* tab = static_cast<const pg::CellTables<dim, degree, double>*>(P.tables_host);
+  const unsigned int mask = (1u << R.nin) - 1u;
+  R.nv = __builtin_popcount(tab->val_rows & mask);
+  R.ng = __builtin_popcount(tab->fx_rows & mask);
+  if (lane_smem_bytes<dim, degree>(R.nv, R.ng, R.nin, R.nout) > 232448) return cudaErrorNotSupported;
   return launch_lanes<PDE, dim, degree, mode, MINB>(P, R, obj, s);
 }
 

@@ -139,10 +139,12 @@ PPF_FX long long to_fixed_fast(double v, int E) {
   const int e = (int)((b >> 52) & 0x7ff);
   // significand with one extra bit below it, at the top position
   const unsigned long long m2 = ((b & 0xfffffffffffffull) | (1ull << 52)) << (TOP - 51);
+  // (an exponent above E, possible only for the ignored results of a block holding a non-finite
+  // value, wraps to a large unsigned shift and clamps like a tiny value)
 #ifdef __CUDA_ARCH__
-  const int r = e == 0 ? 63 : min(E - e, 63);
+  const unsigned int r = e == 0 ? 63u : min((unsigned int)(E - e), 63u);
 #else
-  const int r = e == 0 ? 63 : std::min(E - e, 63);
+  const unsigned int r = e == 0 ? 63u : std::min((unsigned int)(E - e), 63u);
 #endif
   const unsigned long long a = ((m2 >> r) + 1) >> 1;
   const unsigned long long sg = (unsigned long long)((long long)b >> 63);
@@ -162,9 +164,9 @@ PPF_FX long long to_fixed_scaled(double v, int E, unsigned long long sig, int k)
   // (P >> r + 1) >> 1 with r = E - e - k + 61 - TOP >= 2, taken as (P / 2) >> (r - 1) so that
   // the clamped shift stays below 64 for every P
 #ifdef __CUDA_ARCH__
-  const int r1 = e == 0 ? 63 : min(E - e - k + 60 - TOP, 63);
+  const unsigned int r1 = e == 0 ? 63u : min((unsigned int)(E - e - k + 60 - TOP), 63u);
 #else
-  const int r1 = e == 0 ? 63 : std::min(E - e - k + 60 - TOP, 63);
+  const unsigned int r1 = e == 0 ? 63u : std::min((unsigned int)(E - e - k + 60 - TOP), 63u);
 #endif
   const unsigned long long a = (((P >> 1) >> r1) + 1) >> 1;
   const unsigned long long sg = (unsigned long long)((long long)b >> 63);

@@ -67,7 +67,9 @@ struct BlockPlan {
   bool fx_lanes = false;
   int fx_mode = -1;
   int fx_timed = 0;                // online timing of the multigrid outer operator
-  cudaEvent_t fx_ev[12] = {};
+  cudaEvent_t fx_ev[16] = {};
+  unsigned int fx_rows = 0;        // value rows read as gradients
+  unsigned int val_rows = 0;       // value rows read as values or Hessians
 };
 
 // One mesh of a multigrid hierarchy for a single-field linear block (the finest level is the
@@ -83,6 +85,8 @@ struct MGLevel {
   void* invm_sqrt = nullptr;    // per node, level precision
   void* inv_diag = nullptr;     // len, level precision
   void* tables = nullptr;       // CellTables for the LHS (level precision)
+  std::vector<unsigned char> h_tables;  // host copy (the lane kernel takes it as a kernel parameter)
+  bool fx_lanes = false;        // FP64 level whose tables allow the lane kernel
   void* acc = nullptr;          // accumulator
   void* x = nullptr;            // level solution
   void* b = nullptr;            // level defect (right-hand side)
@@ -104,10 +108,11 @@ struct MGLevel {
   void* t1 = nullptr;
   void* cvt = nullptr;          // precision-conversion buffer (coarsest level of a mixed hierarchy)
   // contraction mode of the level's FP64 operator (integer contractions, FP64 Q1/Q2): its first
-  // six plain LHS launches run modes 1, 2, 3 twice under CUDA events, then the fastest stays
+  // plain LHS launches run modes 1, 2, 3 (and 4 where the lane kernel applies) twice under CUDA
+  // events, then the fastest stays
   int fx_mode = -1;
   int fx_timed = 0;
-  cudaEvent_t fx_ev[12] = {};
+  cudaEvent_t fx_ev[16] = {};
 };
 
 struct AdjointState;

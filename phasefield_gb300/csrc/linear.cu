@@ -356,17 +356,18 @@ static int upload_real(ppf_handle h, void** dst, const std::vector<double>& v, i
 // Contraction mode of the multigrid operators (levels and the outer FP64 operator):
 // PPF_CONTRACTION_MODE if set, else the LHS plan's timed choice if a plain launch made one,
 // else integer derivatives with FP64 integration.
-static int multigrid_fx_mode(const BlockPlan& P) {
-  const char* env = std::getenv("PPF_CONTRACTION_MODE");
-  if (env && env[0] >= '1' && env[0] <= '3') return env[0] - '0';
-  return P.fx_mode > 0 ? P.fx_mode : 1;
+static int multigrid_fx_mode(const BlockPlan& P, bool lanes_ok) {
+  if (const int m = env_fx_mode(lanes_ok)) return m;
+  return P.fx_mode > 0 && (P.fx_mode != 4 || lanes_ok) ? P.fx_mode : 1;
 }
 
-// Online choice of a contraction mode: the first six plain launches of an operator run modes 1,
-// 2, 3 twice under CUDA events (real work: the modes agree to rounding), then the fastest
-// stays in `state`. begin returns the mode of this launch and the event slot (-1: not timed);
-// end records the closing event and decides after the sixth.
-static int online_mode_begin(ppf_handle h, int& state, int timed, cudaEvent_t* ev, int fallback, int* slot) {
+// Online choice of a contraction mode: the first 2 nm plain launches of an operator run modes
+// 1 .. nm (nm = 3, or 4 where the lane kernel applies) twice under CUDA events (real work: the
+// modes agree to rounding), then the fastest stays in `state`. begin returns the mode of this
+// launch and the event slot (-1: not timed); end records the closing event and decides after
+// the last timed launch.
+static int online_mode_begin(ppf_handle h, int& state, int timed, cudaEvent_t* ev, int fallback, int* slot,
+                             int nm) {
   *slot = -1;
   if (state > 0) return state;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -382,26 +383,26 @@ static int online_mode_begin(ppf_handle h, int& state, int timed, cudaEvent_t* e
       return state;
     }
   cudaEventRecord(ev[2 * timed], h->stream);
-  return 1 + timed % 3;
+  return 1 + timed % nm;
 }
 
-static int online_mode_end(ppf_handle h, int& state, int& timed, cudaEvent_t* ev, int slot) {
+static int online_mode_end(ppf_handle h, int& state, int& timed, cudaEvent_t* ev, int slot, int nm) {
   if (slot < 0) return PPF_OK;
   PPF_CUDA(h, cudaEventRecord(ev[2 * slot + 1], h->stream));
-  if (++timed < 6) return PPF_OK;
-  PPF_CUDA(h, cudaEventSynchronize(ev[11]));
-  float best[3] = {1e30f, 1e30f, 1e30f};
-  for (int k = 0; k < 6; ++k) {
+  if (++timed < 2 * nm) return PPF_OK;
+  PPF_CUDA(h, cudaEventSynchronize(ev[4 * nm - 1]));
+  float best[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+  for (int k = 0; k < 2 * nm; ++k) {
     float t = 0.f;
     PPF_CUDA(h, cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]));
-    best[k % 3] = std::min(best[k % 3], t);
+    best[k % nm] = std::min(best[k % nm], t);
   }
   int b = 0;
-  for (int k = 1; k < 3; ++k)
+  for (int k = 1; k < nm; ++k)
     if (best[k] < best[b]) b = k;
   state = 1 + b;
-  for (int i = 0; i < 12; ++i) {
-    cudaEventDestroy(ev[i]);
+  for (int i = 0; i < 16; ++i) {
+    if (ev[i]) cudaEventDestroy(ev[i]);
     ev[i] = nullptr;
   }
   return PPF_OK;
@@ -441,25 +442,26 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   L.nrows_in = P.nrows_in;
   L.nrows_out = P.nrows_out;
   L.tables = lv.tables;
+  L.tables_host = lv.h_tables.data();
   L.timer = h->timer;
   L.block_id = (unsigned)B.desc.id;
   L.err = h->d_err;
   // integer contractions where the level's tables allow them (FP64 Q1/Q2); the mode is timed
   // online over the level's first plain LHS launches, so choosing costs no extra launches
   int slot = -1;
-  int m = multigrid_fx_mode(P);
-  const char* env = std::getenv("PPF_CONTRACTION_MODE");
-  const bool fixed = env && env[0] >= '1' && env[0] <= '3';
-  if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed) m = online_mode_begin(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, 1, &slot);
-  L.fx_deriv = m != 3;
-  L.fx_int = m >= 2;
+  const int nm = lv.fx_lanes ? 4 : 3;
+  int m = multigrid_fx_mode(P, lv.fx_lanes);
+  const bool fixed = env_fx_mode(lv.fx_lanes) != 0;
+  if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed)
+    m = online_mode_begin(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, 1, &slot, nm);
+  set_fx_mode(L, m);
   const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
   const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
   PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));
   if (slot >= 0) PPF_CUDA(h, cudaEventRecord(lv.fx_ev[2 * slot], h->stream));  // after the memset
   const int rc = timed_cell_launch(h, lv.precision, mode, L, obj, smem);
   if (rc) return rc;
-  return online_mode_end(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, slot);
+  return online_mode_end(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, slot, nm);
 }
 
 static bool scaled(const LinearState& L) { return L.params.tolerance_type != 0; }
@@ -839,9 +841,12 @@ static int init_linear(ppf_handle h, int b) {
     }
     out_of[f] = 0;
     double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
-    auto tab = build_cell_tables(h->dim, h->k, lv.precision, lo, lv.h, slot_of, slot_comp0, out_of, out_row0);
+    auto tab = build_cell_tables(h->dim, h->k, lv.precision, lo, lv.h, slot_of, slot_comp0, out_of, out_row0,
+                                 B.plan[1].fx_rows, B.plan[1].val_rows);
     PPF_CUDA(h, cudaMalloc(&lv.tables, tab.size()));
     PPF_CUDA(h, cudaMemcpy(lv.tables, tab.data(), tab.size(), cudaMemcpyHostToDevice));
+    lv.fx_lanes = lv.precision == 0 && tables_lanes(tab, h->dim, h->k);
+    lv.h_tables = std::move(tab);
     for (void** p : {&lv.inv_diag, &lv.acc, &lv.x, &lv.b, &lv.r, &lv.w0, &lv.w1}) {
       rc = alloc_real(h, p, lv.len, lv.precision);
       if (rc) return rc;
@@ -1036,26 +1041,26 @@ int linear_solve(ppf_handle h, int b) {
     Lc.nrows_in = P.nrows_in;
     Lc.nrows_out = P.nrows_out;
     Lc.tables = P.d_tables;
+    Lc.tables_host = P.h_tables.data();
     Lc.timer = h->timer;
     Lc.block_id = (unsigned)B.desc.id;
     Lc.err = h->d_err;
     // the finest level is this operator on the same mesh: its timed mode if it has one; else
     // (an FP32 finest level) the plan's own mode, timed online over its first outer launches
     int slot = -1;
+    const int nm = P.fx_lanes ? 4 : 3;
     {
       const int lm = L.levels.empty() ? -1 : L.levels.back().fx_mode;
-      const char* env = std::getenv("PPF_CONTRACTION_MODE");
-      const bool fixed = env && env[0] >= '1' && env[0] <= '3';
-      int m = multigrid_fx_mode(P);
-      if (!fixed && lm > 0) m = lm;
-      else if (!fixed && P.fx) m = online_mode_begin(h, P.fx_mode, P.fx_timed, P.fx_ev, 1, &slot);
-      Lc.fx_deriv = m != 3;
-      Lc.fx_int = m >= 2;
+      const bool fixed = env_fx_mode(P.fx_lanes) != 0;
+      int m = multigrid_fx_mode(P, P.fx_lanes);
+      if (!fixed && lm > 0 && (lm != 4 || P.fx_lanes)) m = lm;
+      else if (!fixed && P.fx) m = online_mode_begin(h, P.fx_mode, P.fx_timed, P.fx_ev, 1, &slot, nm);
+      set_fx_mode(Lc, m);
     }
     const size_t smem = cell_smem(h->dim, h->k, 0, P.nrows_in, P.nrows_out);
     int rc = timed_cell_launch(h, 0, MODE_LHS, Lc, h->model_obj.data(), smem);
     if (rc) return rc;
-    rc = online_mode_end(h, P.fx_mode, P.fx_timed, P.fx_ev, slot);
+    rc = online_mode_end(h, P.fx_mode, P.fx_timed, P.fx_ev, slot, nm);
     if (rc) return rc;
     dim3 grid(grid_for(h->N), F.ncomp);
     level_finalize_kernel<double><<<grid, 256, 0, h->stream>>>(dst, F.acc, scaled(L) ? h->d_invm_sqrt : nullptr,

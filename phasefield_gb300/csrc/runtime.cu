@@ -126,10 +126,15 @@ GLRule gauss_lobatto(int n) {
 // PPF_FP64_CONTRACTIONS=1 asks for the FP64 contractions.
 template <int dim, int degree>
 static void fixed_point_tables(pg::CellTables<dim, degree, double>& t, const GLRule& g, const double* h, double detJ,
-                               unsigned int fx_rows) {
+                               unsigned int fx_rows, unsigned int val_rows) {
   constexpr int n = degree + 1, nq = pg::CellTables<dim, degree, double>::nq;
   t.fx = 0;
   t.fx_rows = fx_rows;
+  t.val_rows = val_rows;
+  for (int r = 0, nv = 0, ng = 0; r < pg::LANE_ROW_SLOTS; ++r) {
+    t.lane_vslot[r] = (signed char)(((val_rows >> r) & 1u) ? nv++ : -1);
+    t.lane_gslot[r] = (signed char)(((fx_rows >> r) & 1u) ? ng++ : -1);
+  }
   if (degree > 2) return;
   const char* env = std::getenv("PPF_FP64_CONTRACTIONS");
   if (env && env[0] == '1') return;
@@ -196,7 +201,8 @@ template <int dim, int degree>
 static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
                                               const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                               const signed char* slot_comp0, const signed char* out_of,
-                                              const signed char* out_row0, unsigned int fx_rows) {
+                                              const signed char* out_row0, unsigned int fx_rows,
+                                              unsigned int val_rows) {
   using Tab = pg::CellTables<dim, degree>;
   constexpr int n = degree + 1, nq = Tab::nq;
   Tab t;
@@ -236,7 +242,7 @@ static std::vector<unsigned char> tables_impl(const double* lo, const double* h,
   }
   for (int i = 0; i < n; ++i) t.gl_x[i] = g.x[i];
   t.vol = detJ;
-  fixed_point_tables<dim, degree>(t, g, h, detJ, fx_rows);
+  fixed_point_tables<dim, degree>(t, g, h, detJ, fx_rows, val_rows);
   std::memcpy(t.slot_of, slot_of, sizeof(t.slot_of));
   std::memcpy(t.slot_comp0, slot_comp0, sizeof(t.slot_comp0));
   std::memcpy(t.out_of, out_of, sizeof(t.out_of));
@@ -251,10 +257,10 @@ template <int dim, int degree>
 static std::vector<unsigned char> tables_impl_f32(const double* lo, const double* h,
                                                   const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                                   const signed char* slot_comp0, const signed char* out_of,
-                                                  const signed char* out_row0, unsigned int) {
+                                                  const signed char* out_row0, unsigned int, unsigned int) {
   using T64 = pg::CellTables<dim, degree, double>;
   using T32 = pg::CellTables<dim, degree, float>;
-  auto b = tables_impl<dim, degree>(lo, h, slot_of, slot_comp0, out_of, out_row0, 0u);
+  auto b = tables_impl<dim, degree>(lo, h, slot_of, slot_comp0, out_of, out_row0, 0u, 0xffffffffu);
   const T64& a = *reinterpret_cast<const T64*>(b.data());
   T32 t;
   std::memset(&t, 0, sizeof(t));
@@ -335,12 +341,12 @@ int env_fx_mode(bool lanes_ok) {
 std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
-                                             const signed char* out_row0, unsigned int fx_rows) {
+                                             const signed char* out_row0, unsigned int fx_rows, unsigned int val_rows) {
   if (precision == 1) {
-    PPF_DD_SWITCH(tables_impl_f32, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows)
+    PPF_DD_SWITCH(tables_impl_f32, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows, val_rows)
     return {};
   }
-  PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows)
+  PPF_DD_SWITCH(tables_impl, lo, h, slot_of, slot_comp0, out_of, out_row0, fx_rows, val_rows)
   return {};
 }
 
@@ -609,7 +615,8 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memset(out_of, -1, sizeof(out_of));
   std::memset(out_row0, 0, sizeof(out_row0));
   const int nf = (int)h->fields.size();
-  unsigned int fx_rows = 0;  // value rows read as gradients (fixed-point copies in the kernel)
+  unsigned int fx_rows = 0;   // value rows read as gradients (fixed-point copies in the kernel)
+  unsigned int val_rows = 0;  // value rows read as values or Hessians (double copies in the lane kernel)
   P.nslots = 0;
   P.nrows_in = 0;
   for (int f = 0; f < nf; ++f)
@@ -623,6 +630,8 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
       P.slot_age[P.nslots] = a;
       if (fl & PPF_DEP_GRADIENT)
         for (int c = 0; c < h->fields[f].ncomp && P.nrows_in + c < 32; ++c) fx_rows |= 1u << (P.nrows_in + c);
+      if (fl & (PPF_DEP_VALUE | PPF_DEP_HESSIAN))
+        for (int c = 0; c < h->fields[f].ncomp && P.nrows_in + c < 32; ++c) val_rows |= 1u << (P.nrows_in + c);
       P.nrows_in += h->fields[f].ncomp;
       P.nslots++;
     }
@@ -636,7 +645,7 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   }
   if (P.nrows_in + P.nrows_out > 127) return fail(h, PPF_ERR_UNSUPPORTED, "block too large");
   double lo[3] = {h->mesh.lower[0], h->mesh.lower[1], h->mesh.lower[2]};
-  auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0, fx_rows);
+  auto tab = build_cell_tables(h->dim, h->k, 0, lo, h->h, slot_of, slot_comp0, out_of, out_row0, fx_rows, val_rows);
   if (tab.empty()) return fail(h, PPF_ERR_UNSUPPORTED, "unsupported dim/degree");
   std::memcpy(P.slot_of, slot_of, sizeof(slot_of));
   std::memcpy(P.slot_comp0, slot_comp0, sizeof(slot_comp0));
@@ -644,6 +653,8 @@ static int plan_block(ppf_handle h, BlockState& B, int which) {
   std::memcpy(P.out_row0, out_row0, sizeof(out_row0));
   P.fx = tables_fx(tab, h->dim, h->k);
   P.fx_lanes = tables_lanes(tab, h->dim, h->k);
+  P.fx_rows = fx_rows;
+  P.val_rows = val_rows;
   P.fx_mode = -1;
   P.fx_timed = 0;
   for (auto& ev : P.fx_ev)

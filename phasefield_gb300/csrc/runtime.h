@@ -31,11 +31,13 @@ void register_model(const ModelOps* ops);
 int cell_threads(int dim, int degree);
 size_t cell_smem(int dim, int degree, int precision, int nrows_in, int nrows_out);
 // builds CellTables<dim,degree,number> bytes (precision 0 FP64, 1 FP32)
-// fx_rows: value rows the FP64 Q1/Q2 kernels keep a fixed-point copy of (rows read as gradients)
+// fx_rows: value rows the FP64 Q1/Q2 kernels keep a fixed-point copy of (rows read as gradients);
+// val_rows: value rows the lane kernel keeps a double copy of (rows read as values or Hessians)
 std::vector<unsigned char> build_cell_tables(int dim, int degree, int precision, const double* lo, const double* h,
                                              const signed char slot_of[pg::MAX_FIELDS][pg::NAGE],
                                              const signed char* slot_comp0, const signed char* out_of,
-                                             const signed char* out_row0, unsigned int fx_rows = 0xffffffffu);
+                                             const signed char* out_row0, unsigned int fx_rows = 0xffffffffu,
+                                             unsigned int val_rows = 0xffffffffu);
 // whether FP64 tables allow the lane kernel (integer contractions, cubic cells)
 bool tables_lanes(const std::vector<unsigned char>& tab, int dim, int degree);
 // the launch-record fields of contraction mode m (1-4)
