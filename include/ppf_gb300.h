@@ -185,12 +185,14 @@ int ppf_upload_state_async(ppf_handle h, int f, int age, const double* host, int
  *   ppf_upload_state_staged copies `host` (lattice order, pinned memory for overlap) into a
  *     device staging buffer of (field f, age) on the handle's upload stream right away, as soon
  *     as the previous staged upload of that (f, age) was consumed; the next run, before its
- *     first block, waits for it and copies it into the state. `host` must stay unchanged until
- *     ppf_wait returned (or the run that consumes it ended).
+ *     first block, waits for it and swaps the staging buffer in as the state of that age (the
+ *     state's former buffer becomes the staging buffer of the next upload; no device copy).
+ *     `host` must stay unchanged until ppf_wait returned (or the run that consumes it ended).
+ *     Device pointers of the state (ppf_state_device_ptr) change at that run.
  *   ppf_run_async queues the increments of ppf_run and returns without waiting: streamed
- *     outputs (ppf_set_output_stream) are copied out of a per-field staging copy, so the next
- *     increment may start while the copy to the host is in flight; errors are reported by
- *     ppf_wait.
+ *     outputs (ppf_set_output_stream) are copied out of a per-field staging copy, which the
+ *     finalize kernel of an explicit block writes beside the state, so the next increment may
+ *     start while the copy to the host is in flight; errors are reported by ppf_wait.
  *   ppf_wait waits for the queued runs, staged uploads and streamed-output copies, and returns
  *     their status (PPF_ERR_NAN, PPF_ERR_DEPENDENCY) like ppf_run. The host buffers of streamed
  *     outputs hold the last increment's results once it returned.
@@ -433,7 +435,8 @@ long long ppf_checkpoint_schedule_cost(int n_steps, int n_snapshots);
  * output is requested and kernel timing is off. */
 int ppf_set_use_graph(ppf_handle h, int on);
 
-/* Device pointer of a field state (for zero-copy callers), valid until the next rotation. */
+/* Device pointer of a field state (for zero-copy callers), valid until the next rotation or
+ * the next run that consumes a staged upload (ppf_upload_state_staged) of that field. */
 int ppf_state_device_ptr(ppf_handle h, int field, int age, double** out);
 
 /* Wait for all work queued on the handle's stream. */

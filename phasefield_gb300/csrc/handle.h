@@ -207,6 +207,8 @@ struct ppf_handle_s {
   ppf::AmrState* amr = nullptr;      // adaptive mesh (ppf_set_adaptivity), else null
   long long mesh_version = 0;
   long long graph_mesh_version = -1;  // mesh the increment graph was captured on
+  long long state_version = 0;        // bumped when a staged upload swaps a state buffer in
+  long long graph_state_version = -1; // state buffers the increment graph was captured on
   // CUDA graph of the explicit increment loop
   prismspf::SimulationTimer* d_timer = nullptr;
   cudaGraphExec_t run_graph = nullptr;

@@ -371,9 +371,12 @@ size_t cell_smem(int dim, int degree, int precision, int nrows_in, int nrows_out
 
 // u = invM (.) acc with constraints: masters/free rows scale their own accumulator, periodic
 // images copy their master's result, Dirichlet rows take their value.
+// With u2 set (a queued run streaming the field out) the result is written there as well, so the
+// copy to the host reads a buffer the following increments do not touch.
 __global__ void finalize_explicit_kernel(double* __restrict__ u, const double* __restrict__ acc,
                                          const double* __restrict__ invm, const int* __restrict__ cmap,
-                                         const double* __restrict__ dvals, long long N, int* err) {
+                                         const double* __restrict__ dvals, long long N, int* err,
+                                         double* __restrict__ u2) {
   const int c = blockIdx.y;
   const long long base = c * N;
   int bad = 0;
@@ -385,6 +388,7 @@ __global__ void finalize_explicit_kernel(double* __restrict__ u, const double* _
     else v = dvals[-1 - cm];
     bad |= !isfinite(v);
     u[gi] = v;
+    if (u2) u2[gi] = v;
   }
   if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(err, int(pg::ERR_NONFINITE));
 }
@@ -834,8 +838,9 @@ unsigned grid_for(long long n) {
 
 static int explicit_solve(ppf_handle h, int b);
 int explicit_solve_entry(ppf_handle h, int b) { return explicit_solve(h, b); }
-int stream_field_out(ppf_handle h, FieldState& F, const double* src);
+int stream_field_out(ppf_handle h, FieldState& F, const double* src, bool staged = false);
 int finish_streamed_outputs(ppf_handle h);
+static int ensure_out_stage(ppf_handle h, FieldState& F);
 
 static int explicit_solve(ppf_handle h, int b) {
   BlockState& B = h->blocks[b];
@@ -852,14 +857,22 @@ static int explicit_solve(ppf_handle h, int b) {
       if (rc) return rc;
       continue;
     }
+    // a queued run streaming this field out: the finalize writes the output staging buffer too
+    // (once the previous increment's copy to the host has left it)
+    const bool staged = F.stream_out && h->async_run;
+    if (staged) {
+      rc = ensure_out_stage(h, F);
+      if (rc) return rc;
+      PPF_CUDA(h, cudaStreamWaitEvent(h->stream, F.out_free, 0));
+    }
     dim3 grid(grid_for(h->N), F.ncomp);
     finalize_explicit_kernel<<<grid, 256, 0, h->stream>>>(F.cur, F.acc, h->d_invm, F.constrained ? F.cmap : nullptr,
-                                                          F.dvals, h->N, h->d_err);
+                                                          F.dvals, h->N, h->d_err, staged ? F.out_stage : nullptr);
     PPF_CUDA(h, cudaGetLastError());
     h->all_launches++;
     if (F.stream_out) {
       // the field is final: copy it out on the copy stream while the later blocks compute
-      rc = stream_field_out(h, F, F.cur);
+      rc = stream_field_out(h, F, staged ? F.out_stage : F.cur, staged);
       if (rc) return rc;
     }
   }
@@ -871,17 +884,28 @@ static int explicit_solve(ppf_handle h, int b) {
 // (ppf_run_async) the field is first copied on the device into its output staging buffer
 // (once the previous increment's copy out of it ended), so later increments may overwrite the
 // state while the copy to the host is in flight.
-int stream_field_out(ppf_handle h, FieldState& F, const double* src) {
+static int ensure_out_stage(ppf_handle h, FieldState& F) {
   if (!h->copy_stream) {
     PPF_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
     PPF_CUDA(h, cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
   }
-  if (h->async_run) {
-    if (!F.out_stage) {
-      PPF_CUDA(h, cudaMalloc(&F.out_stage, sizeof(double) * F.len));
-      PPF_CUDA(h, cudaEventCreateWithFlags(&F.out_free, cudaEventDisableTiming));
-      PPF_CUDA(h, cudaEventRecord(F.out_free, h->copy_stream));
-    }
+  if (!F.out_stage) {
+    PPF_CUDA(h, cudaMalloc(&F.out_stage, sizeof(double) * F.len));
+    PPF_CUDA(h, cudaEventCreateWithFlags(&F.out_free, cudaEventDisableTiming));
+    PPF_CUDA(h, cudaEventRecord(F.out_free, h->copy_stream));
+  }
+  return PPF_OK;
+}
+
+// `staged`: src is already the field's output staging buffer, written by the finalize kernel
+int stream_field_out(ppf_handle h, FieldState& F, const double* src, bool staged) {
+  if (!h->copy_stream) {
+    PPF_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    PPF_CUDA(h, cudaEventCreateWithFlags(&h->copy_ev, cudaEventDisableTiming));
+  }
+  if (h->async_run && !staged) {
+    const int rc = ensure_out_stage(h, F);
+    if (rc) return rc;
     PPF_CUDA(h, cudaStreamWaitEvent(h->stream, F.out_free, 0));
     PPF_CUDA(h, cudaMemcpyAsync(F.out_stage, src, sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
     src = F.out_stage;
@@ -895,19 +919,22 @@ int stream_field_out(ppf_handle h, FieldState& F, const double* src) {
   return PPF_OK;
 }
 
-// Staged uploads waiting for the next run: the handle's stream waits for each upload, copies
-// the staging buffer into the state of its age, and marks the buffer free for the next upload.
+// Staged uploads waiting for the next run: the handle's stream waits for each upload, and the
+// staging buffer becomes the state of its age while the state's former buffer becomes the
+// staging buffer, free for the next upload once the work queued so far (which alone used it)
+// has run. The state's buffers change, so an increment graph captured on them is recaptured.
 int consume_staged_uploads(ppf_handle h) {
   for (size_t f = 0; f < h->fields.size(); ++f) {
     FieldState& F = h->fields[f];
     for (int a = 0; a < 5; ++a) {
       if (!F.in_pending[a]) continue;
-      double* dst = state_ptr(h, (int)f, a);
-      if (!dst) return fail(h, PPF_ERR_ARG, "staged upload for an age that is not stored");
+      double** slot = a == 0 ? &F.cur : (a <= 4 && a <= F.n_old ? &F.old[a - 1] : nullptr);
+      if (!slot || !*slot) return fail(h, PPF_ERR_ARG, "staged upload for an age that is not stored");
       PPF_CUDA(h, cudaStreamWaitEvent(h->stream, F.in_ready[a], 0));
-      PPF_CUDA(h, cudaMemcpyAsync(dst, F.in_stage[a], sizeof(double) * F.len, cudaMemcpyDeviceToDevice, h->stream));
+      std::swap(*slot, F.in_stage[a]);
       PPF_CUDA(h, cudaEventRecord(F.in_free[a], h->stream));
       F.in_pending[a] = false;
+      h->state_version++;
     }
   }
   return PPF_OK;
@@ -1480,6 +1507,7 @@ static int capture_graph(ppf_handle h) {
   h->all_launches = launches0;
   h->graph_stream = h->stream;
   h->graph_mesh_version = h->mesh_version;
+  h->graph_state_version = h->state_version;
   return PPF_OK;
 }
 
@@ -1512,7 +1540,7 @@ static int run_increments(ppf_handle h, unsigned int n_increments, int output_ev
       const unsigned remaining = last >= inc ? last - inc + 1 : 0;
       if (remaining >= (unsigned)period) {
         if (!h->run_graph || h->graph_stream != h->stream || h->graph_phase != h->rot_count % period ||
-            h->graph_mesh_version != h->mesh_version) {
+            h->graph_mesh_version != h->mesh_version || h->graph_state_version != h->state_version) {
           int rc = capture_graph(h);
           if (rc) return rc;
         }

@@ -332,7 +332,8 @@ class Problem:
 
     def device_view(self, f: int, age: int = 0):
         """The device vector of field f at `age` as a torch CUDA tensor (no copy). Valid until
-        the next age rotation; the caller orders its work with the handle's stream."""
+        the next age rotation or the next run that consumes a staged upload of the field; the
+        caller orders its work with the handle's stream."""
         import torch
         ptr = C.c_void_p()
         self._check(self.lib.ppf_state_device_ptr(self.h, f, age, C.byref(ptr)))

@@ -96,3 +96,35 @@ def test_wait_reports_a_nonfinite_increment(gpu_lib):
         assert p.lib.ppf_upload_state_staged(p.h, f, 1, _ptr(pins[f])) == capi.PPF_OK
     assert p.lib.ppf_run_async(p.h, 1, 0) == capi.PPF_OK
     assert p.lib.ppf_wait(p.h) == capi.PPF_ERR_NAN
+
+
+def test_staged_upload_before_graph_replays(gpu_lib, monkeypatch):
+    """A staged upload swaps a new buffer into the state: an increment graph captured on the
+    former buffers must not be replayed. Runs of several increments (graph replays from increment
+    2 on) after staged uploads give the blocking path's fields."""
+    monkeypatch.setenv("PPF_CONTRACTION_MODE", "1")
+    wl = _wl()
+    ref = wl.make_problem()
+    p = wl.make_problem()
+    for h in (ref, p):
+        h.solve(0)
+    N = ref.n_nodes
+    sets = _inputs(N)
+    import torch
+    pin_in = [[torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in s] for s in sets]
+    lib = p.lib
+    inc = 0
+    for r in range(3):
+        c, mu = sets[r % 2]
+        ref.upload(0, c, age=1)
+        ref.upload(1, mu, age=1)
+        for f in (0, 1):
+            assert lib.ppf_upload_state_staged(p.h, f, 1, _ptr(pin_in[r % 2][f])) == capi.PPF_OK
+        inc += 6
+        ref.solve(inc)
+        assert lib.ppf_run_async(p.h, inc, 0) == capi.PPF_OK
+        assert lib.ppf_wait(p.h) == capi.PPF_OK
+        # six increments of atomic-accumulation rounding (a graph replayed on the former
+        # buffers would differ by O(1))
+        for f in (0, 1):
+            assert rel_l2(p.download_solution(f), ref.download_solution(f)) < 1e-12, (r, f)
