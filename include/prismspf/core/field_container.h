@@ -112,6 +112,8 @@ struct CellCtx {
   int cpt = 0;
   int lean = 0;
   int qi[3] = {0, 0, 0};
+  // value terms stored unweighted (a kernel integrating them in fixed point), on any layout
+  int raw_values = 0;
 };
 
 }  // namespace gpu
@@ -320,7 +322,7 @@ class FieldContainer {
   PPF_HD void set_value_term(unsigned int field_index, const ScalarValue& val) {
     const int o = out_row(field_index);
     if (o < 0) return;
-    ctx.outs[o * ctx.stride + slot()] = ctx.lean ? val.v : val.v * ctx.tab->jxw[ctx.q];
+    ctx.outs[o * ctx.stride + slot()] = (ctx.lean || ctx.raw_values) ? val.v : val.v * ctx.tab->jxw[ctx.q];
     ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
   }
 
@@ -328,7 +330,8 @@ class FieldContainer {
     const int o = out_row(field_index);
     if (o < 0) return;
     for (int c = 0; c < int(dim); ++c)
-      ctx.outs[(o + c * (1 + dim)) * ctx.stride + slot()] = ctx.lean ? val[c].v : val[c].v * ctx.tab->jxw[ctx.q];
+      ctx.outs[(o + c * (1 + dim)) * ctx.stride + slot()] =
+          (ctx.lean || ctx.raw_values) ? val[c].v : val[c].v * ctx.tab->jxw[ctx.q];
     ctx.submitted |= 1 << (2 * ctx.tab->out_of[field_index]);
   }
 

@@ -28,6 +28,8 @@
 #include "handle.h"
 #include "models.cuh"
 
+#include <prismspf/gpu/cell_kernel_lanes.cuh>
+
 namespace ppf {
 namespace {
 
@@ -66,8 +68,13 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
   double* outs = vals + CPB * nq;
   long long* vals_fx = reinterpret_cast<long long*>(outs + 3 * CPB * nq);  // integer derivatives
   int* ex_in = reinterpret_cast<int*>(vals_fx + CPB * nq);                 // per-cell block exponent
+  int* ex_out = ex_in + CPB;                                               // of the submitted terms
   const int t = threadIdx.x;
-  if (P.fx && t < CPB) ex_in[t] = 0;  // last read before the previous tile's closing barrier
+  // last read before the previous tile's closing barrier
+  if (P.fx && t < CPB) {
+    ex_in[t] = 0;
+    ex_out[t] = 0;
+  }
   // stage the instance's tables (built on the host for its mesh spacing)
   {
     const unsigned int* src = reinterpret_cast<const unsigned int*>(P.tables + I.tab_off);
@@ -116,10 +123,14 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
   ctx.cell[2] = 0;
   ctx.err = nullptr;
   ctx.submitted = 0;
+  // integer integration of the value and gradient terms where the tables allow it (square cells):
+  // the lane kernel's arithmetic (prismspf/gpu/cell_kernel_lanes.cuh) on this layout
+  const bool fxi = P.fx && tab->fx_lanes;
   if (P.fx) {
     ctx.vals_fx = vals_fx;
     ctx.ex_in = ex_in;
     ctx.cpb = CPB;
+    ctx.raw_values = fxi ? 1 : 0;
   }
   if (active) {
     AllenCahn<2, degree, double> pde{I.m_well, I.kappa};
@@ -127,6 +138,49 @@ __device__ void ens_tile(const EnsLaunch& P, const EnsInstance& I, long long cel
     pde.compute_rhs(fc, SimulationTimer(P.dt, 0.0), 1u);
   }
   __syncthreads();
+  if (fxi) {
+    namespace fx = pg::fx;
+    constexpr int TOPT = LANE_TOP_TERMS;
+    const int S = CPB * nq;
+    const int p = lc * nq + q;
+    if (active) {
+      // block exponent of the cell's terms: the value term as h v, the two gradient terms
+      const int ev = fx::exponent(outs[p]);
+      const int eh = ev + tab->hk + (tab->hpow2 ? 0 : 1);
+      int e = ev == 0 ? 0 : (ev == fx::EXP_NONFINITE || eh >= fx::EXP_NONFINITE ? fx::EXP_NONFINITE : max(eh, 0));
+      e = max(e, fx::exponent(outs[S + p]));
+      e = max(e, fx::exponent(outs[2 * S + p]));
+      atomicMax(&ex_out[lc], e);
+    }
+    __syncthreads();
+    long long* ox = reinterpret_cast<long long*>(outs);
+    if (active) {
+      const int E = ex_out[lc];
+      const double v = outs[p];
+      ox[p] = tab->hpow2 ? fx::to_fixed_fast<TOPT>(v, E - tab->hk) : fx::to_fixed_scaled<TOPT>(v, E, tab->hsig, tab->hk);
+      ox[S + p] = fx::to_fixed_fast<TOPT>(outs[S + p], E);
+      ox[2 * S + p] = fx::to_fixed_fast<TOPT>(outs[2 * S + p], E);
+    }
+    __syncthreads();
+    if (active) {
+      const int E = ex_out[lc];
+      long long T = (long long)((unsigned long long)ox[p] << tab->vw_sh[q]);
+      {
+        const long long* g = ox + S + lc * nq + (q - qa);
+        const long long L = lane_line_integral<n>(qa, g[0], g[1], n > 2 ? g[2] : 0ll);
+        T += (long long)((unsigned long long)L << tab->wo_sh[0][q]);
+      }
+      {
+        const long long* g = ox + 2 * S + lc * nq + (q - qb * n);
+        const long long L = lane_line_integral<n>(qb, g[0], g[n], n > 2 ? g[2 * n] : 0ll);
+        T += (long long)((unsigned long long)L << tab->wo_sh[1][q]);
+      }
+      const double rr = fx::to_double_fast(T, E - 1023 - TOPT + tab->ik[0], tab->isig[0], true);
+      atomicAdd(P.acc_out + I.off + node, E == fx::EXP_NONFINITE ? fx::quiet_nan() : rr);
+    }
+    __syncthreads();
+    return;
+  }
   if (active) {
     double r = outs[lc * nq + q];
     {
@@ -164,8 +218,8 @@ __global__ void __launch_bounds__(THREADS) ensemble_step_kernel(const EnsLaunch 
 template <int CPB1, int CPB2>
 size_t ens_smem_bytes() {
   // tables, values, three output rows, the fixed-point values and the per-cell exponents
-  const size_t t1 = (sizeof(pg::CellTables<2, 1, double>) + 7) / 8 * 8 + 8 * 5 * CPB1 * 4 + 4 * CPB1;
-  const size_t t2 = (sizeof(pg::CellTables<2, 2, double>) + 7) / 8 * 8 + 8 * 5 * CPB2 * 9 + 4 * CPB2;
+  const size_t t1 = (sizeof(pg::CellTables<2, 1, double>) + 7) / 8 * 8 + 8 * 5 * CPB1 * 4 + 8 * CPB1;
+  const size_t t2 = (sizeof(pg::CellTables<2, 2, double>) + 7) / 8 * 8 + 8 * 5 * CPB2 * 9 + 8 * CPB2;
   return std::max(t1, t2) + 64;
 }
 
