@@ -241,11 +241,15 @@ set Model constant n_grains = 12, INT
     assert rel_l2(to_lattice(v1, wl.mesh, "f_tot"), o.get(2, 0)) < 1e-8
 
 
-def test_derivative_getters_are_exact_on_quadratics(gpu_lib, tmp_path):
+@pytest.mark.parametrize("mode", [None, "4"])
+def test_derivative_getters_are_exact_on_quadratics(gpu_lib, tmp_path, monkeypatch, mode):
     """Hessian, Hessian diagonal, Laplacian, divergence, curl, symmetric gradient, quadrature
     point and element volume through the drop-in, on inputs FE_Q(2) represents exactly (two
-    post-processing blocks)."""
+    post-processing blocks); with the contraction mode timed, and fixed to the lane kernel (mode
+    4: its row layout for values, Hessians and gradients)."""
     from phasefield_gb300 import app_build
+    if mode:
+        monkeypatch.setenv("PPF_CONTRACTION_MODE", mode)
     src = ROOT / "tests" / "dropin" / "derivatives"
     exe = app_build.compile_app(src, tmp_path / "derivatives")
     (tmp_path / "parameters.prm").write_text("""
