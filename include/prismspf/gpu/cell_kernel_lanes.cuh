@@ -342,6 +342,137 @@ __global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
   }
 }
 
+// FP32 operators (the smoothing levels of a mixed-precision V-cycle) on the same layout: 32 cells
+// a tile, a line of each cell per thread, plain FP32 contractions (derivatives from the nodal
+// values, integration with the tables' jdt weights), so a tile needs two barriers (nodal values;
+// submitted terms). Any cell shape.
+template <int dim, int degree>
+__host__ __device__ constexpr size_t lane_f32_smem_bytes(int nrows_in, int nrows_out) {
+  using S = LaneShape<dim, degree>;
+  return (size_t)S::nq * LANE_CPT * 4 * (size_t)(nrows_in + nrows_out);
+}
+
+template <class PDE, int dim, int degree, int MODE, int MINB>
+__global__ void __launch_bounds__(LaneShape<dim, degree>::threads, MINB)
+    cell_kernel_lanes_f32(const __grid_constant__ CellLaunch P, const __grid_constant__ PDE pde,
+                          const __grid_constant__ pg::CellTables<dim, degree, float> T,
+                          const __grid_constant__ LaneRows R) {
+  static_assert(degree <= 2 && MODE == MODE_LHS, "the FP32 lane kernel covers Q1/Q2 LHS launches");
+  using S = LaneShape<dim, degree>;
+  using Tab = pg::CellTables<dim, degree, float>;
+  constexpr int n = S::n, nq = S::nq, cols = S::cols, k = degree, CPT = LANE_CPT;
+  constexpr int ROW = nq * CPT;
+  constexpr int JS = cols * CPT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Tab* tab = &T;
+  float* vals = reinterpret_cast<float*>(smem_raw);  // [nin][q][cell]
+  float* outs = vals + R.nin * ROW;                  // [out rows][q][cell]
+  const int t = threadIdx.x;
+  const int lc = t & 31;
+  const int w = t >> 5;
+  const int p0 = w * CPT + lc;
+  const int qa = w % n;
+  const int qb = dim > 2 ? w / n : 0;
+  const unsigned int nn0 = (unsigned int)P.nn[0], nn1 = (unsigned int)P.nn[1];
+  const unsigned int lstride = dim > 2 ? nn0 * nn1 : nn0;
+  const unsigned int ncells = (unsigned int)P.ncells;
+  const unsigned int ntiles = (ncells + CPT - 1) / CPT;
+
+  for (unsigned int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const unsigned int cell_t = tile * CPT + lc;
+    const bool active = cell_t < ncells;
+    const unsigned int cell = active ? cell_t : ncells - 1;
+    int cx, cy = 0, cz = 0;
+    {
+      const unsigned int q0 = (__umulhi(cell, R.div_m[0]) + cell) >> R.div_l[0];
+      cx = (int)(cell - q0 * (unsigned int)P.nc[0]);
+      if (dim == 2) cy = (int)q0;
+      if (dim > 2) {
+        const unsigned int q1 = (__umulhi(q0, R.div_m[1]) + q0) >> R.div_l[1];
+        cy = (int)(q0 - q1 * (unsigned int)P.nc[1]);
+        cz = (int)q1;
+      }
+    }
+    const unsigned int node0 = dim > 2 ? ((unsigned int)(k * cz) * nn1 + (unsigned int)(k * cy + qb)) * nn0 + (unsigned int)(k * cx + qa)
+                                       : (unsigned int)(k * cy) * nn0 + (unsigned int)(k * cx + qa);
+    // the previous tile's integration read the submitted terms and values: done by all threads
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < LANE_MAX_IN; ++r) {
+      if (r < R.nin) {
+        const float* base = reinterpret_cast<const float*>(R.in_base[r]);
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          const unsigned int idx = node0 + (unsigned int)j * lstride + R.in_off[r];
+          float v;
+          if (R.in_cmap[r]) {
+            const int m = __ldg(R.in_cmap[r] + idx);
+            const float own = __ldg(base + idx);
+            v = m == (int)idx ? own : (m >= 0 ? __ldg(base + m) : 0.f);
+          } else {
+            v = __ldg(base + idx);
+          }
+          vals[r * ROW + p0 + j * JS] = v;
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o)
+      if (o < R.nout)
+#pragma unroll
+        for (int i = 0; i <= dim; ++i)
+#pragma unroll
+          for (int j = 0; j < n; ++j) outs[(R.out_row[o] + i) * ROW + p0 + j * JS] = 0.f;
+    __syncthreads();  // nodal values visible
+
+    const SimulationTimer& timer = P.timer_dev ? *P.timer_dev : P.timer;
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+      pg::CellCtx<dim, degree, float> ctx;
+      ctx.tab = tab;
+      ctx.vals = vals;
+      ctx.outs = outs;
+      ctx.stride = ROW;
+      ctx.lc = lc;
+      ctx.q = w + j * cols;
+      ctx.cell[0] = cx;
+      ctx.cell[1] = cy;
+      ctx.cell[2] = cz;
+      ctx.err = P.err;
+      ctx.submitted = 0;
+      ctx.cpt = CPT;
+      FieldContainer<dim, degree, float> fc(ctx);
+      pde.compute_lhs(fc, timer, P.block_id);
+    }
+    __syncthreads();  // submitted terms visible
+
+    // integrate (the tables' jdt weights) and scatter
+#pragma unroll
+    for (int o = 0; o < LANE_MAX_OUT; ++o) {
+      if (o < R.nout) {
+        const int rv = R.out_row[o];
+#pragma unroll
+        for (int j = 0; j < n; ++j) {
+          const int q = w + j * cols;
+          const int qi[3] = {qa, dim > 2 ? qb : j, dim > 2 ? j : 0};
+          float r = outs[rv * ROW + p0 + j * JS];
+#pragma unroll
+          for (int d = 0; d < dim; ++d) {
+            const int sd = d == 0 ? 1 : (d == 1 ? n : n * n);
+            const float* g = outs + (rv + 1 + d) * ROW + (q - qi[d] * sd) * CPT + lc;
+            const float* wt = tab->jdt[d][q];
+#pragma unroll
+            for (int m = 0; m < n; ++m) r = fmaf(wt[m], g[m * sd * CPT], r);
+          }
+          const unsigned int idx = node0 + (unsigned int)j * lstride + R.out_off[o];
+          const int target = R.out_cmap[o] ? __ldg(R.out_cmap[o] + idx) : (int)idx;
+          if (active && target >= 0) atomicAdd(reinterpret_cast<float*>(R.out_acc[o]) + target, r);
+        }
+      }
+    }
+  }
+}
+
 // the flat row lists of a launch record; false when they exceed the lane kernel's limits
 inline bool lane_rows(const CellLaunch& P, int dim, LaneRows* R) {
   std::memset(R, 0, sizeof(*R));
@@ -414,6 +545,53 @@ cudaError_t launch_lanes(const CellLaunch& P, const LaneRows& R, const void* obj
                                                 *reinterpret_cast<const pg::CellTables<dim, degree, double>*>(P.tables_host),
                                                 R);
   return cudaGetLastError();
+}
+
+template <class PDE, int dim, int degree, int MINB>
+cudaError_t launch_lanes_f32(const CellLaunch& P, const LaneRows& R, const void* obj, cudaStream_t s) {
+  using S = LaneShape<dim, degree>;
+  auto kern = cell_kernel_lanes_f32<PDE, dim, degree, MODE_LHS, MINB>;
+  const size_t smem = lane_f32_smem_bytes<dim, degree>(R.nin, P.nrows_out);
+  constexpr int MAX_DEVICES = 64;
+  static size_t attr_smem_of[MAX_DEVICES] = {};
+  static int occ_of[MAX_DEVICES] = {};
+  static int sms_of[MAX_DEVICES] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  size_t& attr_smem = attr_smem_of[dev];
+  int& occ = occ_of[dev];
+  int& sms = sms_of[dev];
+  if (smem > attr_smem) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr_smem = smem;
+    occ = 0;
+  }
+  if (occ == 0) {
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, S::threads, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  const long long ntiles = (P.ncells + LANE_CPT - 1) / LANE_CPT;
+  long long grid = (long long)sms * occ;
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, S::threads, smem, s>>>(P, *reinterpret_cast<const PDE*>(obj),
+                                                *reinterpret_cast<const pg::CellTables<dim, degree, float>*>(P.tables_host),
+                                                R);
+  return cudaGetLastError();
+}
+
+// the FP32 lane kernel for an FP32 Q1/Q2 left-hand side, or cudaErrorNotSupported
+template <class PDE, int dim, int degree>
+cudaError_t launch_cell_kernel_lanes_f32_impl(const CellLaunch& P, const void* obj, cudaStream_t s) {
+  constexpr int MINB = CellLaneMinBlocks<PDE, LaneShape<dim, degree>::threads>::value;
+  LaneRows R;
+  if (!P.tables_host || !lane_rows(P, dim, &R)) return cudaErrorNotSupported;
+  if (lane_f32_smem_bytes<dim, degree>(R.nin, P.nrows_out) > 232448) return cudaErrorNotSupported;
+  return launch_lanes_f32<PDE, dim, degree, MINB>(P, R, obj, s);
 }
 
 // launches the lane kernel, or returns cudaErrorNotSupported when the launch's rows exceed its

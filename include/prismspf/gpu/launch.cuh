@@ -89,6 +89,13 @@ inline bool use_warp_cell_kernel() {
 // for it (contraction modes 2 and 3 of FP64 Q1/Q2 operators)
 template <class PDE, int dim, int degree, int mode, typename number>
 cudaError_t launch_cell_kernel(const CellLaunch& P, const void* obj, size_t smem, cudaStream_t s) {
+  if constexpr (std::is_same<number, float>::value && degree <= 2 && mode == MODE_LHS) {
+    // FP32 left-hand sides (mixed-precision smoothing levels) on the lane layout when asked
+    if (P.fx_lanes) {
+      const cudaError_t e = launch_cell_kernel_lanes_f32_impl<PDE, dim, degree>(P, obj, s);
+      if (e != cudaErrorNotSupported) return e;
+    }
+  }
   if constexpr (cell_fx_capable<dim, degree, number>() && mode != MODE_DIAG) {
     if (P.fx_lanes) {
       // the lane kernel when its rows and tile fit (and the host tables came with the launch),

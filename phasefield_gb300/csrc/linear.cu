@@ -455,6 +455,12 @@ static int level_cell_launch(ppf_handle h, BlockState& B, MGLevel& lv, int mode,
   if (P.fx && lv.precision == 0 && mode == MODE_LHS && !fixed)
     m = online_mode_begin(h, lv.fx_mode, lv.fx_timed, lv.fx_ev, 1, &slot, nm);
   set_fx_mode(L, m);
+  // FP32 levels (mixed precision) run the FP32 lane kernel unless PPF_CONTRACTION_MODE fixes one
+  // of the thread-block modes 1-3
+  if (lv.precision == 1) {
+    const int e = env_fx_mode(true);
+    L.fx_lanes = e == 0 || e == 4;
+  }
   const size_t smem = cell_smem(h->dim, h->k, lv.precision, P.nrows_in, P.nrows_out);
   const void* obj = lv.precision ? h->model_obj_f32.data() : h->model_obj.data();
   PPF_CUDA(h, cudaMemsetAsync(lv.acc, 0, lv.len * esize(lv.precision), h->stream));

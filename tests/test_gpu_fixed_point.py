@@ -229,3 +229,36 @@ def test_derivative_error_is_absolute_in_the_cell_maximum(gpu_lib, mode):
         hk = np.floor(np.log2(h))
         bound = bound + 2.0 ** (np.floor(np.log2(gmax)) + hk + 1 - 52) / h
     assert np.all(np.abs(fixed - exact) <= bound)
+
+
+@pytest.mark.parametrize("dim,degree,sub", [(3, 2, (3, 1, 2)), (3, 1, (5, 3, 1)), (2, 2, (3, 5, 1)), (2, 1, (7, 3, 1))])
+def test_lane_kernel_partial_tiles(gpu_lib, dim, degree, sub):
+    """The lane kernel on lattices of square cells whose cell count is not a multiple of its
+    32-cell tile (the last tile's spare lanes recompute the last cell and scatter nothing), with
+    different cell counts per direction: both blocks' applies and five steps against the oracle."""
+    size = 4.0 * np.array(sub[:dim], dtype=float)
+    wl = W.cahn_hilliard_3d(refine=1 if dim == 3 else 2, degree=degree, dim=dim, size=1.0, subdivisions=sub[:dim] + (1,) * (3 - dim))
+    wl.mesh.size = tuple(size) + (1.0,) * (3 - dim)
+    with env(PPF_CONTRACTION_MODE="4"):
+        p = wl.make_problem()
+        o = po.Oracle(wl)
+        assert p.n_cells % 32 != 0
+        rng = np.random.default_rng(17)
+        mu = rng.uniform(-1, 1, p.n_nodes)
+        for f, v in ((0, wl.initial[0]), (1, mu)):
+            p.upload(f, v, age=1)
+            o.set(f, v, age=1)
+        p.upload(0, wl.initial[0], age=0)
+        o.set(0, wl.initial[0], age=0)
+        for b in (0, 1):
+            got = p.apply(b, 0, None, scale=1)
+            ref = o.apply(b, 0, None, scale=1)
+            assert rel_l2(got, ref) < APPLY_TOL, b
+            assert p.contraction_mode(b, 0) == 4
+        p.close()
+        p = wl.make_problem()
+        p.solve(5)
+        o = po.Oracle(wl)
+        assert o.run(5) == 0
+        for f in (0, 1):
+            assert rel_l2(p.download(f, age=1), o.get(f, 1)) < 1e-9, f
