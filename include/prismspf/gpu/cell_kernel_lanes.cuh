@@ -65,10 +65,12 @@ constexpr int LANE_CPT = 32;  // cells per tile
 constexpr int LANE_TOP_TERMS = 52;
 
 // An operator may ask for a register budget (`cell_lane_min_blocks`, resident blocks per SM);
-// the default aims at about 40 registers a thread.
+// the default aims at about 48 registers a thread (Cahn-Hilliard Q2 3-D: 4 blocks of 288 threads
+// at 46 registers measured 0.210 ms per launch against 0.218 ms for 5 blocks at 38 registers,
+// which the shared memory would allow)
 template <class PDE, int threads, class = void>
 struct CellLaneMinBlocks {
-  static constexpr int value = 65536 / (threads * 40) > 0 ? (65536 / (threads * 40) < 32 ? 65536 / (threads * 40) : 32) : 1;
+  static constexpr int value = 65536 / (threads * 48) > 0 ? (65536 / (threads * 48) < 32 ? 65536 / (threads * 48) : 32) : 1;
 };
 template <class PDE, int threads>
 struct CellLaneMinBlocks<PDE, threads, std::void_t<decltype(PDE::cell_lane_min_blocks)>> {
