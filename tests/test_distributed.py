@@ -37,7 +37,7 @@ def _worker(rank, world, port, results, fail_rank):
 
 def _run(world, fail_rank=-1):
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         results = m.dict()
         mp.spawn(_worker, args=(world, port, results, fail_rank), nprocs=world, join=True)
         return dict(results)

@@ -163,7 +163,7 @@ def _worker(rank, world, port, which, results):
 def test_two_gloo_ranks_match_global(which):
     from oracle import pyoracle as po
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         results = m.dict()
         mp.spawn(_worker, args=(world, _free_port(), which, results), nprocs=world, join=True)
         res = dict(results)
@@ -255,7 +255,7 @@ def _linear_worker(rank, world, port, tolerance_type, preconditioner, results):
 @pytest.mark.parametrize("tolerance_type,preconditioner", [(0, 0), (1, 1)])
 def test_two_gloo_ranks_sharded_cg_matches_global(tolerance_type, preconditioner):
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         results = m.dict()
         mp.spawn(_linear_worker, args=(world, _free_port(), tolerance_type, preconditioner, results), nprocs=world,
                  join=True)
